@@ -1,0 +1,175 @@
+/*
+ * care_gpu.h -- C ABI of the GB300-native CARE read error-correction engine.
+ *
+ * This is the boundary that replaces the CPU engine below RabbitQCPlus's
+ * CARE entry points
+ *     void care::performCorrection(care::ProgramOptions)
+ *     void care::performCorrectionOutToQueue(care::ProgramOptions, Q1, Q2,
+ *                                            producerDone, careStartWrite, changNum)
+ * (reference: include/dispatch_care_correct_cpu.hpp:9-11,
+ *  src/dispatch_care_correct_cpu.cpp:52-249 and 254-457).  Those two C++
+ * functions are re-implemented on top of this ABI by the host layer
+ * (rabbitqcplus_gb300/csrc/host/care_host.cpp, declared in care_host.h); a
+ * RabbitQCPlus build links that object in place of dispatch_care_correct_cpu.o.
+ *
+ * Rules of the ABI: plain pointers and sizes only; every call returns a status
+ * code (CG_OK == 0) and never aborts the process; device memory belongs to the
+ * context, host buffers belong to the caller; one context drives one GPU and
+ * calls on one context must be serialised by the caller.
+ */
+#ifndef CARE_GPU_H
+#define CARE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define CG_OK 0
+#define CG_ERR_INVALID_ARGUMENT 1
+#define CG_ERR_UNSUPPORTED 2
+#define CG_ERR_CUDA 3
+#define CG_ERR_OUT_OF_MEMORY 4
+#define CG_ERR_STATE 5
+#define CG_ERR_IO 6
+#define CG_ERR_TIMEOUT 7
+
+/* maximum number of minhash maps (reference: include/config.hpp:30) */
+#define CG_MAX_HASHMAPS 48
+/* longest read the device kernels accept */
+#define CG_MAX_READ_LENGTH 1024
+
+#define CG_PAIR_SE 0
+#define CG_PAIR_PE 1
+
+/* correction decision (reference: include/options.hpp:23-28, CorrectionType) */
+#define CG_CORR_CLASSIC 0
+#define CG_CORR_FOREST 1
+#define CG_CORR_PRINT 2
+#define CG_CORR_LEARNED 3
+
+/* per-anchor result flags */
+#define CG_RESULT_CORRECTED 1u /* anchor has a correction (TempCorrectedSequence exists) */
+#define CG_RESULT_HQ 2u        /* MSA properties marked the anchor high quality */
+
+/*
+ * Options: the fields of care::ProgramOptions that change what the correction
+ * path computes (reference: include/options.hpp:36-99, parsed in
+ * src/options.cpp:55-390).  cg_default_options gives the reference defaults
+ * except estimated_coverage, which the caller sets from --coverage.
+ */
+typedef struct cg_options {
+    int32_t kmerlength;               /* kmerlength; 0 = autodetect (20 if max read length < 160, else 32) */
+    int32_t num_hash_functions;       /* numHashFunctions, 1..48 */
+    float estimated_coverage;         /* estimatedCoverage (--coverage) */
+    float estimated_errorrate;        /* estimatedErrorrate (0.06) */
+    float m_coverage;                 /* m_coverage (0.6) */
+    float max_error_rate;             /* maxErrorRate (0.2) */
+    float min_overlap_ratio;          /* min_overlap_ratio (0.3) */
+    int32_t min_overlap;              /* min_overlap (30) */
+    float paired_filter_threshold;    /* pairedFilterThreshold (0.06) */
+    int32_t new_columns_to_correct;   /* new_columns_to_correct (15) */
+    int32_t use_quality_scores;       /* useQualityScores */
+    int32_t exclude_ambiguous_reads;  /* excludeAmbiguousReads */
+    int32_t correct_candidates;       /* correctCandidates (not supported: CG_ERR_UNSUPPORTED) */
+    int32_t pair_mode;                /* CG_PAIR_SE / CG_PAIR_PE (pairType) */
+    int32_t correction_type;          /* CG_CORR_* (correctionType) */
+    float threshold_anchor;           /* thresholdAnchor for the learned decision (0.5) */
+    int32_t device;                   /* CUDA device ordinal */
+    int32_t batch_anchors;            /* anchors per device batch; 0 = automatic */
+    int32_t reserved[8];
+} cg_options;
+
+typedef struct cg_ctx cg_ctx;
+
+/* Per-run counters (reference: the per-stage counters printed by
+ * src/correct_cpu.cpp:314-345, as counts instead of times). */
+typedef struct cg_stats {
+    uint64_t num_reads;
+    uint64_t num_anchors_processed;
+    uint64_t raw_candidate_ids;       /* sum over anchors of hash-table hits */
+    uint64_t unique_candidates;       /* after sort/unique/self removal */
+    uint64_t aligned_candidates;      /* after orientation filter */
+    uint64_t msa_candidates;          /* after mismatch-ratio filter */
+    uint64_t msa_builds;              /* MSA builds including refinement rebuilds */
+    uint64_t corrected_anchors;
+    uint64_t hq_anchors;
+    uint64_t table_keys;              /* kept keys over all maps */
+    uint64_t table_values;            /* stored read ids over all maps */
+    int32_t kmerlength;               /* k in use (after autodetect) */
+    int32_t num_maps;
+    int32_t max_read_length;
+    int32_t reserved;
+    double seconds_build;             /* device time of the last cg_build_tables */
+    double seconds_correct;           /* device time of the last cg_correct */
+} cg_stats;
+
+/* Fill *o with the reference defaults. */
+void cg_default_options(cg_options* o);
+
+/* Create a context on o->device.  *out is set only on CG_OK. */
+int cg_create(const cg_options* o, cg_ctx** out);
+
+/* Release the context and all its device memory. */
+void cg_destroy(cg_ctx* ctx);
+
+/* Message of the last failing call on this context (never NULL). */
+const char* cg_last_error(const cg_ctx* ctx);
+
+/*
+ * Append reads to the device read store (reference: ChunkedReadStorage built by
+ * constructChunkedReadStorageFromFiles, include/chunkedreadstorageconstruction.hpp:29-485).
+ * `sequences` holds the reads back to back, read i at [offsets[i], offsets[i+1]).
+ * Bases are upper-cased; every other character becomes A,C,G,T in turn, the
+ * counter restarting every 65536 reads of one call (one call per input file,
+ * or per interleaved file pair), and such reads are marked ambiguous.
+ * `qualities` (same offsets, Phred+33) may be NULL unless quality scores are used.
+ * Reads get consecutive ids in call order.  Must precede cg_build_tables.
+ */
+int cg_append_reads(cg_ctx* ctx, const char* sequences, const uint64_t* offsets,
+                    const char* qualities, uint64_t num_reads);
+
+/*
+ * Build the minhash signatures and the hash tables on the device (reference:
+ * constructCpuMinhasherFromCpuReadStorage, src/cpuminhasherconstruction.cpp:27-212,
+ * OrdinaryCpuMinhasher::insert/compact, include/ordinaryminhasher.hpp:223-254,376-426).
+ */
+int cg_build_tables(cg_ctx* ctx);
+
+/*
+ * Correct anchors [first_read, first_read + num_anchors) (reference: the body of
+ * cpu::correct_cpu, src/correct_cpu.cpp:47-348, per anchor
+ * CpuErrorCorrector::process / processMulti, include/corrector.hpp:145-513).
+ * For anchor j of the range: out_flags[j] gets CG_RESULT_* bits and, when
+ * CG_RESULT_CORRECTED is set, out_sequences[j * out_pitch .. + length) gets the
+ * corrected bases as 'A','C','G','T' (reference: TempCorrectedSequence::sequence).
+ * In paired mode first_read and num_anchors must be even.
+ */
+int cg_correct(cg_ctx* ctx, uint64_t first_read, uint64_t num_anchors,
+               uint8_t* out_flags, char* out_sequences, size_t out_pitch);
+
+/* Counters of the context so far. */
+int cg_get_stats(const cg_ctx* ctx, cg_stats* out);
+
+/* Number of reads in the store, longest read length. */
+int cg_get_read_info(const cg_ctx* ctx, uint64_t* num_reads, int32_t* max_length);
+
+/*
+ * Stage access for tests and tools (device results copied to host):
+ *  cg_get_signatures:  num_maps keys of each read in [first, first+n), read-major
+ *                      (reference: CPUSequenceHasher::hashInto, include/cpusequencehasher.hpp:86-125)
+ *  cg_get_candidates:  candidate ids of one anchor after sort/unique/self removal
+ *                      (reference: determineCandidateReadIds, include/corrector.hpp:571-650);
+ *                      *count gets the number, at most `capacity` are written.
+ */
+int cg_get_signatures(cg_ctx* ctx, uint64_t first, uint64_t n, uint64_t* out);
+int cg_get_candidates(cg_ctx* ctx, uint64_t anchor, uint32_t* out, uint32_t capacity, uint32_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CARE_GPU_H */

@@ -1,0 +1,808 @@
+// ORACLE -- test infrastructure, not product code.
+//
+// A plain C++ restatement of the reference CARE correction path (RabbitQCPlus
+// --correctWithCare, correctionType Classic) used only as the checker of the
+// GPU path in tests/, in __graft_entry__.smoke() and as bench.py's CPU
+// baseline.  The product library never links or calls it.
+//
+// Parity pin: its outputs are checked against fixtures produced by the
+// reference itself (oracle/ref.mk builds the reference's own sources here;
+// tests/golden/make_golden.py runs them), see tests/test_oracle_golden.py.
+//
+// Each function names the reference code it restates (paths relative to the
+// reference project).  Floating-point expressions keep the reference's
+// operand order; the file is compiled as ISO C++17 with -ffp-contract=off, as
+// the reference is.
+
+#include <care_gpu.h>
+
+#include <omp.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------- helpers
+
+// reference: include/hostdevicefunctions.cuh:9-28 (feq / fleq / fgeq)
+inline bool feq(float l, float r) {
+    const float d = l - r < 0 ? -(l - r) : l - r;
+    return d < 1e-5f;
+}
+inline bool fleq(float l, float r) { return (l < r) || feq(l, r); }
+inline bool fgeq(float l, float r) { return (l > r) || feq(l, r); }
+
+// reference: include/hpc_helpers/include/hashers.cuh:129-136 (64-bit Murmur finalizer)
+inline uint64_t murmur64(uint64_t x) {
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ull;
+    x ^= x >> 33;
+    return x;
+}
+
+inline int sdiv(int a, int b) { return (a + b - 1) / b; }
+
+const char kBase[4] = {'A', 'C', 'G', 'T'};
+
+inline uint32_t baseCode(char c) {
+    switch (c) {
+        case 'A': return 0;
+        case 'C': return 1;
+        case 'G': return 2;
+        case 'T': return 3;
+        default: return 0;
+    }
+}
+
+inline char complementChar(char c) {
+    switch (c) {
+        case 'A': return 'T';
+        case 'C': return 'G';
+        case 'G': return 'C';
+        case 'T': return 'A';
+        default: return c;
+    }
+}
+
+// reference: include/sequencehelpers.hpp:151-186 (encodeSequence2Bit):
+// 16 bases per 32-bit word, first base in the two most significant bits,
+// the last word left-aligned.
+void encode2bit(uint32_t* out, const char* s, int len) {
+    const int words = sdiv(len, 16);
+    for (int w = 0; w < words; w++) out[w] = 0;
+    for (int i = 0; i < len; i++) out[i / 16] |= baseCode(s[i]) << (30 - 2 * (i % 16));
+}
+
+inline uint32_t get2bit(const uint32_t* enc, int i) { return (enc[i / 16] >> (30 - 2 * (i % 16))) & 3u; }
+
+void decode2bit(char* out, const uint32_t* enc, int len) {
+    for (int i = 0; i < len; i++) out[i] = kBase[get2bit(enc, i)];
+}
+
+// reference: include/sequencehelpers.hpp:645-691 (convert2BitTo2BitHiLo):
+// hi plane = high bit of each base code, lo plane = low bit, 32 bases per
+// word, first base in the most significant bit.
+void toHiLo(uint32_t* hi, uint32_t* lo, const uint32_t* enc, int len, int wordsPerPlane) {
+    for (int w = 0; w < wordsPerPlane; w++) hi[w] = lo[w] = 0;
+    for (int i = 0; i < len; i++) {
+        const uint32_t b = get2bit(enc, i);
+        hi[i / 32] |= (b >> 1) << (31 - (i % 32));
+        lo[i / 32] |= (b & 1u) << (31 - (i % 32));
+    }
+}
+
+// ---------------------------------------------------------------- read store
+
+struct Store {
+    uint64_t n = 0;
+    int Lmax = 0;
+    int pitch = 0;  // words of 16 bases per read
+    std::vector<uint32_t> enc;
+    std::vector<int> len;
+    std::vector<char> qual;  // n * Lmax
+    std::vector<uint8_t> ambig;
+    bool hasQual = false;
+};
+
+struct Tables {
+    int k = 20;
+    int nmaps = 48;
+    int maxValuesPerKey = 75;
+    uint64_t kmask = 0;
+    // per map: sorted unique kept keys, their value ranges, and the values
+    std::vector<std::vector<uint64_t>> keys;
+    std::vector<std::vector<uint32_t>> begin;
+    std::vector<std::vector<uint32_t>> count;
+    std::vector<std::vector<uint32_t>> values;
+    std::vector<uint64_t> sigs;  // n * nmaps (read-major)
+};
+
+struct Oracle {
+    cg_options o;
+    Store s;
+    Tables t;
+    float qweight[256];
+    double buildSeconds = 0;
+};
+
+// reference: include/cpusequencehasher.hpp:86-125 (hashInto) with the canonical
+// k-mer walk of include/sequencehelpers.hpp:842-930: for each hash function h,
+// the minimum over canonical k-mers of murmur64(kmer + h), masked to 2k bits.
+// Reads shorter than k keep the all-ones value (masked).
+void signature(const uint32_t* enc, int len, int k, int nmaps, uint64_t* out) {
+    const uint64_t kmask = k == 32 ? ~0ull : ((1ull << (2 * k)) - 1);
+    uint64_t mins[CG_MAX_HASHMAPS];
+    for (int h = 0; h < nmaps; h++) mins[h] = ~0ull;
+    if (len >= k) {
+        uint64_t fwd = 0, rc = 0;
+        for (int i = 0; i < len; i++) {
+            const uint64_t b = get2bit(enc, i);
+            fwd = ((fwd << 2) | b) & kmask;
+            rc = (rc >> 2) | ((3ull - b) << (2 * (k - 1)));
+            if (i >= k - 1) {
+                const uint64_t canon = std::min(fwd, rc);
+                for (int h = 0; h < nmaps; h++) mins[h] = std::min(mins[h], murmur64(canon + uint64_t(h)));
+            }
+        }
+    }
+    for (int h = 0; h < nmaps; h++) out[h] = mins[h] & kmask;
+}
+
+// reference: include/chunkedreadstorageconstruction.hpp:67-92 (preprocessSequence),
+// :243-282 (the encoder loop: the round-robin counter restarts for every batch of
+// 65536 parsed reads) and include/qualityscorecompression.hpp:337 (8-bit
+// qualities are stored unchanged).
+void buildStore(Oracle& O, const char* seqs, const uint64_t* offs, const char* quals, uint64_t n) {
+    Store& s = O.s;
+    s.n = n;
+    s.Lmax = 0;
+    for (uint64_t i = 0; i < n; i++) s.Lmax = std::max<int>(s.Lmax, int(offs[i + 1] - offs[i]));
+    s.pitch = sdiv(std::max(s.Lmax, 1), 16);
+    s.enc.assign(n * s.pitch, 0);
+    s.len.resize(n);
+    s.ambig.assign(n, 0);
+    s.hasQual = quals != nullptr;
+    if (s.hasQual) s.qual.assign(n * size_t(s.Lmax), 0);
+    int Ncount = 0;
+    std::string tmp;
+    for (uint64_t i = 0; i < n; i++) {
+        if (i % 65536 == 0) Ncount = 0;
+        const int L = int(offs[i + 1] - offs[i]);
+        tmp.assign(seqs + offs[i], L);
+        bool amb = false;
+        for (auto& c : tmp) {
+            if (c == 'a') c = 'A';
+            else if (c == 'c') c = 'C';
+            else if (c == 'g') c = 'G';
+            else if (c == 't') c = 'T';
+            else if (c != 'A' && c != 'C' && c != 'G' && c != 'T') {
+                c = kBase[Ncount];
+                Ncount = (Ncount + 1) % 4;
+                amb = true;
+            }
+        }
+        s.len[i] = L;
+        s.ambig[i] = amb;
+        encode2bit(&s.enc[i * s.pitch], tmp.data(), L);
+        if (s.hasQual) std::memcpy(&s.qual[i * size_t(s.Lmax)], quals + offs[i], L);
+    }
+}
+
+// reference: src/cpuminhasherconstruction.cpp:27-165 with
+// include/ordinaryminhasher.hpp:376-426 (insert), :223-254 (compact) and
+// include/groupbykey.hpp:69-250: per map, (key, readId) pairs grouped by key,
+// read ids ascending; keys with fewer than 2 or more than maxValuesPerKey ids
+// keep no values.  maxValuesPerKey = calculateResultsPerMapThreshold(int(coverage))
+// (include/minhasherlimit.hpp:9-15).
+void buildTables(Oracle& O, int threads) {
+    const Store& s = O.s;
+    Tables& t = O.t;
+    t.k = O.o.kmerlength;
+    if (t.k == 0) t.k = s.Lmax < 160 ? 20 : 32;  // src/dispatch_care_correct_cpu.cpp:81-95
+    t.nmaps = O.o.num_hash_functions;
+    t.kmask = t.k == 32 ? ~0ull : ((1ull << (2 * t.k)) - 1);
+    {
+        const int cov = int(O.o.estimated_coverage);
+        int r = int(cov * 2.5f);
+        r = std::min(r, 65535);
+        r = std::max(10, r);
+        t.maxValuesPerKey = r;
+    }
+    t.sigs.resize(s.n * t.nmaps);
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1024)
+    for (int64_t i = 0; i < int64_t(s.n); i++) {
+        signature(&s.enc[i * s.pitch], s.len[i], t.k, t.nmaps, &t.sigs[i * t.nmaps]);
+    }
+    t.keys.assign(t.nmaps, {});
+    t.begin.assign(t.nmaps, {});
+    t.count.assign(t.nmaps, {});
+    t.values.assign(t.nmaps, {});
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1)
+    for (int h = 0; h < t.nmaps; h++) {
+        std::vector<std::pair<uint64_t, uint32_t>> kv(s.n);
+        for (uint64_t i = 0; i < s.n; i++) kv[i] = {t.sigs[i * t.nmaps + h], uint32_t(i)};
+        std::sort(kv.begin(), kv.end());
+        const uint32_t upper = uint32_t(std::min(t.maxValuesPerKey, 65535));
+        for (uint64_t a = 0; a < kv.size();) {
+            uint64_t b = a;
+            while (b < kv.size() && kv[b].first == kv[a].first) b++;
+            const uint64_t num = b - a;
+            if (num >= 2 && num <= upper) {
+                t.keys[h].push_back(kv[a].first);
+                t.begin[h].push_back(uint32_t(t.values[h].size()));
+                t.count[h].push_back(uint32_t(num));
+                for (uint64_t j = a; j < b; j++) t.values[h].push_back(kv[j].second);
+            }
+            a = b;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- alignment
+
+struct Aln {
+    int score, overlap, shift, nOps;
+    bool isValid;
+};
+
+// reference: src/cpu_alignment.cpp:32-497 (cpuShiftedHammingDistancePopcount2BitHiLo):
+// right shifts 0..La-minov (anchor shifted), then left shifts -1..-(Lc-minov)
+// (candidate shifted); per shift the mismatch count over the overlap, the
+// first shift with the smallest score wins; each direction stops once no later
+// shift can win (max_errors <= 0).
+Aln align(const uint32_t* aHi, const uint32_t* aLo, int La, const uint32_t* cHi, const uint32_t* cLo, int Lc,
+          int min_overlap, float maxErrorRate, float min_overlap_ratio) {
+    const int totalbases = La + Lc;
+    const int minoverlap = std::max(min_overlap, int(float(La) * min_overlap_ratio));
+    int bestScore = totalbases;
+    int bestShift = -Lc;
+    auto mismatches = [&](const uint32_t* shHi, const uint32_t* shLo, int shiftLen, const uint32_t* oHi,
+                          const uint32_t* oLo, int ov, int maxErrors) {
+        const int parts = (ov + 31) >> 5;
+        const int rem = (parts << 5) - ov;
+        const int ws = shiftLen >> 5, bs = shiftLen & 31;
+        int result = 0;
+        auto word = [&](const uint32_t* p, int i) {
+            const uint32_t a = p[i + ws] << bs;
+            const uint32_t b = bs == 0 ? 0u : (p[i + ws + 1] >> (32 - bs));
+            return a | b;
+        };
+        for (int i = 0; i < parts - 1 && result < maxErrors; i++) {
+            result += __builtin_popcount((word(shHi, i) ^ oHi[i]) | (word(shLo, i) ^ oLo[i]));
+        }
+        if (result < maxErrors) {
+            const uint32_t mask = rem == 0 ? 0xFFFFFFFFu : 0xFFFFFFFFu << rem;
+            result += __builtin_popcount(((word(shHi, parts - 1) ^ oHi[parts - 1]) |
+                                          (word(shLo, parts - 1) ^ oLo[parts - 1])) & mask);
+        }
+        return result;
+    };
+    for (int shift = 0; shift < La - minoverlap + 1; ++shift) {
+        const int ov = std::min(La - shift, Lc);
+        const int maxErr = std::min(int(float(ov) * maxErrorRate), bestScore - totalbases + 2 * ov);
+        if (maxErr <= 0) break;
+        const int m = mismatches(aHi, aLo, shift, cHi, cLo, ov, maxErr);
+        const int score = m < maxErr ? m + totalbases - 2 * ov : std::numeric_limits<int>::max();
+        if (score < bestScore) {
+            bestScore = score;
+            bestShift = shift;
+        }
+    }
+    for (int shift = -1; shift >= -Lc + minoverlap; --shift) {
+        const int ov = std::min(La, Lc + shift);
+        const int maxErr = std::min(int(float(ov) * maxErrorRate), bestScore - totalbases + 2 * ov);
+        if (maxErr <= 0) break;
+        const int m = mismatches(cHi, cLo, -shift, aHi, aLo, ov, maxErr);
+        const int score = m < maxErr ? m + totalbases - 2 * ov : std::numeric_limits<int>::max();
+        if (score < bestScore) {
+            bestScore = score;
+            bestShift = shift;
+        }
+    }
+    Aln r;
+    r.isValid = bestShift != -Lc;
+    const int cb = std::max(-bestShift, 0);
+    const int ce = std::min(Lc, La - bestShift);
+    const int ov = ce - cb;
+    r.score = bestScore;
+    r.overlap = ov;
+    r.shift = bestShift;
+    r.nOps = bestScore - totalbases + 2 * ov;
+    return r;
+}
+
+// reference: include/alignmentorientation.hpp:10-92 (chooseBestAlignmentOrientation):
+// 1 = forward, 2 = reverse complement, 3 = none
+int orientation(const Aln& f, const Aln& r, int La, float min_overlap_ratio, int min_overlap, float maxErrorRate) {
+    const int minimumOverlap = int(La * min_overlap_ratio) > min_overlap ? int(La * min_overlap_ratio) : min_overlap;
+    int ret = 3;
+    if (f.isValid && f.overlap >= minimumOverlap) {
+        if (r.isValid && r.overlap >= minimumOverlap) {
+            const float ratio = (float)f.nOps / f.overlap;
+            const float revcomplratio = (float)r.nOps / r.overlap;
+            if (ratio < revcomplratio) {
+                if (ratio < maxErrorRate) ret = 1;
+            } else if (revcomplratio < ratio) {
+                if (revcomplratio < maxErrorRate) ret = 2;
+            } else {
+                if (ratio < maxErrorRate) ret = f.overlap > r.overlap ? 1 : 2;
+            }
+        } else {
+            if ((float)f.nOps / f.overlap < maxErrorRate) ret = 1;
+        }
+    } else {
+        if (r.isValid && r.overlap >= minimumOverlap) {
+            if ((float)r.nOps / r.overlap < maxErrorRate) ret = 2;
+        }
+    }
+    return ret;
+}
+
+// ---------------------------------------------------------------- MSA
+
+struct Cand {
+    uint32_t id;
+    int len;
+    int orient;  // 1 fwd, 2 rc
+    Aln aln;
+    bool paired;
+    float weight;
+    std::string seq;   // bases in aligned orientation
+    std::string qual;  // qualities in aligned orientation (reversed for rc)
+};
+
+struct Msa {
+    int nColumns = 0, begin = 0, end = 0, nCand = 0;
+    std::vector<int> cA, cC, cG, cT, cov, origCov;
+    std::vector<float> wA, wC, wG, wT, support, origW;
+    std::string cons;
+};
+
+// reference: src/msa.cpp:9-173 (build, addSequence, findConsensus,
+// findOrigWeightAndCoverage).  Column weights are accumulated anchor first,
+// then candidates in list order.
+void buildMsa(Msa& m, const std::string& anchor, const std::string& aqual, const std::vector<Cand>& cs,
+              bool useQ, const float* qw) {
+    int startindex = 0, endindex = int(anchor.size());
+    for (const auto& c : cs) {
+        startindex = std::min(c.aln.shift, startindex);
+        endindex = std::max(c.len + c.aln.shift, endindex);
+    }
+    m.nColumns = endindex - startindex;
+    m.begin = std::max(-startindex, 0);
+    m.end = m.begin + int(anchor.size());
+    m.nCand = int(cs.size());
+    const int C = m.nColumns;
+    for (auto* v : {&m.cA, &m.cC, &m.cG, &m.cT, &m.cov, &m.origCov}) v->assign(C, 0);
+    for (auto* v : {&m.wA, &m.wC, &m.wG, &m.wT, &m.support, &m.origW}) v->assign(C, 0.0f);
+    m.cons.assign(C, 0);
+    auto add = [&](const std::string& seq, const std::string& q, int shift, float f) {
+        for (int i = 0; i < int(seq.size()); i++) {
+            const int g = m.begin + shift + i;
+            const float w = f * (useQ ? qw[(unsigned char)q[i]] : 1.0f);
+            switch (seq[i]) {
+                case 'A': m.cA[g]++; m.wA[g] += w; break;
+                case 'C': m.cC[g]++; m.wC[g] += w; break;
+                case 'G': m.cG[g]++; m.wG[g] += w; break;
+                case 'T': m.cT[g]++; m.wT[g] += w; break;
+            }
+            m.cov[g]++;
+        }
+    };
+    add(anchor, aqual, 0, 1.0f);
+    for (const auto& c : cs) add(c.seq, c.qual, c.aln.shift, c.weight);
+    for (int col = 0; col < C; col++) {
+        char cons = 'A';
+        float cw = m.wA[col];
+        if (m.wC[col] > cw) { cons = 'C'; cw = m.wC[col]; }
+        if (m.wG[col] > cw) { cons = 'G'; cw = m.wG[col]; }
+        if (m.wT[col] > cw) { cons = 'T'; cw = m.wT[col]; }
+        m.cons[col] = cons;
+        const float colW = m.wA[col] + m.wC[col] + m.wG[col] + m.wT[col];
+        m.support[col] = cw / colW;
+    }
+    for (int col = m.begin; col < m.end; col++) {
+        switch (anchor[col - m.begin]) {
+            case 'A': m.origW[col] = m.wA[col]; m.origCov[col] = m.cA[col]; break;
+            case 'C': m.origW[col] = m.wC[col]; m.origCov[col] = m.cC[col]; break;
+            case 'G': m.origW[col] = m.wG[col]; m.origCov[col] = m.cG[col]; break;
+            case 'T': m.origW[col] = m.wT[col]; m.origCov[col] = m.cT[col]; break;
+        }
+    }
+}
+
+// reference: src/msa.cpp:532-734 (findCandidatesOfDifferentRegion); returns
+// false when no minimization is performed, else fills `remove`.
+bool differentRegion(const Msa& m, const std::string& anchor, const std::vector<Cand>& cs, int datasetCoverage,
+                     std::vector<char>& remove) {
+    if (anchor.compare(0, anchor.size(), m.cons, m.begin, anchor.size()) == 0) return false;
+    const int thr = int(datasetCoverage * 0.3f);
+    int col = -1, foundIdx = -1, consIdx = -1;
+    for (int c = m.begin; c < m.end && col < 0; c++) {
+        const int counts[4] = {m.cA[c], m.cC[c], m.cG[c], m.cT[c]};
+        const char cons = m.cons[c];
+        consIdx = cons == 'A' ? 0 : cons == 'C' ? 1 : cons == 'G' ? 2 : 3;
+        int sig = -1;
+        for (int i = 0; i < 4; i++)
+            if (i != consIdx && thr <= counts[i]) sig = i;
+        if (sig != -1) {
+            col = c;
+            foundIdx = sig;
+        }
+    }
+    if (col < 0) return false;
+    const char foundBase = kBase[foundIdx];
+    const char origBase = anchor[col - m.begin];
+    const bool keepMatching = origBase == foundBase;
+    remove.assign(cs.size(), 0);
+    for (size_t i = 0; i < cs.size(); i++) {
+        const int rb = m.begin + cs[i].aln.shift;
+        const int re = rb + cs[i].len;
+        if (col < rb || re <= col) continue;
+        const char b = cs[i].seq[col - rb];
+        if (keepMatching ? (b != foundBase) : (b == foundBase)) remove[i] = 1;
+    }
+    for (size_t i = 0; i < cs.size(); i++) {
+        if (remove[i] && cs[i].weight >= 0.90f) {
+            std::fill(remove.begin(), remove.end(), 0);
+            break;
+        }
+    }
+    return true;
+}
+
+struct Props {
+    float avg_support, min_support;
+    int min_coverage, max_coverage;
+    bool isHQ;
+};
+
+// reference: src/msa.cpp:304-376 (getMSAProperties)
+Props msaProperties(const Msa& m, float err, float cov, float mcov) {
+    const float avgThr = 1.0f - 1.0f * err;
+    const float minThr = 1.0f - 3.0f * err;
+    const float covThr = mcov / 6.0f * cov;
+    const int first = m.begin, last = m.end, dist = last - first;
+    Props p;
+    p.min_support = *std::min_element(m.support.begin() + first, m.support.begin() + last);
+    float sum = 0.0f;
+    for (int c = first; c < last; c++) sum += m.support[c];
+    p.avg_support = sum / dist;
+    p.min_coverage = *std::min_element(m.cov.begin() + first, m.cov.begin() + last);
+    p.max_coverage = *std::max_element(m.cov.begin() + first, m.cov.begin() + last);
+    p.isHQ = false;
+    const bool allGood = fgeq(p.avg_support, avgThr) && fgeq(p.min_support, minThr) && fgeq(float(p.min_coverage), covThr);
+    if (allGood) {
+        int smallest = 100;
+        const int pct = int(std::ceil(err * 100.0f));
+        for (int percent = pct; percent >= 0; percent--) {
+            const float factor = percent / 100.0f;
+            if (fgeq(p.avg_support, 1.0f - 1.0f * factor) && fgeq(p.min_support, 1.0f - 3.0f * factor)) smallest = percent;
+        }
+        p.isHQ = fgeq(float(p.min_coverage), covThr) && fleq(float(smallest), pct * 0.5f);
+    }
+    return p;
+}
+
+// reference: src/msa.cpp:379-453 (getCorrectedAnchor)
+bool correctedAnchor(const Msa& m, const Props& p, const std::string& anchor, float err, float cov, float mcov,
+                     std::string& out) {
+    if (m.nCand == 0) return false;
+    const float avgThr = 1.0f - 1.0f * err;
+    const float minThr = 1.0f - 3.0f * err;
+    const float covThr = mcov / 6.0f * cov;
+    const bool byConsensus = fgeq(p.avg_support, avgThr) && fgeq(p.min_support, minThr) && fgeq(float(p.min_coverage), covThr);
+    out.resize(anchor.size());
+    if (byConsensus) {
+        for (size_t i = 0; i < anchor.size(); i++) out[i] = m.cons[m.begin + i];
+    } else {
+        for (size_t i = 0; i < anchor.size(); i++) {
+            const int c = m.begin + int(i);
+            out[i] = (m.support[c] > 0.90f && m.origCov[c] <= 2) ? m.cons[c] : anchor[i];
+        }
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------- per anchor
+
+std::string decodeRead(const Store& s, uint64_t id) {
+    std::string r(s.len[id], 'A');
+    decode2bit(&r[0], &s.enc[id * s.pitch], s.len[id]);
+    return r;
+}
+
+// reference: include/corrector.hpp:571-650 (determineCandidateReadIds) with
+// include/ordinaryminhasher.hpp:135-221,437-449 (determineNumValues, retrieveValues, queryMap)
+void candidates(const Oracle& O, uint64_t anchor, std::vector<uint32_t>& out, uint64_t* rawCount) {
+    const Store& s = O.s;
+    const Tables& t = O.t;
+    out.clear();
+    if (O.o.exclude_ambiguous_reads && s.ambig[anchor]) return;
+    if (s.len[anchor] >= t.k) {
+        const uint64_t* sig = &t.sigs[anchor * t.nmaps];
+        for (int h = 0; h < t.nmaps; h++) {
+            const auto& ks = t.keys[h];
+            auto it = std::lower_bound(ks.begin(), ks.end(), sig[h]);
+            if (it != ks.end() && *it == sig[h]) {
+                const size_t j = it - ks.begin();
+                if (int(t.count[h][j]) > t.maxValuesPerKey) continue;
+                out.insert(out.end(), t.values[h].begin() + t.begin[h][j],
+                           t.values[h].begin() + t.begin[h][j] + t.count[h][j]);
+            }
+        }
+    }
+    if (rawCount) *rawCount += out.size();
+    std::sort(out.begin(), out.end());
+    out.erase(std::unique(out.begin(), out.end()), out.end());
+    auto it = std::lower_bound(out.begin(), out.end(), uint32_t(anchor));
+    if (it != out.end() && *it == uint32_t(anchor)) out.erase(it);
+    if (O.o.exclude_ambiguous_reads) {
+        out.erase(std::remove_if(out.begin(), out.end(), [&](uint32_t c) { return s.ambig[c] != 0; }), out.end());
+    }
+}
+
+// reference: include/util.hpp:1005-1143 (flagPairedCandidates via
+// findPositionsOfPairedReadIds, :1151-1200): positions of ids in range 1 whose
+// mate (id/2 equal) is in range 2 and vice versa.
+void pairFlags(const std::vector<uint32_t>& r1, const std::vector<uint32_t>& r2, std::vector<char>& f1,
+               std::vector<char>& f2) {
+    f1.assign(r1.size(), 0);
+    f2.assign(r2.size(), 0);
+    size_t a = 0, b = 0;
+    while (a < r1.size() && b < r2.size()) {
+        const int e1 = (a + 1 < r1.size() && r1[a] / 2 == r1[a + 1] / 2) ? 2 : 1;
+        const int e2 = (b + 1 < r2.size() && r2[b] / 2 == r2[b + 1] / 2) ? 2 : 1;
+        const bool same = r1[a] / 2 == r2[b] / 2;
+        if (e1 == 1 && e2 == 1) {
+            if (same) {
+                if (r1[a] != r2[b]) { f1[a] = 1; f2[b] = 1; }
+                a++; b++;
+            } else {
+                if (r1[a] < r2[b]) a++; else b++;
+            }
+        } else if (e1 == 2 && e2 == 2) {
+            if (same) {
+                f1[a] = 1; f2[b] = 1; f1[a + 1] = 1; f2[b + 1] = 1;
+                a += 2; b += 2;
+            } else {
+                if (r1[a] < r2[b]) a += 2; else b += 2;
+            }
+        } else if (e1 == 2 && e2 == 1) {
+            if (same) {
+                if (r1[a] == r2[b]) { a++; f1[a] = 1; f2[b] = 1; a++; b++; }
+                else { f1[a] = 1; f2[b] = 1; a++; b++; a++; }
+            } else {
+                if (r1[a] < r2[b]) a += 2; else b++;
+            }
+        } else {
+            if (same) {
+                if (r1[a] == r2[b]) { b++; f1[a] = 1; f2[b] = 1; a++; b++; }
+                else { f1[a] = 1; f2[b] = 1; a++; b++; b++; }
+            } else {
+                if (r1[a] < r2[b]) a++; else b += 2;
+            }
+        }
+    }
+}
+
+struct Counters {
+    uint64_t raw = 0, uniq = 0, aligned = 0, msaCands = 0, msaBuilds = 0, corrected = 0, hq = 0;
+};
+
+// reference: include/corrector.hpp:145-312 (process) and 325-513 (processMulti):
+// candidates -> alignments -> orientation -> filters -> MSA -> refinement ->
+// anchor correction.  Returns the CG_RESULT_* flags.
+uint8_t correctOne(const Oracle& O, uint64_t anchor, const std::vector<uint32_t>& candIds,
+                   const std::vector<char>& paired, std::string& corrected, Counters& cnt) {
+    const Store& s = O.s;
+    const cg_options& o = O.o;
+    const int La = s.len[anchor];
+    const int W = sdiv(s.Lmax, 32) + 1;
+    if (candIds.empty()) return 0;
+    cnt.uniq += candIds.size();
+    std::vector<uint32_t> aHi(W), aLo(W), cHi(W), cLo(W), rHi(W), rLo(W);
+    toHiLo(aHi.data(), aLo.data(), &s.enc[anchor * s.pitch], La, W);
+    const std::string anchorStr = decodeRead(s, anchor);
+    std::string anchorQ;
+    if (o.use_quality_scores) anchorQ.assign(&s.qual[anchor * size_t(s.Lmax)], La);
+    std::vector<Cand> cs;
+    std::vector<uint32_t> rcEnc(s.pitch);
+    for (size_t i = 0; i < candIds.size(); i++) {
+        const uint32_t id = candIds[i];
+        const int Lc = s.len[id];
+        const uint32_t* enc = &s.enc[id * s.pitch];
+        toHiLo(cHi.data(), cLo.data(), enc, Lc, W);
+        std::string fwd = decodeRead(s, id);
+        std::string rcs(Lc, 'A');
+        for (int p = 0; p < Lc; p++) rcs[p] = complementChar(fwd[Lc - 1 - p]);
+        encode2bit(rcEnc.data(), rcs.data(), Lc);
+        toHiLo(rHi.data(), rLo.data(), rcEnc.data(), Lc, W);
+        const Aln f = align(aHi.data(), aLo.data(), La, cHi.data(), cLo.data(), Lc, o.min_overlap, o.max_error_rate, o.min_overlap_ratio);
+        const Aln r = align(aHi.data(), aLo.data(), La, rHi.data(), rLo.data(), Lc, o.min_overlap, o.max_error_rate, o.min_overlap_ratio);
+        const int ori = orientation(f, r, La, o.min_overlap_ratio, o.min_overlap, o.estimated_errorrate * 4.0f);
+        if (ori == 3) continue;
+        Cand c;
+        c.id = id;
+        c.len = Lc;
+        c.orient = ori;
+        c.aln = ori == 1 ? f : r;
+        c.paired = paired.empty() ? false : paired[i] != 0;
+        c.seq = ori == 1 ? fwd : rcs;
+        if (o.use_quality_scores) {
+            c.qual.assign(&s.qual[id * size_t(s.Lmax)], Lc);
+            if (ori == 2) std::reverse(c.qual.begin(), c.qual.end());
+        }
+        cs.push_back(std::move(c));
+    }
+    cnt.aligned += cs.size();
+    if (cs.empty()) return 0;
+    // mismatch ratio filter: include/corrector.hpp:1053-1149 (SE), 1151-1211 (PE)
+    std::vector<Cand> kept;
+    if (o.pair_mode == CG_PAIR_PE) {
+        for (auto& c : cs) {
+            if (c.paired) kept.push_back(std::move(c));
+            else if (float(c.aln.nOps) / float(c.aln.overlap) < o.paired_filter_threshold) kept.push_back(std::move(c));
+        }
+    } else {
+        const float base = o.estimated_errorrate * 1.0f;
+        const float goodThr = o.estimated_coverage * o.m_coverage;
+        int counts[3] = {0, 0, 0};
+        for (const auto& c : cs) {
+            const float r = float(c.aln.nOps) / float(c.aln.overlap);
+            if (r < 2 * base) counts[0]++;
+            if (r < 3 * base) counts[1]++;
+            if (r < 4 * base) counts[2]++;
+        }
+        float thr = std::numeric_limits<float>::lowest();
+        if (counts[0] > 0 || counts[1] > 0 || counts[2] > 0) {
+            if (counts[0] >= goodThr) thr = 2 * base;
+            else if (counts[1] >= goodThr) thr = 3 * base;
+            else if (counts[2] >= goodThr) thr = 4 * base;
+        }
+        for (auto& c : cs) {
+            if (float(c.aln.nOps) / float(c.aln.overlap) < thr) kept.push_back(std::move(c));
+        }
+    }
+    if (kept.empty()) return 0;
+    // overlap weights: include/corrector.hpp:1260-1280, include/hostdevicefunctions.cuh:93-95
+    for (auto& c : kept) c.weight = 1.0f - std::sqrt(c.aln.nOps / (c.aln.overlap * o.max_error_rate));
+    cnt.msaCands += kept.size();
+    Msa m;
+    buildMsa(m, anchorStr, anchorQ, kept, o.use_quality_scores != 0, O.qweight);
+    cnt.msaBuilds++;
+    // refinement: include/corrector.hpp:1307-1421
+    for (int it = 0; it < 5; it++) {
+        std::vector<char> remove;
+        if (!differentRegion(m, anchorStr, kept, int(o.estimated_coverage), remove)) break;
+        std::vector<Cand> next;
+        for (size_t i = 0; i < kept.size(); i++)
+            if (!remove[i]) next.push_back(std::move(kept[i]));
+        const bool changed = next.size() != kept.size();
+        kept.swap(next);
+        if (!changed) break;  // an unchanged rebuild repeats the same MSA and decision
+        buildMsa(m, anchorStr, anchorQ, kept, o.use_quality_scores != 0, O.qweight);
+        cnt.msaBuilds++;
+    }
+    // correctAnchorClassic: include/corrector.hpp:1423-1446
+    const Props p = msaProperties(m, o.estimated_errorrate, o.estimated_coverage, o.m_coverage);
+    if (!correctedAnchor(m, p, anchorStr, o.estimated_errorrate, o.estimated_coverage, o.m_coverage, corrected)) return 0;
+    cnt.corrected++;
+    if (p.isHQ) cnt.hq++;
+    return uint8_t(CG_RESULT_CORRECTED | (p.isHQ ? CG_RESULT_HQ : 0));
+}
+
+}  // namespace
+
+extern "C" {
+
+void* orc_create(const cg_options* o, const char* seqs, const uint64_t* offsets, const char* quals, uint64_t n,
+                 int threads) {
+    if (!o || !seqs || !offsets || n == 0) return nullptr;
+    if (o->use_quality_scores && !quals) return nullptr;
+    Oracle* O = new Oracle();
+    O->o = *o;
+    // reference: include/qualityscoreweights.hpp:17-33
+    for (int i = 0; i < 256; i++) {
+        const float p = i < 33 ? 1.0f : std::pow(10.0f, -(i - 33) / 10.0f);
+        O->qweight[i] = std::max(0.001f, 1.0f - p);
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    buildStore(*O, seqs, offsets, quals, n);
+    buildTables(*O, threads);
+    O->buildSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return O;
+}
+
+void orc_destroy(void* h) { delete static_cast<Oracle*>(h); }
+
+int orc_info(void* h, uint64_t* nreads, int* lmax, int* k, int* nmaps, double* buildSeconds) {
+    const Oracle* O = static_cast<Oracle*>(h);
+    *nreads = O->s.n;
+    *lmax = O->s.Lmax;
+    *k = O->t.k;
+    *nmaps = O->t.nmaps;
+    *buildSeconds = O->buildSeconds;
+    return 0;
+}
+
+int orc_signatures(void* h, uint64_t first, uint64_t n, uint64_t* out) {
+    const Oracle* O = static_cast<Oracle*>(h);
+    if (first + n > O->s.n) return CG_ERR_INVALID_ARGUMENT;
+    std::memcpy(out, &O->t.sigs[first * O->t.nmaps], n * O->t.nmaps * sizeof(uint64_t));
+    return 0;
+}
+
+int orc_candidates(void* h, uint64_t anchor, uint32_t* out, uint32_t cap, uint32_t* count) {
+    const Oracle* O = static_cast<Oracle*>(h);
+    if (anchor >= O->s.n) return CG_ERR_INVALID_ARGUMENT;
+    std::vector<uint32_t> c;
+    candidates(*O, anchor, c, nullptr);
+    *count = uint32_t(c.size());
+    std::memcpy(out, c.data(), std::min<size_t>(cap, c.size()) * 4);
+    return 0;
+}
+
+// Corrects anchors [first, first+count); flags and corrected sequences as in
+// cg_correct.  counters (7 entries, may be NULL): raw ids, unique candidates,
+// aligned, msa candidates, msa builds, corrected, hq.
+int orc_correct(void* h, uint64_t first, uint64_t count, uint8_t* flags, char* out, size_t pitch, int threads,
+                uint64_t* counters) {
+    const Oracle* O = static_cast<Oracle*>(h);
+    if (first + count > O->s.n) return CG_ERR_INVALID_ARGUMENT;
+    const bool pe = O->o.pair_mode == CG_PAIR_PE;
+    if (pe && ((first | count) & 1)) return CG_ERR_INVALID_ARGUMENT;
+    Counters total;
+    const int64_t units = int64_t(pe ? count / 2 : count);
+#pragma omp parallel num_threads(threads)
+    {
+        Counters cnt;
+        std::vector<uint32_t> c1, c2;
+        std::vector<char> f1, f2, none;
+        std::string corr;
+#pragma omp for schedule(dynamic, 8)
+        for (int64_t u = 0; u < units; u++) {
+            if (!pe) {
+                const uint64_t a = first + uint64_t(u);
+                candidates(*O, a, c1, &cnt.raw);
+                const uint8_t f = correctOne(*O, a, c1, none, corr, cnt);
+                flags[a - first] = f;
+                if (f & CG_RESULT_CORRECTED) std::memcpy(out + (a - first) * pitch, corr.data(), corr.size());
+            } else {
+                const uint64_t a = first + 2 * uint64_t(u);
+                candidates(*O, a, c1, &cnt.raw);
+                candidates(*O, a + 1, c2, &cnt.raw);
+                pairFlags(c1, c2, f1, f2);
+                const uint8_t fa = correctOne(*O, a, c1, f1, corr, cnt);
+                flags[a - first] = fa;
+                if (fa & CG_RESULT_CORRECTED) std::memcpy(out + (a - first) * pitch, corr.data(), corr.size());
+                const uint8_t fb = correctOne(*O, a + 1, c2, f2, corr, cnt);
+                flags[a + 1 - first] = fb;
+                if (fb & CG_RESULT_CORRECTED) std::memcpy(out + (a + 1 - first) * pitch, corr.data(), corr.size());
+            }
+        }
+#pragma omp critical
+        {
+            total.raw += cnt.raw; total.uniq += cnt.uniq; total.aligned += cnt.aligned;
+            total.msaCands += cnt.msaCands; total.msaBuilds += cnt.msaBuilds;
+            total.corrected += cnt.corrected; total.hq += cnt.hq;
+        }
+    }
+    if (counters) {
+        counters[0] = total.raw; counters[1] = total.uniq; counters[2] = total.aligned;
+        counters[3] = total.msaCands; counters[4] = total.msaBuilds; counters[5] = total.corrected;
+        counters[6] = total.hq;
+    }
+    return 0;
+}
+
+}  // extern "C"

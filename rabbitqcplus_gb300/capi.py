@@ -1,0 +1,202 @@
+"""ctypes mirror of include/care_gpu.h and a thin Python front end.
+
+`CareOptions` is the C struct `cg_options`; `CareGpu` owns one `cg_ctx`.
+The calls go straight to libcaregpu.so; there is no Python or CPU fallback: a
+missing library or a failing CUDA call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _lib
+
+CG_OK = 0
+CG_ERRORS = {1: "invalid argument", 2: "unsupported", 3: "CUDA error", 4: "out of memory", 5: "bad state",
+             6: "I/O error", 7: "timeout"}
+CG_MAX_HASHMAPS = 48
+CG_PAIR_SE, CG_PAIR_PE = 0, 1
+CG_CORR_CLASSIC, CG_CORR_FOREST, CG_CORR_PRINT, CG_CORR_LEARNED = 0, 1, 2, 3
+CG_RESULT_CORRECTED, CG_RESULT_HQ = 1, 2
+
+
+class CareOptions(ctypes.Structure):
+    _fields_ = [
+        ("kmerlength", ctypes.c_int32),
+        ("num_hash_functions", ctypes.c_int32),
+        ("estimated_coverage", ctypes.c_float),
+        ("estimated_errorrate", ctypes.c_float),
+        ("m_coverage", ctypes.c_float),
+        ("max_error_rate", ctypes.c_float),
+        ("min_overlap_ratio", ctypes.c_float),
+        ("min_overlap", ctypes.c_int32),
+        ("paired_filter_threshold", ctypes.c_float),
+        ("new_columns_to_correct", ctypes.c_int32),
+        ("use_quality_scores", ctypes.c_int32),
+        ("exclude_ambiguous_reads", ctypes.c_int32),
+        ("correct_candidates", ctypes.c_int32),
+        ("pair_mode", ctypes.c_int32),
+        ("correction_type", ctypes.c_int32),
+        ("threshold_anchor", ctypes.c_float),
+        ("device", ctypes.c_int32),
+        ("batch_anchors", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 8),
+    ]
+
+    @classmethod
+    def defaults(cls, coverage: float = 30.0, **kw) -> "CareOptions":
+        """Reference defaults (include/options.hpp:36-99) with --coverage set."""
+        o = cls()
+        o.kmerlength = 20
+        o.num_hash_functions = 48
+        o.estimated_coverage = coverage
+        o.estimated_errorrate = 0.06
+        o.m_coverage = 0.6
+        o.max_error_rate = 0.2
+        o.min_overlap_ratio = 0.3
+        o.min_overlap = 30
+        o.paired_filter_threshold = 0.06
+        o.new_columns_to_correct = 15
+        o.use_quality_scores = 0
+        o.exclude_ambiguous_reads = 0
+        o.correct_candidates = 0
+        o.pair_mode = CG_PAIR_SE
+        o.correction_type = CG_CORR_CLASSIC
+        o.threshold_anchor = 0.5
+        o.device = 0
+        o.batch_anchors = 0
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+
+class CgStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "num_reads", "num_anchors_processed", "raw_candidate_ids", "unique_candidates", "aligned_candidates",
+        "msa_candidates", "msa_builds", "corrected_anchors", "hq_anchors", "table_keys", "table_values")] + [
+        ("kmerlength", ctypes.c_int32), ("num_maps", ctypes.c_int32), ("max_read_length", ctypes.c_int32),
+        ("reserved", ctypes.c_int32), ("seconds_build", ctypes.c_double), ("seconds_correct", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
+
+
+# every symbol include/care_gpu.h declares
+EXPORTED = ["cg_default_options", "cg_create", "cg_destroy", "cg_last_error", "cg_append_reads",
+            "cg_build_tables", "cg_correct", "cg_get_stats", "cg_get_read_info", "cg_get_signatures",
+            "cg_get_candidates"]
+
+
+def gpu_lib() -> ctypes.CDLL:
+    L = _lib.gpu()
+    if not getattr(L, "_cg_typed", False):
+        P = ctypes.c_void_p
+        L.cg_default_options.argtypes = [P]
+        L.cg_create.argtypes = [P, ctypes.POINTER(P)]
+        L.cg_destroy.argtypes = [P]
+        L.cg_last_error.restype = ctypes.c_char_p
+        L.cg_last_error.argtypes = [P]
+        L.cg_append_reads.argtypes = [P, P, P, P, ctypes.c_uint64]
+        L.cg_build_tables.argtypes = [P]
+        L.cg_correct.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, P, P, ctypes.c_size_t]
+        L.cg_get_stats.argtypes = [P, P]
+        L.cg_get_read_info.argtypes = [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int32)]
+        L.cg_get_signatures.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, P]
+        L.cg_get_candidates.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
+        for f in EXPORTED:
+            if f not in ("cg_destroy", "cg_default_options", "cg_last_error"):
+                getattr(L, f).restype = ctypes.c_int
+        L._cg_typed = True
+    return L
+
+
+class CareError(RuntimeError):
+    pass
+
+
+class CareGpu:
+    """One device context: append reads, build tables, correct anchors."""
+
+    def __init__(self, options: CareOptions):
+        self._L = gpu_lib()
+        self.options = options
+        h = ctypes.c_void_p()
+        rc = self._L.cg_create(ctypes.byref(options), ctypes.byref(h))
+        if rc != CG_OK:
+            raise CareError(f"cg_create failed: {CG_ERRORS.get(rc, rc)}")
+        self._h = h
+
+    def _check(self, rc: int, what: str):
+        if rc != CG_OK:
+            msg = self._L.cg_last_error(self._h).decode(errors="replace")
+            raise CareError(f"{what}: {CG_ERRORS.get(rc, rc)}: {msg}")
+
+    def append_reads(self, sequences: np.ndarray, offsets: np.ndarray, qualities: np.ndarray | None = None):
+        s = np.ascontiguousarray(sequences, dtype=np.uint8)
+        o = np.ascontiguousarray(offsets, dtype=np.uint64)
+        q = None if qualities is None else np.ascontiguousarray(qualities, dtype=np.uint8)
+        self._check(self._L.cg_append_reads(self._h, s.ctypes.data, o.ctypes.data,
+                                            None if q is None else q.ctypes.data, len(o) - 1), "cg_append_reads")
+
+    def build_tables(self):
+        self._check(self._L.cg_build_tables(self._h), "cg_build_tables")
+
+    def read_info(self):
+        n, l = ctypes.c_uint64(), ctypes.c_int32()
+        self._check(self._L.cg_get_read_info(self._h, ctypes.byref(n), ctypes.byref(l)), "cg_get_read_info")
+        return n.value, l.value
+
+    def correct(self, first: int = 0, count: int | None = None, flags: np.ndarray | None = None,
+                out: np.ndarray | None = None):
+        n, lmax = self.read_info()
+        if count is None:
+            count = n - first
+        if flags is None:
+            flags = np.zeros(count, dtype=np.uint8)
+        if out is None:
+            out = np.zeros((count, max(lmax, 1)), dtype=np.uint8)
+        self._check(self._L.cg_correct(self._h, first, count, flags.ctypes.data, out.ctypes.data, out.strides[0]),
+                    "cg_correct")
+        return flags, out
+
+    def stats(self) -> dict:
+        s = CgStats()
+        self._check(self._L.cg_get_stats(self._h, ctypes.byref(s)), "cg_get_stats")
+        return s.as_dict()
+
+    def signatures(self, first: int, n: int, num_maps: int) -> np.ndarray:
+        out = np.zeros((n, num_maps), dtype=np.uint64)
+        self._check(self._L.cg_get_signatures(self._h, first, n, out.ctypes.data), "cg_get_signatures")
+        return out
+
+    def candidates(self, anchor: int) -> np.ndarray:
+        cap = 48 * 65536
+        out = np.zeros(cap, dtype=np.uint32)
+        cnt = ctypes.c_uint32()
+        self._check(self._L.cg_get_candidates(self._h, anchor, out.ctypes.data, cap, ctypes.byref(cnt)),
+                    "cg_get_candidates")
+        return out[:cnt.value].copy()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.cg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def apply_corrections(sequences: np.ndarray, offsets: np.ndarray, flags: np.ndarray,
+                      corrected: np.ndarray) -> np.ndarray:
+    """Output reads as the reference's STEP3 writes them for anchor-only
+    correction (src/correctionresultoutput.cpp:1256-1510): a read with a
+    correction record becomes its corrected sequence, others stay unchanged."""
+    out = np.array(sequences, dtype=np.uint8, copy=True)
+    lens = np.diff(offsets).astype(np.int64)
+    idx = np.nonzero(flags & CG_RESULT_CORRECTED)[0]
+    for i in idx:
+        b = int(offsets[i])
+        out[b:b + lens[i]] = corrected[i, :lens[i]]
+    return out
