@@ -1,0 +1,283 @@
+"""Benchmark of the CARE correction hot path on one GB300 (or N replicas).
+
+Workload (default): the 10 Mbp genome with 200 diverged repeat copies, 2M x
+150 bp single-end reads at 30x, substitution rate rising 0.2% -> 2% from 5'
+to 3' (seeded synthetic data of that shape; k=20, 48 maps, coverage 30).
+
+One step = correction of every anchor of that read set.
+  value  corrected reads/s with the read store and hash tables resident in HBM
+         (device time of cg_correct, CUDA events on the library's stream)
+  e2e    the same metric through the public C ABI with host buffers: append the
+         reads from host memory, build the store and the tables on the device,
+         correct every anchor and copy every result back to host memory
+The read store (0.5 GB) and tables (several GB) exceed the 129 MB L2, so no
+separate flush is needed between steps.
+
+`--impl reference` times the reference algorithm on the host cores: the
+reference's own build does not exist on the GPU machine, so this arm runs the
+CPU restatement of it (oracle/, bit-exact with the reference on the committed
+fixtures) with all host threads, each step a bounded sample of anchors.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+from rabbitqcplus_gb300 import capi, sim  # noqa: E402
+
+METRIC = "corrected reads/s on 1 GB300: plain vs batched+learned, at equal TP/FP vs truth"
+UNIT = "reads/s"
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                for line in out.stdout.strip().splitlines():
+                    self.samples.append([x.strip() for x in line.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and
+                          s[3 + i].lower() in ("active", "1")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_arm(reads, opts, sample_anchors: int, threads: int, seconds_target: float = 15.0):
+    """Reference algorithm (oracle restatement) on host cores over a bounded anchor sample."""
+    import oracle
+    t0 = time.perf_counter()
+    orc = oracle.Oracle(opts, reads.sequences, reads.offsets, None, threads=threads)
+    build_s = time.perf_counter() - t0
+    # grow the sample until it takes a few seconds, capped by seconds_target
+    n = min(sample_anchors, reads.n)
+    first = reads.n // 3
+    t0 = time.perf_counter()
+    orc.correct(first, min(2000, n), threads=threads)
+    dt = time.perf_counter() - t0
+    rate = min(2000, n) / max(dt, 1e-6)
+    n = int(min(n, max(2000, rate * seconds_target)))
+    t0 = time.perf_counter()
+    orc.correct(first, n, threads=threads)
+    dt = time.perf_counter() - t0
+    orc.close()
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} anchors (ids {first}..{first + n - 1}) of the workload against its full "
+                      f"hash tables; table build {build_s:.1f}s not included"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c1_10mbp_repeats_se")
+    ap.add_argument("--genome", type=int, default=0, help="scale the config to this genome length")
+    ap.add_argument("--cpu-sample", type=int, default=200_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = env_rank()
+    threads = os.cpu_count() or 1
+
+    cfg = sim.scaled(args.config, args.genome) if args.genome else sim.CONFIGS[args.config]
+    coverage = round(cfg.num_reads * (cfg.read_len_min + cfg.read_len_max) / 2 / cfg.genome_length)
+    opts = capi.CareOptions.defaults(float(coverage), kmerlength=20,
+                                     pair_mode=capi.CG_PAIR_PE if cfg.paired else capi.CG_PAIR_SE)
+    config = {"workload": f"{args.config}: genome {cfg.genome_length} bp, {cfg.num_reads} reads "
+                          f"{cfg.read_len_min}-{cfg.read_len_max} bp, {coverage}x, k=20, 48 maps",
+              "reads": cfg.num_reads, "coverage": coverage, "kmerlength": 20, "hashmaps": 48,
+              "paired": bool(cfg.paired), "l2": "inputs larger than L2 (read store + tables > 129 MB)"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        reads = sim.SimReads(cfg)
+        vals = []
+        for i in range(args.warmup + args.steps):
+            r = cpu_arm(reads, capi.CareOptions.defaults(float(coverage), kmerlength=20), args.cpu_sample,
+                        threads, seconds_target=8.0)
+            if i >= args.warmup:
+                vals.append(r["value"])
+        v = statistics.median(vals)
+        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "u32", "data": "synthetic", "config": config, "impl": "reference",
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": r["sample"]},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    reads = sim.SimReads(cfg)
+    opts.device = local
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # resident correction: build once, then time K full passes
+    g = capi.CareGpu(opts)
+    g.append_reads(reads.sequences, reads.offsets)
+    g.build_tables()
+    n, lmax = g.read_info()
+    flags = np.zeros(n, np.uint8)
+    out = np.zeros((n, lmax), np.uint8)
+    for _ in range(args.warmup):
+        g.correct(0, n, flags, out)
+    st0 = g.stats()
+    barrier()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        dev_seconds = 0.0
+        for _ in range(args.steps):
+            g.correct(0, n, flags, out)
+            dev_seconds += g.stats()["seconds_correct"]
+        barrier()
+        wall = time.perf_counter() - t0
+    st1 = g.stats()
+    t = torch.tensor([dev_seconds], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev_seconds = float(t.item())
+    value = world * n * args.steps / dev_seconds
+    launches = st1["kernel_launches"] - st0["kernel_launches"]
+    final = capi.apply_corrections(reads.sequences, reads.offsets, flags, out)
+    score = reads.score(final)
+
+    # roofline of the dominant kernel (by device time in the timed region)
+    stages = {"align": st1["seconds_align"] - st0["seconds_align"],
+              "msa": st1["seconds_msa"] - st0["seconds_msa"],
+              "candidates": st1["seconds_candidates"] - st0["seconds_candidates"]}
+    dom = max(stages, key=stages.get)
+    hbm_peak, peak_kind = measured_peaks()
+    per_step_cands = (st1["unique_candidates"] - st0["unique_candidates"]) / args.steps
+    per_step_msa = (st1["msa_candidates"] - st0["msa_candidates"]) / args.steps
+    wp = (lmax + 31) // 32 + 1
+    if dom == "align":
+        # per candidate: its fwd+rc hi/lo planes, its id, the packed result (write + reread),
+        # the filtered record; per anchor: its planes and counters
+        bytes_step = per_step_cands * (16 * wp + 4 + 8 + 8) + per_step_msa * 11 + n * (8 * wp + 16)
+        launches_k = (st1["align_launches"] - st0["align_launches"])
+    elif dom == "msa":
+        bytes_step = per_step_msa * (11 + 4 * ((lmax + 15) // 16)) + n * (4 * ((lmax + 15) // 16) + lmax + 8)
+        launches_k = (st1["msa_launches"] - st0["msa_launches"])
+    else:
+        bytes_step = (st1["raw_candidate_ids"] - st0["raw_candidate_ids"]) / args.steps * 8 + n * 48 * 24
+        launches_k = launches
+    dur = stages[dom] / max(launches_k, 1)
+    bytes_launch = bytes_step * args.steps / max(launches_k, 1)
+    achieved = bytes_launch / dur / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+            "avg_launch_ms": dur * 1e3, "stage_seconds_per_step": {k: v / args.steps for k, v in stages.items()}}
+
+    # e2e through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e_times = []
+        for i in range(1 + 1):
+            barrier()
+            t0 = time.perf_counter()
+            g2 = capi.CareGpu(opts)
+            g2.append_reads(reads.sequences, reads.offsets)
+            g2.build_tables()
+            g2.correct(0, n, flags, out)
+            g2.close()
+            barrier()
+            if i >= 1:
+                e2e_times.append(time.perf_counter() - t0)
+        te = max(e2e_times)
+        tt = torch.tensor([te], dtype=torch.float64, device="cuda")
+        if dist is not None:
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e = {"value": world * n / float(tt.item()), "unit": UNIT,
+               "h2d_bytes_per_step": int(reads.sequences.nbytes + reads.offsets.nbytes),
+               "d2h_bytes_per_step": int(flags.nbytes + out.nbytes),
+               "includes": "append from host, device read-store + table build, correction, results to host"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_arm(reads, capi.CareOptions.defaults(float(coverage), kmerlength=20), args.cpu_sample, threads)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dev_seconds / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+                "config": config, "form": "plain", "e2e": e2e, "gpu_launches": int(launches),
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "wall_seconds_timed": wall, "build_seconds": st1["seconds_build"],
+                "score": score, "stats": {k: st1[k] for k in ("raw_candidate_ids", "unique_candidates",
+                                                              "aligned_candidates", "msa_candidates",
+                                                              "corrected_anchors", "hq_anchors", "table_keys",
+                                                              "table_values")}}
+        print(json.dumps(line), flush=True)
+    g.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

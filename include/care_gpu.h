@@ -105,6 +105,12 @@ typedef struct cg_stats {
     int32_t reserved;
     double seconds_build;             /* device time of the last cg_build_tables */
     double seconds_correct;           /* device time of the last cg_correct */
+    double seconds_candidates;        /* device time in candidate stages (query, unique), accumulated */
+    double seconds_align;             /* device time in the alignment/filter kernel, accumulated */
+    double seconds_msa;               /* device time in the MSA/correction kernel, accumulated */
+    uint64_t kernel_launches;         /* kernels this context launched, accumulated */
+    uint64_t align_launches;          /* launches of the alignment/filter kernel */
+    uint64_t msa_launches;            /* launches of the MSA/correction kernel */
 } cg_stats;
 
 /* Fill *o with the reference defaults. */
@@ -166,6 +172,17 @@ int cg_get_read_info(const cg_ctx* ctx, uint64_t* num_reads, int32_t* max_length
  *                      *count gets the number, at most `capacity` are written.
  */
 int cg_get_signatures(cg_ctx* ctx, uint64_t first, uint64_t n, uint64_t* out);
+/*
+ * Whole file-to-file run (reference: care::performCorrection,
+ * src/dispatch_care_correct_cpu.cpp:52-252): read 1 input file (single end, or
+ * interleaved pairs) or 2 paired files, correct every read, write
+ * output_directory/outputs[i] in the input's format (gzip if gz_output),
+ * optionally with " care:q=N" header labels.  *num_records gets the number of
+ * correction records (the changNum of the queue protocol).
+ */
+int cg_correct_files(const cg_options* options, const char* const* inputs, int num_inputs,
+                     const char* output_directory, const char* const* outputs, int num_outputs,
+                     int quality_labels, int gz_output, uint64_t* num_records);
 int cg_get_candidates(cg_ctx* ctx, uint64_t anchor, uint32_t* out, uint32_t capacity, uint32_t* count);
 
 #ifdef __cplusplus

@@ -22,7 +22,7 @@ CXXFLAGS := -DTHRUST_DEVICE_SYSTEM=THRUST_DEVICE_SYSTEM_OMP \
             -I$(REF) -I$(REF)/common -I$(REF)/include -I$(REF)/include/huffman \
             -I$(REF)/include/chunkdecoding -I$(REF)/include/gzip \
             -I$(REF)/src/include -I$(REF)/dependencies/thrust-1.17.0 \
-            -g -O3 -w -fopenmp -ffp-contract=off
+            -O3 -w -fopenmp -ffp-contract=off
 LIBS := -lpthread -fopenmp -lrt -lgomp -lstdc++fs -lz -ldl
 
 REF_OBJS := $(patsubst %,$(OBJ)/%.o,$(REF_SRCS))

@@ -35,13 +35,17 @@ NVCCFLAGS = ["-O3", "-std=c++17", ARCH, "-lineinfo", "--fmad=false", "-prec-div=
              "--expt-relaxed-constexpr", "-I" + INCLUDE_DIR, "-I" + CSRC]
 
 GPU_CU_SOURCES = [
-    "care_kernels.cu",
+    "k_store.cu",
+    "k_tables.cu",
+    "k_correct.cu",
     "care_capi.cu",
 ]
 GPU_CPP_SOURCES = [
-    "host/fastq_io.cpp",
+    "host/seqio.cpp",
     "host/care_host.cpp",
 ]
+# gzip FASTA/FASTQ through zlib where its header is installed
+HAVE_ZLIB = os.path.exists("/usr/include/zlib.h")
 
 _lock = threading.Lock()
 _loaded: dict[str, ctypes.CDLL] = {}
@@ -93,11 +97,13 @@ def build_gpu(force: bool = False, jobs: int = 8) -> str:
         obj = os.path.join(LIB_DIR, "obj", os.path.basename(s) + ".o")
         objs.append(obj)
         if force or _newer(obj, [src] + hdrs):
-            cmds.append([CXX, *CXXFLAGS, "-I" + INCLUDE_DIR, "-I" + CSRC, "-I/usr/local/cuda/include", "-c", src, "-o", obj])
+            cmds.append([CXX, *CXXFLAGS, *(["-DCG_HAVE_ZLIB"] if HAVE_ZLIB else []), "-I" + INCLUDE_DIR, "-I" + CSRC,
+                         "-I/usr/local/cuda/include", "-c", src, "-o", obj])
     with ThreadPoolExecutor(max_workers=jobs) as ex:
         list(ex.map(_run, cmds))
     if force or cmds or not os.path.exists(out):
-        _run([NVCC, ARCH, "-shared", *objs, "-o", out, "-Xcompiler", "-fopenmp", "-lcudart", "-lgomp"])
+        _run([NVCC, ARCH, "-shared", *objs, "-o", out, "-Xcompiler", "-fopenmp", "-lcudart", "-lgomp",
+              *(["-lz"] if HAVE_ZLIB else [])])
     return out
 
 

@@ -77,7 +77,9 @@ class CgStats(ctypes.Structure):
         "num_reads", "num_anchors_processed", "raw_candidate_ids", "unique_candidates", "aligned_candidates",
         "msa_candidates", "msa_builds", "corrected_anchors", "hq_anchors", "table_keys", "table_values")] + [
         ("kmerlength", ctypes.c_int32), ("num_maps", ctypes.c_int32), ("max_read_length", ctypes.c_int32),
-        ("reserved", ctypes.c_int32), ("seconds_build", ctypes.c_double), ("seconds_correct", ctypes.c_double)]
+        ("reserved", ctypes.c_int32), ("seconds_build", ctypes.c_double), ("seconds_correct", ctypes.c_double),
+        ("seconds_candidates", ctypes.c_double), ("seconds_align", ctypes.c_double), ("seconds_msa", ctypes.c_double),
+        ("kernel_launches", ctypes.c_uint64), ("align_launches", ctypes.c_uint64), ("msa_launches", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
@@ -86,7 +88,7 @@ class CgStats(ctypes.Structure):
 # every symbol include/care_gpu.h declares
 EXPORTED = ["cg_default_options", "cg_create", "cg_destroy", "cg_last_error", "cg_append_reads",
             "cg_build_tables", "cg_correct", "cg_get_stats", "cg_get_read_info", "cg_get_signatures",
-            "cg_get_candidates"]
+            "cg_get_candidates", "cg_correct_files"]
 
 
 def gpu_lib() -> ctypes.CDLL:
@@ -105,6 +107,8 @@ def gpu_lib() -> ctypes.CDLL:
         L.cg_get_read_info.argtypes = [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int32)]
         L.cg_get_signatures.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, P]
         L.cg_get_candidates.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
+        L.cg_correct_files.argtypes = [P, P, ctypes.c_int, ctypes.c_char_p, P, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
         for f in EXPORTED:
             if f not in ("cg_destroy", "cg_default_options", "cg_last_error"):
                 getattr(L, f).restype = ctypes.c_int
@@ -200,3 +204,18 @@ def apply_corrections(sequences: np.ndarray, offsets: np.ndarray, flags: np.ndar
         b = int(offsets[i])
         out[b:b + lens[i]] = corrected[i, :lens[i]]
     return out
+
+
+def correct_files(options: CareOptions, inputs: list[str], output_directory: str, outputs: list[str],
+                  quality_labels: bool = False, gz_output: bool = False) -> int:
+    """File-to-file correction (care::performCorrection); returns the number of correction records."""
+    L = gpu_lib()
+    ins = (ctypes.c_char_p * len(inputs))(*[x.encode() for x in inputs])
+    outs = (ctypes.c_char_p * len(outputs))(*[x.encode() for x in outputs])
+    n = ctypes.c_uint64()
+    rc = L.cg_correct_files(ctypes.byref(options), ctypes.cast(ins, ctypes.c_void_p), len(inputs),
+                            output_directory.encode(), ctypes.cast(outs, ctypes.c_void_p), len(outputs),
+                            int(quality_labels), int(gz_output), ctypes.byref(n))
+    if rc != CG_OK:
+        raise CareError(f"cg_correct_files: {CG_ERRORS.get(rc, rc)}")
+    return n.value

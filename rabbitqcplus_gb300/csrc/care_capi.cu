@@ -1,0 +1,631 @@
+// C ABI of the CARE correction engine (include/care_gpu.h): context, device
+// memory, and the order of the kernels.
+//
+// reference: care::performCorrection's STEP1 and STEP2
+// (src/dispatch_care_correct_cpu.cpp:52-170) -- read store and minhasher
+// construction, then cpu::correct_cpu (src/correct_cpu.cpp:47-348) -- with the
+// per-anchor pipeline of CpuErrorCorrector (include/corrector.hpp:145-513)
+// split into batched device stages.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "care_gpu.h"
+#include "care_internal.h"
+
+using namespace cg;
+
+namespace {
+
+// grow-only device buffer
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        size_t want = std::max(n, bytes + bytes / 2);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            e = cudaMalloc(&p, n);
+            if (e != cudaSuccess) return e;
+            want = n;
+        }
+        bytes = want;
+        return cudaSuccess;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+struct MapTable {
+    Slot* slots = nullptr;
+    uint32_t* values = nullptr;
+    uint64_t cap = 0;
+    uint64_t keys = 0;
+    uint64_t nvalues = 0;
+};
+
+}  // namespace
+
+struct cg_ctx {
+    cg_options o{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t st0 = nullptr, st1 = nullptr, st2 = nullptr, st3 = nullptr;  // stage boundaries of a batch
+    std::string err;
+
+    // host staging of appended reads
+    std::vector<char> hChars;
+    std::vector<uint64_t> hOffs{0};
+    std::vector<char> hQual;
+    std::vector<uint64_t> callStarts;  // first read id of each append call
+    bool haveQual = true;
+
+    // device read store
+    bool built = false;
+    uint64_t n = 0;
+    int lmax = 0, pitch = 0, wp = 0, k = 20, nmaps = 48, maxValuesPerKey = 75;
+    DevBuf enc, len, hilo, qual, ambig, sig;
+    std::vector<MapTable> maps;
+    TablesArg tables{};
+    Params params{};
+
+    // batch buffers
+    DevBuf qrange, rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, nfinal, flags, out, counters;
+    DevBuf scanTmp;
+    uint32_t* hPinned = nullptr;  // 2 words: total raw, max raw
+
+    cg_stats stats{};
+};
+
+namespace {
+
+int fail(cg_ctx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define CG_CUDA(ctx, call)                                                                              \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) {                                                                        \
+            return fail((ctx), e_ == cudaErrorMemoryAllocation ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA,    \
+                        "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);    \
+        }                                                                                               \
+    } while (0)
+
+// kernels one exclusive scan of n elements launches
+uint64_t scan_launches(uint64_t n) {
+    uint64_t k = 0;
+    while (true) {
+        const uint64_t tiles = (n + 4095) / 4096;
+        if (tiles <= 1) return k + 1;
+        k += 2;
+        n = tiles;
+    }
+}
+
+uint64_t pow2_at_least(uint64_t x) {
+    uint64_t p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+// Float constants in the reference's operand order (host, no contraction).
+void make_params(cg_ctx* c) {
+    Params& p = c->params;
+    const cg_options& o = c->o;
+    p.k = c->k;
+    p.nmaps = c->nmaps;
+    p.minOverlap = o.min_overlap;
+    p.maxErrorRate = o.max_error_rate;
+    p.minOverlapRatio = o.min_overlap_ratio;
+    p.orientMaxErrorRate = o.estimated_errorrate * 4.0f;              // alignmentorientation.hpp:90
+    p.mmBase = o.estimated_errorrate * 1.0f;                          // corrector.hpp:1063
+    p.mm2 = 2 * p.mmBase;
+    p.mm3 = 3 * p.mmBase;
+    p.mm4 = 4 * p.mmBase;
+    p.goodAlignmentsCountThreshold = o.estimated_coverage * o.m_coverage;  // corrector.hpp:1064
+    p.pairedThreshold = o.paired_filter_threshold;
+    p.avgSupportThreshold = 1.0f - 1.0f * o.estimated_errorrate;     // msa.cpp:314-316
+    p.minSupportThreshold = 1.0f - 3.0f * o.estimated_errorrate;
+    p.minCoverageThreshold = o.m_coverage / 6.0f * o.estimated_coverage;
+    p.errPercent = (int)std::ceil(o.estimated_errorrate * 100.0f);  // msa.cpp:361
+    p.hqPercentLimit = p.errPercent * 0.5f;
+    for (int pc = 0; pc <= 100; pc++) {
+        const float factor = pc / 100.0f;
+        p.hqAvg[pc] = 1.0f - 1.0f * factor;
+        p.hqMin[pc] = 1.0f - 3.0f * factor;
+    }
+    p.significantCount = int(int(o.estimated_coverage) * 0.3f);     // msa.cpp:536-540
+    p.useQuality = o.use_quality_scores != 0;
+    p.excludeAmbiguous = o.exclude_ambiguous_reads != 0;
+    p.paired = o.pair_mode == CG_PAIR_PE;
+    // include/qualityscoreweights.hpp:17-33
+    for (int i = 0; i < 256; i++) {
+        const float e = i < 33 ? 1.0f : std::pow(10.0f, -(i - 33) / 10.0f);
+        p.qweight[i] = std::max(0.001f, 1.0f - e);
+    }
+}
+
+StoreArg store_arg(const cg_ctx* c) {
+    StoreArg s;
+    s.enc = c->enc.as<uint32_t>();
+    s.len = c->len.as<uint16_t>();
+    s.hilo = c->hilo.as<uint32_t>();
+    s.qual = c->qual.as<uint8_t>();
+    s.ambig = c->ambig.as<uint8_t>();
+    s.pitch = c->pitch;
+    s.wp = c->wp;
+    s.lmax = c->lmax;
+    s.n = c->n;
+    return s;
+}
+
+void release_tables(cg_ctx* c) {
+    for (auto& m : c->maps) {
+        if (m.slots) cudaFree(m.slots);
+        if (m.values) cudaFree(m.values);
+    }
+    c->maps.clear();
+}
+
+int build_store(cg_ctx* c) {
+    const uint64_t n = c->hOffs.size() - 1;
+    c->n = n;
+    int lmax = 0;
+    for (uint64_t i = 0; i < n; i++) lmax = std::max<int>(lmax, int(c->hOffs[i + 1] - c->hOffs[i]));
+    c->lmax = std::max(lmax, 1);
+    c->pitch = (c->lmax + 15) / 16;
+    c->wp = (c->lmax + 31) / 32 + 1;
+    c->k = c->o.kmerlength == 0 ? (lmax < 160 ? 20 : 32) : c->o.kmerlength;  // dispatch_care_correct_cpu.cpp:81-95
+    c->nmaps = c->o.num_hash_functions;
+    {
+        // include/minhasherlimit.hpp:9-15 (the coverage argument is an int)
+        const int cov = int(c->o.estimated_coverage);
+        int r = int(cov * 2.5f);
+        r = std::min(r, 65535);
+        r = std::max(10, r);
+        c->maxValuesPerKey = r;
+    }
+    const bool q = c->o.use_quality_scores != 0;
+    CG_CUDA(c, c->enc.ensure(n * c->pitch * sizeof(uint32_t)));
+    CG_CUDA(c, c->len.ensure(n * sizeof(uint16_t)));
+    CG_CUDA(c, c->ambig.ensure(n));
+    CG_CUDA(c, c->hilo.ensure(n * 4 * (uint64_t)c->wp * sizeof(uint32_t)));
+    if (q) CG_CUDA(c, c->qual.ensure(n * (uint64_t)c->lmax));
+    CG_CUDA(c, cudaMemsetAsync(c->enc.p, 0, n * c->pitch * sizeof(uint32_t), c->stream));
+    if (q) CG_CUDA(c, cudaMemsetAsync(c->qual.p, 0, n * (uint64_t)c->lmax, c->stream));
+    // upload and encode per append call (the N counter restarts per call)
+    DevBuf dChars, dOffs, dQual, dInv, tmp;
+    for (size_t ci = 0; ci < c->callStarts.size(); ci++) {
+        const uint64_t r0 = c->callStarts[ci];
+        const uint64_t r1 = ci + 1 < c->callStarts.size() ? c->callStarts[ci + 1] : n;
+        const uint64_t m = r1 - r0;
+        if (m == 0) continue;
+        const uint64_t b0 = c->hOffs[r0], b1 = c->hOffs[r1];
+        std::vector<uint64_t> offs(m + 1);
+        for (uint64_t i = 0; i <= m; i++) offs[i] = c->hOffs[r0 + i] - b0;
+        CG_CUDA(c, dChars.ensure(std::max<uint64_t>(b1 - b0, 1)));
+        CG_CUDA(c, dOffs.ensure((m + 1) * sizeof(uint64_t)));
+        CG_CUDA(c, dInv.ensure((m + 1) * sizeof(uint32_t)));
+        CG_CUDA(c, tmp.ensure(scan_tmp_bytes(m + 1)));
+        CG_CUDA(c, cudaMemcpyAsync(dChars.p, c->hChars.data() + b0, b1 - b0, cudaMemcpyHostToDevice, c->stream));
+        CG_CUDA(c, cudaMemcpyAsync(dOffs.p, offs.data(), (m + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                                   c->stream));
+        if (q) {
+            CG_CUDA(c, dQual.ensure(std::max<uint64_t>(b1 - b0, 1)));
+            CG_CUDA(c, cudaMemcpyAsync(dQual.p, c->hQual.data() + b0, b1 - b0, cudaMemcpyHostToDevice, c->stream));
+        }
+        CG_CUDA(c, launch_count_invalid(dChars.as<char>(), dOffs.as<uint64_t>(), m, dInv.as<uint32_t>(), c->stream));
+        CG_CUDA(c, scan_exclusive_u32(dInv.as<uint32_t>(), m, tmp.p, c->stream));
+        CG_CUDA(c, launch_encode(dChars.as<char>(), dOffs.as<uint64_t>(), q ? dQual.as<char>() : nullptr, m, r0,
+                                 dInv.as<uint32_t>(), nullptr, c->enc.as<uint32_t>(), c->len.as<uint16_t>(),
+                                 c->qual.as<uint8_t>(), c->ambig.as<uint8_t>(), c->pitch, c->lmax, c->stream));
+        // the staging buffers are freed below only after the stream drained
+    }
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    dChars.release();
+    dOffs.release();
+    dQual.release();
+    dInv.release();
+    tmp.release();
+    StoreArg st = store_arg(c);
+    CG_CUDA(c, launch_hilo(st, c->hilo.as<uint32_t>(), c->stream));
+    return CG_OK;
+}
+
+int build_tables(cg_ctx* c) {
+    const uint64_t n = c->n;
+    CG_CUDA(c, c->sig.ensure(n * c->nmaps * sizeof(unsigned long long)));
+    StoreArg st = store_arg(c);
+    CG_CUDA(c, launch_signatures(st, c->k, c->nmaps, c->sig.as<unsigned long long>(), c->stream));
+    const uint64_t cap = pow2_at_least(std::max<uint64_t>(2 * n, 1024));
+    if (cap > 0x80000000ull) return fail(c, CG_ERR_UNSUPPORTED, "too many reads for one table (%llu)",
+                                         (unsigned long long)n);
+    DevBuf tmp, cursor, packed, scanTmp;
+    CG_CUDA(c, tmp.ensure(cap * sizeof(Slot)));
+    CG_CUDA(c, cursor.ensure(cap * sizeof(uint32_t)));
+    CG_CUDA(c, packed.ensure((cap + 1) * sizeof(unsigned long long)));
+    CG_CUDA(c, scanTmp.ensure(scan_tmp_bytes(cap + 1)));
+    unsigned long long* hTot = nullptr;
+    CG_CUDA(c, cudaMallocHost(&hTot, sizeof(unsigned long long)));
+    release_tables(c);
+    c->maps.resize(c->nmaps);
+    c->stats.table_keys = 0;
+    c->stats.table_values = 0;
+    int rc = CG_OK;
+    for (int h = 0; h < c->nmaps && rc == CG_OK; h++) {
+        const unsigned long long* keys = c->sig.as<unsigned long long>() + (uint64_t)h * n;
+        cudaError_t e = launch_table_init(tmp.as<Slot>(), cap, c->stream);
+        if (e == cudaSuccess) e = launch_table_count(keys, n, tmp.as<Slot>(), (uint32_t)(cap - 1), c->stream);
+        if (e == cudaSuccess) e = launch_table_mark(tmp.as<Slot>(), cap, c->maxValuesPerKey,
+                                                    packed.as<unsigned long long>(), c->stream);
+        if (e == cudaSuccess) e = scan_exclusive_u64(packed.as<unsigned long long>(), cap + 1, scanTmp.p, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hTot, packed.as<unsigned long long>() + cap,
+                                                  sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) {
+            rc = fail(c, CG_ERR_CUDA, "table %d count: %s", h, cudaGetErrorString(e));
+            break;
+        }
+        MapTable& mt = c->maps[h];
+        mt.keys = *hTot >> 32;
+        mt.nvalues = *hTot & 0xffffffffull;
+        mt.cap = pow2_at_least(std::max<uint64_t>(2 * mt.keys, 64));
+        e = cudaMalloc(&mt.slots, mt.cap * sizeof(Slot));
+        if (e == cudaSuccess) e = cudaMalloc(&mt.values, std::max<uint64_t>(mt.nvalues, 1) * sizeof(uint32_t));
+        if (e == cudaSuccess) e = launch_table_init(mt.slots, mt.cap, c->stream);
+        if (e == cudaSuccess) e = launch_table_place(tmp.as<Slot>(), cap, packed.as<unsigned long long>(),
+                                                     c->maxValuesPerKey, mt.slots, (uint32_t)(mt.cap - 1),
+                                                     nullptr, c->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(cursor.p, 0, cap * sizeof(uint32_t), c->stream);
+        if (e == cudaSuccess) e = launch_table_fill(keys, n, tmp.as<Slot>(), (uint32_t)(cap - 1),
+                                                    cursor.as<uint32_t>(), mt.values, c->stream);
+        if (e == cudaSuccess) e = launch_table_sort(mt.slots, mt.cap, mt.values, c->stream);
+        if (e != cudaSuccess) {
+            rc = fail(c, e == cudaErrorMemoryAllocation ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA, "table %d build: %s",
+                      h, cudaGetErrorString(e));
+            break;
+        }
+        c->stats.table_keys += mt.keys;
+        c->stats.table_values += mt.nvalues;
+        c->tables.slots[h] = mt.slots;
+        c->tables.values[h] = mt.values;
+        c->tables.mask[h] = (uint32_t)(mt.cap - 1);
+    }
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    cudaFreeHost(hTot);
+    tmp.release();
+    cursor.release();
+    packed.release();
+    scanTmp.release();
+    if (rc != CG_OK) return rc;
+    CG_CUDA(c, e);
+    c->tables.nmaps = c->nmaps;
+    c->tables.maxValuesPerKey = c->maxValuesPerKey;
+    return CG_OK;
+}
+
+BatchArg batch_arg(cg_ctx* c, uint64_t first, int count) {
+    BatchArg b{};
+    b.first = first;
+    b.count = count;
+    b.sig = c->sig.as<unsigned long long>();
+    b.qrange = c->qrange.as<uint2>();
+    b.rawCount = c->rawCount.as<uint32_t>();
+    b.cand = c->cand.as<uint32_t>();
+    b.ncand = c->ncand.as<uint32_t>();
+    b.paired = c->paired.as<uint8_t>();
+    b.aln = c->aln.as<uint2>();
+    b.fid = c->fid.as<uint32_t>();
+    b.fshift = c->fshift.as<int16_t>();
+    b.forient = c->forient.as<uint8_t>();
+    b.fweight = c->fweight.as<float>();
+    b.nfinal = c->nfinal.as<uint32_t>();
+    b.flags = c->flags.as<uint8_t>();
+    b.out = c->out.as<char>();
+    b.outPitch = c->lmax;
+    b.counters = c->counters.as<unsigned long long>();
+    return b;
+}
+
+// Candidate ids of a batch (query, scan, gather/unique).  On return
+// c->hPinned[0] holds the batch's raw id total.
+int run_candidates(cg_ctx* c, uint64_t first, int count) {
+    const StoreArg st = store_arg(c);
+    CG_CUDA(c, cudaEventRecord(c->st0, c->stream));
+    CG_CUDA(c, c->qrange.ensure((size_t)count * c->nmaps * sizeof(uint2)));
+    CG_CUDA(c, c->rawCount.ensure((size_t)(count + 2) * sizeof(uint32_t)));
+    CG_CUDA(c, c->ncand.ensure((size_t)count * sizeof(uint32_t)));
+    CG_CUDA(c, c->scanTmp.ensure(scan_tmp_bytes(count + 1)));
+    CG_CUDA(c, cudaMemsetAsync(c->rawCount.p, 0, (size_t)(count + 2) * sizeof(uint32_t), c->stream));
+    BatchArg b = batch_arg(c, first, count);
+    CG_CUDA(c, launch_query_count(st, c->tables, c->params, b, c->stream));
+    CG_CUDA(c, scan_exclusive_u32(b.rawCount, (size_t)count + 1, c->scanTmp.p, c->stream));
+    c->stats.kernel_launches += 1 + scan_launches(count + 1);
+    CG_CUDA(c, cudaMemcpyAsync(c->hPinned, b.rawCount + count, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                               c->stream));
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    const uint64_t total = c->hPinned[0];
+    const uint32_t maxRaw = c->hPinned[1];
+    const size_t cap = std::max<uint64_t>(total, 1);
+    CG_CUDA(c, c->cand.ensure(cap * sizeof(uint32_t)));
+    CG_CUDA(c, c->paired.ensure(cap));
+    CG_CUDA(c, c->aln.ensure(cap * sizeof(uint2)));
+    CG_CUDA(c, c->fid.ensure(cap * sizeof(uint32_t)));
+    CG_CUDA(c, c->fshift.ensure(cap * sizeof(int16_t)));
+    CG_CUDA(c, c->forient.ensure(cap));
+    CG_CUDA(c, c->fweight.ensure(cap * sizeof(float)));
+    b = batch_arg(c, first, count);
+    CG_CUDA(c, launch_gather_unique(st, c->tables, c->params, b, (int)std::max<uint32_t>(maxRaw, 1), c->stream));
+    c->stats.kernel_launches += 1;
+    return CG_OK;
+}
+
+int run_batch(cg_ctx* c, uint64_t first, int count, uint8_t* hFlags, char* hOut, size_t outPitch) {
+    int rc = run_candidates(c, first, count);
+    if (rc != CG_OK) return rc;
+    const StoreArg st = store_arg(c);
+    CG_CUDA(c, c->nfinal.ensure((size_t)count * sizeof(uint32_t)));
+    CG_CUDA(c, c->flags.ensure((size_t)count));
+    CG_CUDA(c, c->out.ensure((size_t)count * c->lmax));
+    BatchArg b = batch_arg(c, first, count);
+    if (c->params.paired) {
+        CG_CUDA(c, launch_pair_flags(b, c->stream));
+        c->stats.kernel_launches += 1;
+    }
+    CG_CUDA(c, cudaEventRecord(c->st1, c->stream));
+    CG_CUDA(c, launch_align_filter(st, c->params, b, c->stream));
+    CG_CUDA(c, cudaEventRecord(c->st2, c->stream));
+    CG_CUDA(c, launch_msa_correct(st, c->params, b, c->stream));
+    CG_CUDA(c, cudaEventRecord(c->st3, c->stream));
+    c->stats.kernel_launches += 2;
+    c->stats.align_launches += 1;
+    c->stats.msa_launches += 1;
+    CG_CUDA(c, cudaMemcpyAsync(hFlags, b.flags, (size_t)count, cudaMemcpyDeviceToHost, c->stream));
+    CG_CUDA(c, cudaMemcpy2DAsync(hOut, outPitch, b.out, (size_t)c->lmax, std::min<size_t>(outPitch, c->lmax),
+                                 (size_t)count, cudaMemcpyDeviceToHost, c->stream));
+    CG_CUDA(c, cudaEventSynchronize(c->st3));
+    float t01 = 0, t12 = 0, t23 = 0;
+    cudaEventElapsedTime(&t01, c->st0, c->st1);
+    cudaEventElapsedTime(&t12, c->st1, c->st2);
+    cudaEventElapsedTime(&t23, c->st2, c->st3);
+    c->stats.seconds_candidates += t01 / 1000.0;
+    c->stats.seconds_align += t12 / 1000.0;
+    c->stats.seconds_msa += t23 / 1000.0;
+    return CG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void cg_default_options(cg_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->kmerlength = 20;
+    o->num_hash_functions = 48;
+    o->estimated_coverage = 1.0f;
+    o->estimated_errorrate = 0.06f;
+    o->m_coverage = 0.6f;
+    o->max_error_rate = 0.2f;
+    o->min_overlap_ratio = 0.30f;
+    o->min_overlap = 30;
+    o->paired_filter_threshold = 0.06f;
+    o->new_columns_to_correct = 15;
+    o->pair_mode = CG_PAIR_SE;
+    o->correction_type = CG_CORR_CLASSIC;
+    o->threshold_anchor = 0.5f;
+}
+
+int cg_create(const cg_options* o, cg_ctx** out) {
+    if (!o || !out) return CG_ERR_INVALID_ARGUMENT;
+    if (o->num_hash_functions < 1 || o->num_hash_functions > CG_MAX_HASHMAPS) return CG_ERR_INVALID_ARGUMENT;
+    if (o->kmerlength < 0 || o->kmerlength > 32) return CG_ERR_INVALID_ARGUMENT;
+    if (!(o->estimated_coverage > 0.0f)) return CG_ERR_INVALID_ARGUMENT;
+    if (o->pair_mode != CG_PAIR_SE && o->pair_mode != CG_PAIR_PE) return CG_ERR_INVALID_ARGUMENT;
+    if (o->correct_candidates) return CG_ERR_UNSUPPORTED;
+    if (o->correction_type != CG_CORR_CLASSIC) return CG_ERR_UNSUPPORTED;
+    cg_ctx* c = new (std::nothrow) cg_ctx();
+    if (!c) return CG_ERR_OUT_OF_MEMORY;
+    c->o = *o;
+    c->device = o->device;
+    auto bail = [&](cudaError_t e) {
+        delete c;
+        return e == cudaErrorMemoryAllocation ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA;
+    };
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return bail(e);
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(e);
+    e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    for (cudaEvent_t* ev : {&c->st0, &c->st1, &c->st2, &c->st3})
+        if (e == cudaSuccess) e = cudaEventCreate(ev);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->hPinned, 4 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = c->counters.ensure(kNumCounters * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(c->counters.p, 0, kNumCounters * sizeof(unsigned long long));
+    if (e != cudaSuccess) return bail(e);
+    *out = c;
+    return CG_OK;
+}
+
+void cg_destroy(cg_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    release_tables(c);
+    for (DevBuf* b : {&c->enc, &c->len, &c->hilo, &c->qual, &c->ambig, &c->sig, &c->qrange, &c->rawCount, &c->cand,
+                      &c->ncand, &c->paired, &c->aln, &c->fid, &c->fshift, &c->forient, &c->fweight, &c->nfinal,
+                      &c->flags, &c->out, &c->counters, &c->scanTmp})
+        b->release();
+    if (c->hPinned) cudaFreeHost(c->hPinned);
+    for (cudaEvent_t ev : {c->ev0, c->ev1, c->st0, c->st1, c->st2, c->st3})
+        if (ev) cudaEventDestroy(ev);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* cg_last_error(const cg_ctx* c) { return c ? c->err.c_str() : "no context"; }
+
+int cg_append_reads(cg_ctx* c, const char* sequences, const uint64_t* offsets, const char* qualities,
+                    uint64_t num_reads) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    if (c->built) return fail(c, CG_ERR_STATE, "reads cannot be appended after cg_build_tables");
+    if (!sequences || !offsets || num_reads == 0) return fail(c, CG_ERR_INVALID_ARGUMENT, "empty read batch");
+    if (c->o.use_quality_scores && !qualities)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "quality scores requested but not given");
+    for (uint64_t i = 0; i < num_reads; i++) {
+        if (offsets[i + 1] < offsets[i]) return fail(c, CG_ERR_INVALID_ARGUMENT, "offsets not ascending at %llu",
+                                                     (unsigned long long)i);
+        if (offsets[i + 1] - offsets[i] > CG_MAX_READ_LENGTH)
+            return fail(c, CG_ERR_UNSUPPORTED, "read %llu longer than %d", (unsigned long long)i, CG_MAX_READ_LENGTH);
+    }
+    if ((c->hOffs.size() - 1) + num_reads > 0xffffffffull)
+        return fail(c, CG_ERR_UNSUPPORTED, "more than 2^32-1 reads");
+    const uint64_t base = c->hChars.size();
+    const uint64_t bytes = offsets[num_reads] - offsets[0];
+    c->callStarts.push_back(c->hOffs.size() - 1);
+    c->hChars.insert(c->hChars.end(), sequences + offsets[0], sequences + offsets[0] + bytes);
+    if (c->o.use_quality_scores) c->hQual.insert(c->hQual.end(), qualities + offsets[0], qualities + offsets[0] + bytes);
+    for (uint64_t i = 1; i <= num_reads; i++) c->hOffs.push_back(base + offsets[i] - offsets[0]);
+    return CG_OK;
+}
+
+int cg_build_tables(cg_ctx* c) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    if (c->hOffs.size() < 2) return fail(c, CG_ERR_STATE, "no reads appended");
+    if (c->o.pair_mode == CG_PAIR_PE && ((c->hOffs.size() - 1) & 1))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "paired mode needs an even number of reads");
+    CG_CUDA(c, cudaSetDevice(c->device));
+    CG_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    int rc = build_store(c);
+    if (rc != CG_OK) return rc;
+    rc = build_tables(c);
+    if (rc != CG_OK) return rc;
+    make_params(c);
+    CG_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    CG_CUDA(c, cudaEventSynchronize(c->ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->stats.seconds_build = ms / 1000.0;
+    c->stats.num_reads = c->n;
+    c->stats.kmerlength = c->k;
+    c->stats.num_maps = c->nmaps;
+    c->stats.max_read_length = c->lmax;
+    c->built = true;
+    // the host copy of the reads is no longer needed
+    std::vector<char>().swap(c->hChars);
+    std::vector<char>().swap(c->hQual);
+    return CG_OK;
+}
+
+int cg_correct(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* out_flags, char* out_seq, size_t out_pitch) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    if (!c->built) return fail(c, CG_ERR_STATE, "cg_build_tables has not run");
+    if (first + num > c->n || first + num < first) return fail(c, CG_ERR_INVALID_ARGUMENT, "anchor range out of bounds");
+    if (num == 0) return CG_OK;
+    if (!out_flags || !out_seq || out_pitch < (size_t)c->lmax)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "output buffers missing or pitch below %d", c->lmax);
+    if (c->params.paired && ((first | num) & 1)) return fail(c, CG_ERR_INVALID_ARGUMENT, "paired mode needs even ranges");
+    CG_CUDA(c, cudaSetDevice(c->device));
+    int B = c->o.batch_anchors > 0 ? c->o.batch_anchors : 65536;
+    if (c->params.paired && (B & 1)) B++;
+    CG_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    for (uint64_t a = 0; a < num; a += (uint64_t)B) {
+        const int cnt = (int)std::min<uint64_t>((uint64_t)B, num - a);
+        const int rc = run_batch(c, first + a, cnt, out_flags + a, out_seq + a * out_pitch, out_pitch);
+        if (rc != CG_OK) return rc;
+    }
+    CG_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    CG_CUDA(c, cudaEventSynchronize(c->ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->stats.seconds_correct = ms / 1000.0;
+    c->stats.num_anchors_processed += num;
+    return CG_OK;
+}
+
+int cg_get_stats(const cg_ctx* c, cg_stats* out) {
+    if (!c || !out) return CG_ERR_INVALID_ARGUMENT;
+    cg_stats s = c->stats;
+    unsigned long long cnt[kNumCounters] = {0};
+    if (c->counters.p) {
+        cudaSetDevice(c->device);
+        if (cudaMemcpy(cnt, c->counters.p, sizeof(cnt), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return CG_ERR_CUDA;
+    }
+    s.raw_candidate_ids = cnt[kCounterRaw];
+    s.unique_candidates = cnt[kCounterUnique];
+    s.aligned_candidates = cnt[kCounterAligned];
+    s.msa_candidates = cnt[kCounterMsaCands];
+    s.msa_builds = cnt[kCounterMsaBuilds];
+    s.corrected_anchors = cnt[kCounterCorrected];
+    s.hq_anchors = cnt[kCounterHQ];
+    *out = s;
+    return CG_OK;
+}
+
+int cg_get_read_info(const cg_ctx* c, uint64_t* num_reads, int32_t* max_length) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    if (num_reads) *num_reads = c->built ? c->n : c->hOffs.size() - 1;
+    if (max_length) *max_length = c->lmax;
+    return CG_OK;
+}
+
+int cg_get_signatures(cg_ctx* c, uint64_t first, uint64_t n, uint64_t* out) {
+    if (!c || !out) return CG_ERR_INVALID_ARGUMENT;
+    if (!c->built) return fail(c, CG_ERR_STATE, "cg_build_tables has not run");
+    if (first + n > c->n) return fail(c, CG_ERR_INVALID_ARGUMENT, "read range out of bounds");
+    std::vector<uint64_t> col(n);
+    for (int h = 0; h < c->nmaps; h++) {
+        CG_CUDA(c, cudaMemcpy(col.data(), c->sig.as<unsigned long long>() + (uint64_t)h * c->n + first,
+                              n * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        for (uint64_t i = 0; i < n; i++) out[i * c->nmaps + h] = col[i];
+    }
+    return CG_OK;
+}
+
+int cg_get_candidates(cg_ctx* c, uint64_t anchor, uint32_t* out, uint32_t capacity, uint32_t* count) {
+    if (!c || !count) return CG_ERR_INVALID_ARGUMENT;
+    if (!c->built) return fail(c, CG_ERR_STATE, "cg_build_tables has not run");
+    if (anchor >= c->n) return fail(c, CG_ERR_INVALID_ARGUMENT, "anchor out of bounds");
+    CG_CUDA(c, cudaSetDevice(c->device));
+    int rc = run_candidates(c, anchor, 1);
+    if (rc != CG_OK) return rc;
+    uint32_t nc = 0;
+    CG_CUDA(c, cudaMemcpyAsync(&nc, c->ncand.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    *count = nc;
+    const uint32_t w = std::min(nc, capacity);
+    if (w && out) CG_CUDA(c, cudaMemcpy(out, c->cand.p, w * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return CG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,161 @@
+// Internal declarations shared by the CUDA kernel files and the C ABI layer.
+//
+// Device layout (one context, one GPU):
+//   read store      enc   u32 [N][pitch]      2-bit bases, 16 per word, first base in the MSBs
+//                   len   u16 [N]
+//                   hilo  u32 [N][2][2][wp]   hi/lo bit planes (32 bases per word) of the forward
+//                                             and reverse-complement read, wp = ceil(Lmax/32)+1
+//                                             (one zero word of padding for shifted reads)
+//                   qual  u8  [N][Lmax]       Phred+33 (only with quality scores)
+//                   ambig u8  [N]             read had a non-ACGT base
+//   signatures      sig   u64 [maps][N]       minhash key of every read for every map
+//   hash tables     per map: open-addressing slots {key, offset, count} and the
+//                   read ids of every kept key, ascending
+//   per batch       candidate lists, alignment results, filtered lists and the
+//                   corrected anchors, all addressed by per-anchor offsets
+#ifndef CARE_INTERNAL_H
+#define CARE_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "care_gpu.h"
+
+namespace cg {
+
+constexpr uint64_t kEmptyKey = ~0ull;
+constexpr int kSegmentReads = 65536;  // N-replacement counter restarts per parser batch
+constexpr int kMaxMaps = CG_MAX_HASHMAPS;
+constexpr int kMaxBucket = 65535;     // BucketSize is uint16 in the reference
+
+struct Slot {
+    unsigned long long key;
+    uint32_t offset;
+    uint32_t count;
+};
+static_assert(sizeof(Slot) == 16, "slot layout");
+
+// All maps' lookup tables, passed by value to the query kernels.
+struct TablesArg {
+    const Slot* slots[kMaxMaps];
+    const uint32_t* values[kMaxMaps];
+    uint32_t mask[kMaxMaps];
+    int nmaps;
+    int maxValuesPerKey;
+};
+
+// Read store view.
+struct StoreArg {
+    const uint32_t* enc;
+    const uint16_t* len;
+    const uint32_t* hilo;
+    const uint8_t* qual;
+    const uint8_t* ambig;
+    int pitch;      // u32 words per read in enc
+    int wp;         // u32 words per plane in hilo
+    int lmax;
+    uint64_t n;
+};
+
+// Float constants of the correction decision, computed once on the host in
+// the reference's operand order (ISO C++, no contraction).
+struct Params {
+    int k;
+    int nmaps;
+    int minOverlap;
+    float maxErrorRate;        // maxErrorRate (alignment)
+    float minOverlapRatio;
+    float orientMaxErrorRate;  // estimatedErrorrate * 4.0f
+    float mmBase;              // estimatedErrorrate * 1.0f
+    float mm2, mm3, mm4;       // 2/3/4 * mmBase
+    float goodAlignmentsCountThreshold;  // estimatedCoverage * m_coverage
+    float pairedThreshold;
+    float avgSupportThreshold;  // 1 - 1*err
+    float minSupportThreshold;  // 1 - 3*err
+    float minCoverageThreshold; // m_coverage / 6 * cov
+    int errPercent;             // ceil(err * 100)
+    float hqPercentLimit;       // errPercent * 0.5f
+    float hqAvg[101];           // 1 - 1*percent/100 for percent 0..100
+    float hqMin[101];           // 1 - 3*percent/100
+    int significantCount;       // int(int(cov) * 0.3f)
+    int useQuality;
+    int excludeAmbiguous;
+    int paired;
+    float qweight[256];
+};
+
+// ---------------------------------------------------------------- launches
+// Every launcher enqueues on `s` and returns the launch status.
+
+// exclusive scans, in place; `tmp` needs scan_tmp_bytes(n) bytes
+size_t scan_tmp_bytes(size_t n);
+cudaError_t scan_exclusive_u32(uint32_t* data, size_t n, void* tmp, cudaStream_t s);
+cudaError_t scan_exclusive_u64(unsigned long long* data, size_t n, void* tmp, cudaStream_t s);
+
+// read store
+cudaError_t launch_count_invalid(const char* chars, const uint64_t* offs, uint64_t n, uint32_t* invalid,
+                                 cudaStream_t s);
+cudaError_t launch_encode(const char* chars, const uint64_t* offs, const char* quals, uint64_t n,
+                          uint64_t firstId, const uint32_t* invalidScan, const uint64_t* segStart,
+                          uint32_t* enc, uint16_t* len, uint8_t* qual, uint8_t* ambig, int pitch, int lmax,
+                          cudaStream_t s);
+cudaError_t launch_hilo(StoreArg st, uint32_t* hilo, cudaStream_t s);
+cudaError_t launch_signatures(StoreArg st, int k, int nmaps, unsigned long long* sig, cudaStream_t s);
+
+// hash tables
+cudaError_t launch_table_init(Slot* t, uint64_t cap, cudaStream_t s);
+cudaError_t launch_table_count(const unsigned long long* keys, uint64_t n, Slot* tmp, uint32_t tmpMask,
+                               cudaStream_t s);
+cudaError_t launch_table_mark(const Slot* tmp, uint64_t cap, int maxValues, unsigned long long* packed,
+                              cudaStream_t s);
+cudaError_t launch_table_place(Slot* tmp, uint64_t cap, const unsigned long long* packedScan, int maxValues,
+                               Slot* fin, uint32_t finMask, uint32_t* cursor, cudaStream_t s);
+cudaError_t launch_table_fill(const unsigned long long* keys, uint64_t n, const Slot* tmp, uint32_t tmpMask,
+                              uint32_t* cursor, uint32_t* values, cudaStream_t s);
+cudaError_t launch_table_sort(const Slot* fin, uint64_t finCap, uint32_t* values, cudaStream_t s);
+
+// correction batch
+struct BatchArg {
+    uint64_t first;         // first anchor id
+    int count;              // anchors in batch
+    const unsigned long long* sig;  // [nmaps][N]
+    uint2* qrange;          // [count][nmaps] (offset, count) per map
+    uint32_t* rawCount;     // [count+2]: raw counts, exclusive-scanned in place into offsets
+                            // ([count] = total after the scan); [count+1] = batch maximum
+    uint32_t* cand;         // [totalRaw] unique candidate ids
+    uint32_t* ncand;        // [count]
+    uint8_t* paired;        // [totalRaw] pair flags (PE)
+    uint2* aln;             // [totalRaw] packed alignment results
+    uint32_t* fid;          // [totalRaw] filtered candidates: id
+    int16_t* fshift;        // [totalRaw]
+    uint8_t* forient;       // [totalRaw] 1 fwd, 2 rc
+    float* fweight;         // [totalRaw]
+    uint32_t* nfinal;       // [count]
+    uint8_t* flags;         // [count] CG_RESULT_*
+    char* out;              // [count][outPitch]
+    int outPitch;
+    unsigned long long* counters;  // device counters, see kCounter*
+};
+enum {
+    kCounterRaw = 0,
+    kCounterUnique,
+    kCounterAligned,
+    kCounterMsaCands,
+    kCounterMsaBuilds,
+    kCounterCorrected,
+    kCounterHQ,
+    kCounterTimeouts,
+    kNumCounters
+};
+
+cudaError_t launch_query_count(StoreArg st, TablesArg tb, Params p, BatchArg b, cudaStream_t s);
+cudaError_t launch_gather_unique(StoreArg st, TablesArg tb, Params p, BatchArg b, int maxRawPerAnchor,
+                                 cudaStream_t s);
+cudaError_t launch_pair_flags(BatchArg b, cudaStream_t s);
+cudaError_t launch_align_filter(StoreArg st, Params p, BatchArg b, cudaStream_t s);
+cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, cudaStream_t s);
+size_t msa_smem_bytes(int maxCols);
+
+}  // namespace cg
+
+#endif

@@ -1,0 +1,294 @@
+// Host side of the drop-in boundary (see care_host.h).
+#include "care_host.h"
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "seqio.h"
+
+namespace care_gb300 {
+
+cg_options toCgOptions(const ProgramOptions& o) {
+    cg_options c;
+    cg_default_options(&c);
+    c.kmerlength = o.autodetectKmerlength ? 0 : o.kmerlength;
+    c.num_hash_functions = o.numHashFunctions;
+    c.estimated_coverage = o.estimatedCoverage;
+    c.estimated_errorrate = o.estimatedErrorrate;
+    c.m_coverage = o.m_coverage;
+    c.max_error_rate = o.maxErrorRate;
+    c.min_overlap_ratio = o.min_overlap_ratio;
+    c.min_overlap = o.min_overlap;
+    c.paired_filter_threshold = o.pairedFilterThreshold;
+    c.new_columns_to_correct = o.new_columns_to_correct;
+    c.use_quality_scores = o.useQualityScores;
+    c.exclude_ambiguous_reads = o.excludeAmbiguousReads;
+    c.correct_candidates = o.correctCandidates;
+    c.pair_mode = o.pairType == SequencePairType::PairedEnd ? CG_PAIR_PE : CG_PAIR_SE;
+    c.correction_type = (int)o.correctionType;
+    c.threshold_anchor = o.thresholdAnchor;
+    c.device = o.deviceIds.empty() ? 0 : o.deviceIds[0];
+    return c;
+}
+
+namespace {
+
+struct Ctx {
+    cg_ctx* c = nullptr;
+    ~Ctx() {
+        if (c) cg_destroy(c);
+    }
+};
+
+void check(cg_ctx* c, int rc, const char* what) {
+    if (rc != CG_OK) {
+        throw std::runtime_error(std::string(what) + " failed (" + std::to_string(rc) + "): " +
+                                 (c ? cg_last_error(c) : ""));
+    }
+}
+
+bool isAmbiguousChar(char ch) {
+    switch (ch) {
+        case 'A': case 'C': case 'G': case 'T': case 'a': case 'c': case 'g': case 't': return false;
+        default: return true;
+    }
+}
+
+char upper(char ch) {
+    switch (ch) {
+        case 'a': return 'A';
+        case 'c': return 'C';
+        case 'g': return 'G';
+        case 't': return 'T';
+        default: return ch;
+    }
+}
+
+// STEP1-2: reads of the input group, device build and correction.
+// Output per read: final sequence written into `seqOut` (same offsets as the
+// input) and a status byte (0 no record, 1 LQ record, 3 HQ record).
+struct Corrected {
+    ReadSet reads;
+    std::vector<char> seqOut;
+    std::vector<uint8_t> status;
+    uint64_t records = 0;
+    cg_stats stats{};
+};
+
+Corrected runCorrection(const ProgramOptions& o) {
+    if (o.inputfiles.empty()) throw std::runtime_error("no input files");
+    if (o.correctionType == CorrectionType::Print) throw std::runtime_error("correction type Print is not supported");
+    Corrected r;
+    std::vector<uint64_t> groupStarts;  // one device append call per input group
+    if (o.pairType == SequencePairType::PairedEnd && o.inputfiles.size() == 2) {
+        groupStarts.push_back(0);
+        readPairedFiles(o.inputfiles[0], o.inputfiles[1], r.reads);
+    } else {
+        for (size_t i = 0; i < o.inputfiles.size(); i++) {
+            groupStarts.push_back(r.reads.size());
+            readSingleFile(o.inputfiles[i], r.reads, (uint8_t)i);
+        }
+    }
+    const uint64_t n = r.reads.size();
+    if (n == 0) throw std::runtime_error("input contains no reads");
+    bool useQ = o.useQualityScores && r.reads.hasQualities;  // src/main_correct_cpu.cpp:109-121
+    ProgramOptions eff = o;
+    eff.useQualityScores = useQ;
+    const cg_options co = toCgOptions(eff);
+    Ctx ctx;
+    check(nullptr, cg_create(&co, &ctx.c), "cg_create");
+    for (size_t gi = 0; gi < groupStarts.size(); gi++) {
+        const uint64_t a = groupStarts[gi];
+        const uint64_t b = gi + 1 < groupStarts.size() ? groupStarts[gi + 1] : n;
+        if (b == a) continue;
+        check(ctx.c,
+              cg_append_reads(ctx.c, r.reads.sequences.data(), r.reads.offsets.data() + a,
+                              useQ ? r.reads.qualities.data() : nullptr, b - a),
+              "cg_append_reads");
+    }
+    check(ctx.c, cg_build_tables(ctx.c), "cg_build_tables");
+    uint64_t nr = 0;
+    int32_t lmax = 0;
+    check(ctx.c, cg_get_read_info(ctx.c, &nr, &lmax), "cg_get_read_info");
+    r.seqOut = r.reads.sequences;
+    r.status.assign(n, 0);
+    const uint64_t chunk = 1u << 20;
+    std::vector<uint8_t> flags(chunk);
+    std::vector<char> seqs(chunk * (size_t)lmax);
+    for (uint64_t first = 0; first < n; first += chunk) {
+        const uint64_t cnt = std::min(chunk, n - first);
+        check(ctx.c, cg_correct(ctx.c, first, cnt, flags.data(), seqs.data(), (size_t)lmax), "cg_correct");
+        for (uint64_t j = 0; j < cnt; j++) {
+            if (!(flags[j] & CG_RESULT_CORRECTED)) continue;
+            const uint64_t id = first + j;
+            const uint64_t off = r.reads.offsets[id];
+            const int len = (int)(r.reads.offsets[id + 1] - off);
+            const char* orig = r.reads.sequences.data() + off;
+            const char* corr = seqs.data() + j * (size_t)lmax;
+            const bool hq = (flags[j] & CG_RESULT_HQ) != 0;
+            bool ambiguous = false;
+            for (int p = 0; p < len && !ambiguous; p++) ambiguous = isAmbiguousChar(orig[p]);
+            char* dst = r.seqOut.data() + off;
+            if (ambiguous) {
+                // include/corrector.hpp:1651-1667: no edit list for reads with N
+                std::memcpy(dst, corr, len);
+                r.status[id] = hq ? 3 : 1;
+                r.records++;
+                continue;
+            }
+            const int maxEdits = len / 7;
+            int edits = 0;
+            for (int p = 0; p < len && edits <= maxEdits; p++) edits += corr[p] != upper(orig[p]);
+            if (edits <= maxEdits) {
+                if (hq && edits == 0) continue;  // src/correct_cpu.cpp:263-273 drops such records
+                for (int p = 0; p < len; p++)
+                    if (corr[p] != upper(orig[p])) dst[p] = corr[p];
+            } else {
+                std::memcpy(dst, corr, len);
+            }
+            r.status[id] = hq ? 3 : 1;
+            r.records++;
+        }
+    }
+    check(ctx.c, cg_get_stats(ctx.c, &r.stats), "cg_get_stats");
+    return r;
+}
+
+std::string labelled(const std::string& header, uint8_t status, bool labels) {
+    if (!labels) return header;
+    // src/correctionresultoutput.cpp:403-414
+    return header + (status == 3 ? " care:q=3" : status == 1 ? " care:q=1" : " care:q=0");
+}
+
+}  // namespace
+
+RunReport performCorrection(const ProgramOptions& o) {
+    Corrected r = runCorrection(o);
+    std::vector<FileFormat> formats;
+    for (const auto& f : o.inputfiles) formats.push_back(detectFormat(f));
+    FileFormat fmt = formats[0];
+    if (o.gzoutput) {
+        if (fmt == FileFormat::FASTQ) fmt = FileFormat::FASTQGZ;
+        if (fmt == FileFormat::FASTA) fmt = FileFormat::FASTAGZ;
+    } else {
+        if (fmt == FileFormat::FASTQGZ) fmt = FileFormat::FASTQ;
+        if (fmt == FileFormat::FASTAGZ) fmt = FileFormat::FASTA;
+    }
+    if (o.outputfilenames.empty()) throw std::runtime_error("no output file names");
+    std::vector<std::unique_ptr<SequenceWriter>> writers;
+    for (const auto& name : o.outputfilenames)
+        writers.emplace_back(new SequenceWriter(o.outputdirectory + "/" + name, fmt));
+    const uint64_t n = r.reads.size();
+    static const std::string empty;
+    for (uint64_t i = 0; i < n; i++) {
+        const uint64_t off = r.reads.offsets[i];
+        const size_t len = r.reads.offsets[i + 1] - off;
+        const int w = writers.size() == 1 ? 0 : std::min<int>(r.reads.fileId[i], (int)writers.size() - 1);
+        const std::string q = r.reads.hasQualities ? std::string(r.reads.qualities.data() + off, len) : empty;
+        writers[w]->write(labelled(r.reads.headers[i], r.status[i], o.outputCorrectionQualityLabels),
+                          r.seqOut.data() + off, len, q);
+    }
+    RunReport rep;
+    rep.reads = n;
+    rep.records = r.records;
+    rep.stats = r.stats;
+    return rep;
+}
+
+RunReport performCorrectionToSink(const ProgramOptions& o, const std::function<void(int)>& onStart,
+                                  const ChunkSink& sink) {
+    Corrected r = runCorrection(o);
+    RunReport rep;
+    rep.reads = r.reads.size();
+    rep.records = r.records;
+    rep.stats = r.stats;
+    onStart((int)r.records);  // src/correctionresultoutput.cpp:465-466
+    if (r.records == 0) return rep;
+    const int cap = 1 << 20;
+    const int nfiles = (o.pairType == SequencePairType::PairedEnd && o.inputfiles.size() == 2) ? 2 : 1;
+    std::vector<char*> buf(nfiles, nullptr);
+    std::vector<int> used(nfiles, 0);
+    for (int f = 0; f < nfiles; f++) buf[f] = new char[cap];
+    bool ok = true;
+    auto put = [&](int f, const char* p, size_t len) {
+        std::memcpy(buf[f] + used[f], p, len);
+        used[f] += (int)len;
+    };
+    for (uint64_t i = 0; i < rep.reads && ok; i++) {
+        const uint64_t off = r.reads.offsets[i];
+        const size_t len = r.reads.offsets[i + 1] - off;
+        const int f = nfiles == 1 ? 0 : r.reads.fileId[i];
+        const std::string hdr = labelled(r.reads.headers[i], r.status[i], o.outputCorrectionQualityLabels);
+        const size_t need = hdr.size() + 2 * len + 6;
+        if (need >= (size_t)cap) throw std::runtime_error("record larger than a 1 MiB chunk");
+        if (used[f] + need >= (size_t)cap) {
+            ok = sink(f, buf[f], used[f]);
+            buf[f] = ok ? new char[cap] : nullptr;
+            used[f] = 0;
+            if (!ok) break;
+        }
+        // src/correctionresultoutput.cpp:733-770: '@' header, sequence, '+', quality
+        put(f, "@", 1);
+        put(f, hdr.data(), hdr.size());
+        put(f, "\n", 1);
+        put(f, r.seqOut.data() + off, len);
+        put(f, "\n+\n", 3);
+        if (r.reads.hasQualities) put(f, r.reads.qualities.data() + off, len);
+        put(f, "\n", 1);
+    }
+    for (int f = 0; f < nfiles; f++) {
+        if (!buf[f]) continue;
+        if (ok && used[f] > 0) {
+            ok = sink(f, buf[f], used[f]);
+        } else {
+            delete[] buf[f];
+        }
+    }
+    return rep;
+}
+
+}  // namespace care_gb300
+
+// ---------------------------------------------------------------- C ABI
+extern "C" int cg_correct_files(const cg_options* options, const char* const* inputs, int num_inputs,
+                                const char* output_directory, const char* const* outputs, int num_outputs,
+                                int quality_labels, int gz_output, uint64_t* num_records) {
+    using namespace care_gb300;
+    if (!options || !inputs || num_inputs < 1 || num_inputs > 2 || !outputs || num_outputs < 1 || !output_directory)
+        return CG_ERR_INVALID_ARGUMENT;
+    ProgramOptions o;
+    o.kmerlength = options->kmerlength;
+    o.autodetectKmerlength = options->kmerlength == 0;
+    o.numHashFunctions = options->num_hash_functions;
+    o.estimatedCoverage = options->estimated_coverage;
+    o.estimatedErrorrate = options->estimated_errorrate;
+    o.m_coverage = options->m_coverage;
+    o.maxErrorRate = options->max_error_rate;
+    o.min_overlap_ratio = options->min_overlap_ratio;
+    o.min_overlap = options->min_overlap;
+    o.pairedFilterThreshold = options->paired_filter_threshold;
+    o.new_columns_to_correct = options->new_columns_to_correct;
+    o.useQualityScores = options->use_quality_scores;
+    o.excludeAmbiguousReads = options->exclude_ambiguous_reads;
+    o.correctCandidates = options->correct_candidates;
+    o.pairType = options->pair_mode == CG_PAIR_PE ? SequencePairType::PairedEnd : SequencePairType::SingleEnd;
+    o.correctionType = (CorrectionType)options->correction_type;
+    o.thresholdAnchor = options->threshold_anchor;
+    o.deviceIds = {options->device};
+    o.outputCorrectionQualityLabels = quality_labels != 0;
+    o.gzoutput = gz_output != 0;
+    o.outputdirectory = output_directory;
+    for (int i = 0; i < num_inputs; i++) o.inputfiles.push_back(inputs[i]);
+    for (int i = 0; i < num_outputs; i++) o.outputfilenames.push_back(outputs[i]);
+    try {
+        RunReport rep = performCorrection(o);
+        if (num_records) *num_records = rep.records;
+        return CG_OK;
+    } catch (const std::exception&) {
+        return CG_ERR_IO;
+    }
+}

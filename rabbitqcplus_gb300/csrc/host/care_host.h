@@ -1,0 +1,111 @@
+// Host side of the drop-in boundary: the reference's two CARE entry points,
+// re-implemented over the C ABI of include/care_gpu.h.
+//
+// reference: include/dispatch_care_correct_cpu.hpp:9-11
+//     void care::performCorrection(ProgramOptions);
+//     void care::performCorrectionOutToQueue(ProgramOptions, Q1, Q2, producerDone,
+//                                            careStartWrite, changNum);
+// and the STEP3 output rules of src/correctionresultoutput.cpp:448-970,1256-1551
+// (anchor-only correction: a read with a correction record takes its
+// corrected sequence -- as edits when it had no ambiguous base and at most
+// length/7 positions changed, else whole -- and the record count is the
+// changNum of the queue protocol).
+#ifndef CARE_HOST_H
+#define CARE_HOST_H
+
+#include <atomic>
+#include <cstdint>
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "care_gpu.h"
+
+#include <unistd.h>
+
+namespace care_gb300 {
+
+enum class SequencePairType { Invalid, SingleEnd, PairedEnd };
+enum class CorrectionType : int { Classic = 0, Forest = 1, Print = 2, Learned = 3 };
+
+// The fields of care::ProgramOptions (reference include/options.hpp:36-99)
+// that the correction path and its output read, with the same names and defaults.
+struct ProgramOptions {
+    int min_overlap = 30;
+    float maxErrorRate = 0.2f;
+    float min_overlap_ratio = 0.30f;
+    bool excludeAmbiguousReads = false;
+    bool correctCandidates = false;
+    bool useQualityScores = false;
+    bool autodetectKmerlength = false;
+    bool outputCorrectionQualityLabels = false;
+    bool gzoutput = false;
+    float estimatedCoverage = 1.0f;
+    float estimatedErrorrate = 0.06f;
+    float m_coverage = 0.6f;
+    int batchsize = 1000;
+    int new_columns_to_correct = 15;
+    int kmerlength = 20;
+    int numHashFunctions = 48;
+    CorrectionType correctionType = CorrectionType::Classic;
+    CorrectionType correctionTypeCands = CorrectionType::Classic;
+    float thresholdAnchor = .5f;
+    float pairedFilterThreshold = 0.06f;
+    bool showProgress = false;
+    int threads = 1;
+    std::vector<int> deviceIds;
+    int qualityScoreBits = 8;
+    SequencePairType pairType = SequencePairType::SingleEnd;
+    std::string outputdirectory = "";
+    std::string tempdirectory = "";
+    std::vector<std::string> inputfiles;
+    std::vector<std::string> outputfilenames;
+};
+
+cg_options toCgOptions(const ProgramOptions& o);
+
+// One output chunk: `data` (allocated with new char[]) holds whole FASTQ
+// records of output file `file`; ownership passes to the sink.
+using ChunkSink = std::function<bool(int file, char* data, int size)>;
+
+struct RunReport {
+    uint64_t reads = 0;
+    uint64_t records = 0;  // correction records (changNum)
+    cg_stats stats{};
+};
+
+// STEP1-3 into files outputdirectory/outputfilenames[i].  Throws on error.
+RunReport performCorrection(const ProgramOptions& programOptions);
+
+// STEP1-3 into 1 MiB chunks; onStart(changNum) is called before the first
+// chunk; no chunk is produced when changNum is 0.  Throws on error.
+RunReport performCorrectionToSink(const ProgramOptions& programOptions, const std::function<void(int)>& onStart,
+                                  const ChunkSink& sink);
+
+// The reference's queue protocol on any queue type with
+// try_enqueue(std::pair<char*, int>) (moodycamel::ReaderWriterQueue in RabbitQCPlus).
+template <class Queue>
+void performCorrectionOutToQueue(ProgramOptions programOptions, Queue* Q1, Queue* Q2, std::atomic_int* producerDone,
+                                 std::atomic_int* careStartWrite, int* changNum) {
+    performCorrectionToSink(
+        programOptions,
+        [&](int n) {
+            *changNum = n;
+            *careStartWrite = 1;
+        },
+        [&](int file, char* data, int size) {
+            Queue* q = file == 0 ? Q1 : Q2;
+            while (!q->try_enqueue(std::pair<char*, int>(data, size))) {
+                if (*producerDone == 1) {
+                    delete[] data;
+                    return false;
+                }
+                usleep(100);
+            }
+            return true;
+        });
+}
+
+}  // namespace care_gb300
+
+#endif

@@ -1,0 +1,407 @@
+// Minhash tables: build and query.
+//
+// reference: include/ordinaryminhasher.hpp:135-254,376-449 and
+// include/groupbykey.hpp:69-250 (per map: group (key, readId) by key, read ids
+// ascending, drop keys with fewer than 2 or more than maxValuesPerKey ids),
+// include/corrector.hpp:571-650 (candidate ids: union of the anchor's buckets,
+// sorted, unique, self removed, optionally ambiguous reads removed) and
+// include/util.hpp:1005-1200 (pair flags of paired-end candidates).
+//
+// Build, per map, without a sort: (1) count every key in an open-addressing
+// table of 2N slots, (2) scan the kept keys' counts into value offsets,
+// (3) place kept keys into a compact final table, (4) scatter read ids into
+// their buckets, (5) sort each bucket (at most maxValuesPerKey ids).  The
+// bucket contents -- the only thing a query observes -- equal the reference's.
+
+#include "care_device.cuh"
+#include "care_internal.h"
+
+namespace cg {
+
+namespace {
+
+__global__ void table_init_kernel(Slot* __restrict__ t, uint64_t cap) {
+    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < cap) {
+        t[s].key = kEmptyKey;
+        t[s].offset = 0;
+        t[s].count = 0;
+    }
+}
+
+__global__ void table_count_kernel(const unsigned long long* __restrict__ keys, uint64_t n, Slot* __restrict__ tmp,
+                                   uint32_t mask) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long key = keys[i];
+    if (key == kEmptyKey) return;  // only possible for k == 32; never queried
+    uint32_t s = slot_of(key, mask);
+    for (uint32_t probe = 0; probe <= mask; probe++) {
+        const unsigned long long old = atomicCAS(&tmp[s].key, kEmptyKey, key);
+        if (old == kEmptyKey || old == key) {
+            atomicAdd(&tmp[s].count, 1u);
+            return;
+        }
+        s = (s + 1) & mask;
+    }
+}
+
+// packed[s] = (1 << 32) | count for a kept key, else 0; packed[cap] = 0
+__global__ void table_mark_kernel(const Slot* __restrict__ tmp, uint64_t cap, int maxValues,
+                                  unsigned long long* __restrict__ packed) {
+    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s > cap) return;
+    if (s == cap) {
+        packed[s] = 0;
+        return;
+    }
+    const Slot t = tmp[s];
+    const uint32_t upper = (uint32_t)min(maxValues, kMaxBucket);
+    const bool kept = t.key != kEmptyKey && t.count >= 2u && t.count <= upper;
+    packed[s] = kept ? ((1ull << 32) | t.count) : 0ull;
+}
+
+__global__ void table_place_kernel(Slot* __restrict__ tmp, uint64_t cap, const unsigned long long* __restrict__ scan,
+                                   int maxValues, Slot* __restrict__ fin, uint32_t finMask) {
+    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= cap) return;
+    Slot t = tmp[s];
+    if (t.key == kEmptyKey) return;
+    const uint32_t upper = (uint32_t)min(maxValues, kMaxBucket);
+    const bool kept = t.count >= 2u && t.count <= upper;
+    const uint32_t off = (uint32_t)(scan[s] & 0xffffffffull);
+    tmp[s].offset = kept ? off : 0xffffffffu;
+    if (!kept) return;
+    uint32_t f = slot_of(t.key, finMask);
+    for (uint32_t probe = 0; probe <= finMask; probe++) {
+        const unsigned long long old = atomicCAS(&fin[f].key, kEmptyKey, t.key);
+        if (old == kEmptyKey) {
+            fin[f].offset = off;
+            fin[f].count = t.count;
+            return;
+        }
+        f = (f + 1) & finMask;
+    }
+}
+
+__global__ void table_fill_kernel(const unsigned long long* __restrict__ keys, uint64_t n,
+                                  const Slot* __restrict__ tmp, uint32_t mask, uint32_t* __restrict__ cursor,
+                                  uint32_t* __restrict__ values) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long key = keys[i];
+    if (key == kEmptyKey) return;
+    uint32_t s = slot_of(key, mask);
+    for (uint32_t probe = 0; probe <= mask; probe++) {
+        const Slot t = tmp[s];
+        if (t.key == key) {
+            if (t.offset != 0xffffffffu) {
+                const uint32_t pos = atomicAdd(&cursor[s], 1u);
+                values[t.offset + pos] = (uint32_t)i;
+            }
+            return;
+        }
+        if (t.key == kEmptyKey) return;
+        s = (s + 1) & mask;
+    }
+}
+
+// one thread per final slot: insertion sort of the bucket's read ids
+__global__ void table_sort_kernel(const Slot* __restrict__ fin, uint64_t cap, uint32_t* __restrict__ values) {
+    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= cap) return;
+    const Slot t = fin[s];
+    if (t.key == kEmptyKey) return;
+    uint32_t* v = values + t.offset;
+    for (uint32_t i = 1; i < t.count; i++) {
+        const uint32_t x = v[i];
+        int j = (int)i - 1;
+        while (j >= 0 && v[j] > x) {
+            v[j + 1] = v[j];
+            j--;
+        }
+        v[j + 1] = x;
+    }
+}
+
+// ---------------------------------------------------------------- query
+
+__device__ __forceinline__ uint2 lookup(const Slot* __restrict__ slots, uint32_t mask, unsigned long long key) {
+    if (key == kEmptyKey) return make_uint2(0, 0);
+    uint32_t s = slot_of(key, mask);
+    for (uint32_t probe = 0; probe <= mask; probe++) {
+        const Slot t = slots[s];
+        if (t.key == key) return make_uint2(t.offset, t.count);
+        if (t.key == kEmptyKey) return make_uint2(0, 0);
+        s = (s + 1) & mask;
+    }
+    return make_uint2(0, 0);
+}
+
+// One warp per anchor: the anchor's bucket of every map.
+__global__ void query_count_kernel(StoreArg st, TablesArg tb, Params p, BatchArg b) {
+    const int a = (int)(((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (a >= b.count) return;
+    const uint32_t lane = lane_id();
+    const uint64_t aid = b.first + (uint64_t)a;
+    const bool active = st.len[aid] >= p.k && !(p.excludeAmbiguous && st.ambig[aid]);
+    uint32_t total = 0;
+    for (int m = (int)lane; m < tb.nmaps; m += 32) {
+        uint2 r = make_uint2(0, 0);
+        if (active) {
+            r = lookup(tb.slots[m], tb.mask[m], b.sig[(uint64_t)m * st.n + aid]);
+            if ((int)r.y > tb.maxValuesPerKey) r = make_uint2(0, 0);
+        }
+        b.qrange[(uint64_t)a * tb.nmaps + m] = r;
+        total += r.y;
+    }
+    total = __reduce_add_sync(0xffffffffu, total);
+    if (lane == 0) {
+        b.rawCount[a] = total;
+        atomicMax(&b.rawCount[b.count + 1], total);  // batch maximum
+    }
+}
+
+constexpr int kGatherThreads = 128;
+
+// One block per anchor: gather the bucket contents into shared memory, bitonic
+// sort, keep first occurrences, drop the anchor itself (and ambiguous reads
+// if requested).  rawOff = exclusive scan of the raw counts.
+__global__ void __launch_bounds__(kGatherThreads) gather_unique_kernel(StoreArg st, TablesArg tb, Params p,
+                                                                       BatchArg b, const uint32_t* __restrict__ rawOff,
+                                                                       int sortSize) {
+    extern __shared__ uint32_t buf[];
+    __shared__ uint2 rng[kMaxMaps];
+    __shared__ uint32_t pre[kMaxMaps + 1];
+    __shared__ uint32_t warpSum[kGatherThreads / 32];
+    const int a = blockIdx.x;
+    const uint64_t aid = b.first + (uint64_t)a;
+    const uint32_t raw = rawOff[a + 1] - rawOff[a];
+    const int tid = threadIdx.x;
+    if (raw == 0) {
+        if (tid == 0) b.ncand[a] = 0;
+        return;
+    }
+    if (tid < tb.nmaps) rng[tid] = b.qrange[(uint64_t)a * tb.nmaps + tid];
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t acc = 0;
+        for (int m = 0; m < tb.nmaps; m++) {
+            pre[m] = acc;
+            acc += rng[m].y;
+        }
+        pre[tb.nmaps] = acc;
+    }
+    __syncthreads();
+    for (int m = 0; m < tb.nmaps; m++) {
+        const uint32_t c = rng[m].y;
+        const uint32_t* src = tb.values[m] + rng[m].x;
+        for (uint32_t j = tid; j < c; j += kGatherThreads) buf[pre[m] + j] = src[j];
+    }
+    int S = 32;
+    while ((uint32_t)S < raw) S <<= 1;
+    for (int j = (int)raw + tid; j < S; j += kGatherThreads) buf[j] = 0xffffffffu;
+    __syncthreads();
+    for (int k = 2; k <= S; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < S; i += kGatherThreads) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const uint32_t x = buf[i], y = buf[ixj];
+                    const bool asc = (i & k) == 0;
+                    if ((x > y) == asc) {
+                        buf[i] = y;
+                        buf[ixj] = x;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // keep flags over contiguous chunks, block scan, compact
+    const int per = S / kGatherThreads > 0 ? S / kGatherThreads : 1;
+    const int lo = tid * per;
+    auto keep = [&](int j) -> bool {
+        if (j >= S) return false;
+        const uint32_t v = buf[j];
+        if (v == 0xffffffffu) return false;
+        if (j > 0 && buf[j - 1] == v) return false;
+        if ((uint64_t)v == aid) return false;
+        if (p.excludeAmbiguous && st.ambig[v]) return false;
+        return true;
+    };
+    uint32_t mine = 0;
+    for (int j = lo; j < lo + per; j++) mine += keep(j);
+    const int lane = tid & 31, warp = tid >> 5;
+    uint32_t incl = mine;
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += y;
+    }
+    if (lane == 31) warpSum[warp] = incl;
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < kGatherThreads / 32; w++) {
+        if (w < warp) before += warpSum[w];
+        total += warpSum[w];
+    }
+    uint32_t pos = before + incl - mine;
+    uint32_t* out = b.cand + rawOff[a];
+    for (int j = lo; j < lo + per; j++) {
+        if (keep(j)) out[pos++] = buf[j];
+    }
+    if (tid == 0) {
+        b.ncand[a] = total;
+        atomicAdd(&b.counters[kCounterRaw], (unsigned long long)raw);
+        atomicAdd(&b.counters[kCounterUnique], (unsigned long long)total);
+    }
+}
+
+// One thread per read pair (2i, 2i+1) of the batch: flag candidates whose mate
+// is a candidate of the other read of the pair (include/util.hpp:1005-1143).
+__global__ void pair_flags_kernel(BatchArg b, const uint32_t* __restrict__ rawOff) {
+    const int pr = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a1 = 2 * pr;
+    if (a1 + 1 >= b.count) return;
+    const uint32_t* r1 = b.cand + rawOff[a1];
+    const uint32_t* r2 = b.cand + rawOff[a1 + 1];
+    uint8_t* f1 = b.paired + rawOff[a1];
+    uint8_t* f2 = b.paired + rawOff[a1 + 1];
+    const uint32_t n1 = b.ncand[a1], n2 = b.ncand[a1 + 1];
+    for (uint32_t i = 0; i < n1; i++) f1[i] = 0;
+    for (uint32_t i = 0; i < n2; i++) f2[i] = 0;
+    uint32_t x = 0, y = 0;
+    while (x < n1 && y < n2) {
+        const int e1 = (x + 1 < n1 && r1[x] / 2 == r1[x + 1] / 2) ? 2 : 1;
+        const int e2 = (y + 1 < n2 && r2[y] / 2 == r2[y + 1] / 2) ? 2 : 1;
+        const bool same = r1[x] / 2 == r2[y] / 2;
+        if (e1 == 1 && e2 == 1) {
+            if (same) {
+                if (r1[x] != r2[y]) {
+                    f1[x] = 1;
+                    f2[y] = 1;
+                }
+                x++;
+                y++;
+            } else if (r1[x] < r2[y]) {
+                x++;
+            } else {
+                y++;
+            }
+        } else if (e1 == 2 && e2 == 2) {
+            if (same) {
+                f1[x] = f1[x + 1] = 1;
+                f2[y] = f2[y + 1] = 1;
+                x += 2;
+                y += 2;
+            } else if (r1[x] < r2[y]) {
+                x += 2;
+            } else {
+                y += 2;
+            }
+        } else if (e1 == 2 && e2 == 1) {
+            if (same) {
+                if (r1[x] == r2[y]) {
+                    x++;
+                    f1[x] = 1;
+                    f2[y] = 1;
+                    x++;
+                    y++;
+                } else {
+                    f1[x] = 1;
+                    f2[y] = 1;
+                    x += 2;
+                    y++;
+                }
+            } else if (r1[x] < r2[y]) {
+                x += 2;
+            } else {
+                y++;
+            }
+        } else {
+            if (same) {
+                if (r1[x] == r2[y]) {
+                    y++;
+                    f1[x] = 1;
+                    f2[y] = 1;
+                    x++;
+                    y++;
+                } else {
+                    f1[x] = 1;
+                    f2[y] = 1;
+                    x++;
+                    y += 2;
+                }
+            } else if (r1[x] < r2[y]) {
+                x++;
+            } else {
+                y += 2;
+            }
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_table_init(Slot* t, uint64_t cap, cudaStream_t s) {
+    table_init_kernel<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(t, cap);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_table_count(const unsigned long long* keys, uint64_t n, Slot* tmp, uint32_t tmpMask,
+                               cudaStream_t s) {
+    table_count_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(keys, n, tmp, tmpMask);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_table_mark(const Slot* tmp, uint64_t cap, int maxValues, unsigned long long* packed,
+                              cudaStream_t s) {
+    table_mark_kernel<<<(unsigned)((cap + 1 + 255) / 256), 256, 0, s>>>(tmp, cap, maxValues, packed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_table_place(Slot* tmp, uint64_t cap, const unsigned long long* packedScan, int maxValues,
+                               Slot* fin, uint32_t finMask, uint32_t* /*cursor*/, cudaStream_t s) {
+    table_place_kernel<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(tmp, cap, packedScan, maxValues, fin, finMask);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_table_fill(const unsigned long long* keys, uint64_t n, const Slot* tmp, uint32_t tmpMask,
+                              uint32_t* cursor, uint32_t* values, cudaStream_t s) {
+    table_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(keys, n, tmp, tmpMask, cursor, values);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_table_sort(const Slot* fin, uint64_t finCap, uint32_t* values, cudaStream_t s) {
+    table_sort_kernel<<<(unsigned)((finCap + 255) / 256), 256, 0, s>>>(fin, finCap, values);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_query_count(StoreArg st, TablesArg tb, Params p, BatchArg b, cudaStream_t s) {
+    const uint64_t threads = (uint64_t)b.count * 32;
+    query_count_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(st, tb, p, b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_unique(StoreArg st, TablesArg tb, Params p, BatchArg b, int maxRawPerAnchor,
+                                 cudaStream_t s) {
+    int S = 32;
+    while (S < maxRawPerAnchor) S <<= 1;
+    const size_t smem = (size_t)S * sizeof(uint32_t);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(gather_unique_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    gather_unique_kernel<<<b.count, kGatherThreads, smem, s>>>(st, tb, p, b, b.rawCount, S);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pair_flags(BatchArg b, cudaStream_t s) {
+    const int pairs = b.count / 2;
+    if (pairs == 0) return cudaSuccess;
+    pair_flags_kernel<<<(pairs + 127) / 128, 128, 0, s>>>(b, b.rawCount);
+    return cudaGetLastError();
+}
+
+}  // namespace cg
