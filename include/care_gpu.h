@@ -157,6 +157,15 @@ int cg_build_tables(cg_ctx* ctx);
 int cg_correct(cg_ctx* ctx, uint64_t first_read, uint64_t num_anchors,
                uint8_t* out_flags, char* out_sequences, size_t out_pitch);
 
+/*
+ * Load the anchor classifier for CG_CORR_FOREST from a file image in the
+ * reference's forest format (reference: ForestClf, include/forest.hpp:38-55,
+ * 141-162; descriptor "13 extract_anchor_v3").  At most max_trees trees are
+ * used (0 = all; reference: maxForestTreesAnchor); the decision threshold is
+ * options.threshold_anchor.  Needed before cg_correct in forest mode.
+ */
+int cg_load_forest(cg_ctx* ctx, const void* data, size_t size, uint32_t max_trees);
+
 /* Counters of the context so far. */
 int cg_get_stats(const cg_ctx* ctx, cg_stats* out);
 

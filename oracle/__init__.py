@@ -64,6 +64,7 @@ def lib() -> ctypes.CDLL:
         L.orc_signatures.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, P]
         L.orc_candidates.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
         L.orc_correct.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, P, P, ctypes.c_size_t, ctypes.c_int, P]
+        L.orc_load_forest.argtypes = [P, P, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_float]
         _lib = L
     return _lib
 
@@ -89,6 +90,11 @@ class Oracle:
         L.orc_info(self._h, ctypes.byref(n), ctypes.byref(lmax), ctypes.byref(k), ctypes.byref(nm), ctypes.byref(bs))
         self.n, self.max_length, self.k, self.num_maps = n.value, lmax.value, k.value, nm.value
         self.build_seconds = bs.value
+
+    def load_forest(self, data: bytes, max_trees: int = 0xFFFFFFFF, threshold: float = 0.5):
+        buf = np.frombuffer(data, np.uint8)
+        if self._L.orc_load_forest(self._h, buf.ctypes.data, len(buf), max_trees, threshold) != 0:
+            raise ValueError("malformed forest file")
 
     def signatures(self, first: int, n: int) -> np.ndarray:
         out = np.zeros((n, self.num_maps), dtype=np.uint64)

@@ -126,8 +126,22 @@ struct Tables {
     std::vector<uint64_t> sigs;  // n * nmaps (read-major)
 };
 
+// reference: include/forest.hpp:21-67 (node layout, preorder file format)
+struct ForestNode {
+    uint8_t att;
+    uint8_t flag;  // bit 1: lhs is a leaf, bit 0: rhs is a leaf
+    double split;
+    uint32_t lhs, rhs;  // child index, or the leaf's float bits
+};
+
+struct Forest {
+    std::vector<std::vector<ForestNode>> trees;
+    float thresh = 0.5f;
+};
+
 struct Oracle {
     cg_options o;
+    Forest forest;
     Store s;
     Tables t;
     float qweight[256];
@@ -513,6 +527,54 @@ bool correctedAnchor(const Msa& m, const Props& p, const std::string& anchor, fl
     return true;
 }
 
+// reference: include/classification.hpp:748-797 (extract_anchor_v3)
+void anchorFeatures(const Msa& m, const Props& p, int i, float cov, float out[13]) {
+    const int pos = m.begin + i;
+    const float wsum = m.wA[pos] + m.wC[pos] + m.wG[pos] + m.wT[pos];
+    float weightCons = 0, countCons = 0;
+    switch (m.cons[pos]) {
+        case 'A': weightCons = m.wA[pos]; countCons = m.cA[pos]; break;
+        case 'C': weightCons = m.wC[pos]; countCons = m.cC[pos]; break;
+        case 'G': weightCons = m.wG[pos]; countCons = m.cG[pos]; break;
+        case 'T': weightCons = m.wT[pos]; countCons = m.cT[pos]; break;
+    }
+    out[0] = float(m.origCov[pos]) / m.cov[pos];
+    out[1] = m.origW[pos] / wsum;
+    out[2] = m.origW[pos] / m.origCov[pos];
+    out[3] = countCons / m.cov[pos];
+    out[4] = m.support[pos];
+    out[5] = weightCons / countCons;
+    out[6] = wsum / m.cov[pos];
+    out[7] = m.cov[pos] / cov;
+    out[8] = wsum / cov;
+    out[9] = p.avg_support;
+    out[10] = p.min_support;
+    out[11] = float(p.max_coverage) / cov;
+    out[12] = float(p.min_coverage) / cov;
+}
+
+// reference: include/forest.hpp:70-81 (prob) and 217-226 (decide)
+bool forestDecide(const Forest& f, const float* feats) {
+    float sum = 0.f;
+    for (const auto& tree : f.trees) {
+        size_t i = 0;
+        float prob;
+        while (true) {
+            const ForestNode& n = tree[i];
+            if (feats[n.att] <= n.split) {
+                if (n.flag / 2) { std::memcpy(&prob, &n.lhs, 4); break; }
+                i = n.lhs;
+            } else {
+                if (n.flag % 2) { std::memcpy(&prob, &n.rhs, 4); break; }
+                i = n.rhs;
+            }
+        }
+        sum += prob;
+        if (sum / f.trees.size() >= f.thresh) return true;
+    }
+    return false;
+}
+
 // ---------------------------------------------------------------- per anchor
 
 std::string decodeRead(const Store& s, uint64_t id) {
@@ -693,8 +755,24 @@ uint8_t correctOne(const Oracle& O, uint64_t anchor, const std::vector<uint32_t>
         buildMsa(m, anchorStr, anchorQ, kept, o.use_quality_scores != 0, O.qweight);
         cnt.msaBuilds++;
     }
-    // correctAnchorClassic: include/corrector.hpp:1423-1446
     const Props p = msaProperties(m, o.estimated_errorrate, o.estimated_coverage, o.m_coverage);
+    if (o.correction_type == CG_CORR_FOREST) {
+        // correctAnchorClf: include/corrector.hpp:1448-1472
+        corrected.assign(m.cons.begin() + m.begin, m.cons.begin() + m.end);
+        if (!p.isHQ) {
+            float feats[13];
+            for (int i = 0; i < La; i++) {
+                if (anchorStr[i] != m.cons[m.begin + i]) {
+                    anchorFeatures(m, p, i, o.estimated_coverage, feats);
+                    if (!forestDecide(O.forest, feats)) corrected[i] = anchorStr[i];
+                }
+            }
+        }
+        cnt.corrected++;
+        if (p.isHQ) cnt.hq++;
+        return uint8_t(CG_RESULT_CORRECTED | (p.isHQ ? CG_RESULT_HQ : 0));
+    }
+    // correctAnchorClassic: include/corrector.hpp:1423-1446
     if (!correctedAnchor(m, p, anchorStr, o.estimated_errorrate, o.estimated_coverage, o.m_coverage, corrected)) return 0;
     cnt.corrected++;
     if (p.isHQ) cnt.hq++;
@@ -724,6 +802,74 @@ void* orc_create(const cg_options* o, const char* seqs, const uint64_t* offsets,
 }
 
 void orc_destroy(void* h) { delete static_cast<Oracle*>(h); }
+
+// Forest in the reference's file format (include/forest.hpp:38-55, 141-162);
+// returns 0, or -1 on a malformed file.
+int orc_load_forest(void* h, const uint8_t* data, uint64_t size, uint32_t maxTrees, float thresh) {
+    Oracle* O = static_cast<Oracle*>(h);
+    uint64_t pos = 0;
+    auto rd = [&](void* dst, uint64_t n) {
+        if (pos + n > size) throw 1;
+        std::memcpy(dst, data + pos, n);
+        pos += n;
+    };
+    try {
+        uint64_t dl;
+        rd(&dl, 8);
+        std::string desc(dl, 0);
+        rd(&desc[0], dl);
+        if (desc != "13 extract_anchor_v3") return -1;
+        uint32_t nt;
+        rd(&nt, 4);
+        nt = std::min(nt, maxTrees);
+        O->forest.trees.assign(nt, {});
+        O->forest.thresh = thresh;
+        for (auto& tree : O->forest.trees) {
+            uint32_t nn;
+            rd(&nn, 4);
+            std::vector<std::pair<uint32_t, int>> stack;  // (node, side to fill: 0 lhs 1 rhs)
+            auto readNode = [&]() -> uint32_t {
+                ForestNode n;
+                rd(&n.att, 1);
+                rd(&n.split, 8);
+                rd(&n.flag, 1);
+                n.lhs = n.rhs = 0;
+                tree.push_back(n);
+                return uint32_t(tree.size() - 1);
+            };
+            // preorder: node, lhs subtree (or leaf prob), rhs subtree (or leaf prob)
+            std::vector<uint32_t> path;
+            uint32_t root = readNode();
+            path.push_back(root);
+            std::vector<int> state{0};
+            while (!path.empty()) {
+                const uint32_t cur = path.back();
+                int& st = state.back();
+                if (st == 2) {
+                    path.pop_back();
+                    state.pop_back();
+                    continue;
+                }
+                const bool leaf = st == 0 ? (tree[cur].flag / 2) != 0 : (tree[cur].flag % 2) != 0;
+                const int side = st;
+                st++;
+                if (leaf) {
+                    uint32_t bits;
+                    rd(&bits, 4);
+                    (side == 0 ? tree[cur].lhs : tree[cur].rhs) = bits;
+                } else {
+                    const uint32_t child = readNode();
+                    (side == 0 ? tree[cur].lhs : tree[cur].rhs) = child;
+                    path.push_back(child);
+                    state.push_back(0);
+                }
+            }
+        }
+    } catch (int) {
+        return -1;
+    }
+    return 0;
+}
 
 int orc_info(void* h, uint64_t* nreads, int* lmax, int* k, int* nmaps, double* buildSeconds) {
     const Oracle* O = static_cast<Oracle*>(h);

@@ -88,7 +88,7 @@ class CgStats(ctypes.Structure):
 # every symbol include/care_gpu.h declares
 EXPORTED = ["cg_default_options", "cg_create", "cg_destroy", "cg_last_error", "cg_append_reads",
             "cg_build_tables", "cg_correct", "cg_get_stats", "cg_get_read_info", "cg_get_signatures",
-            "cg_get_candidates", "cg_correct_files"]
+            "cg_get_candidates", "cg_correct_files", "cg_load_forest"]
 
 
 def gpu_lib() -> ctypes.CDLL:
@@ -109,6 +109,7 @@ def gpu_lib() -> ctypes.CDLL:
         L.cg_get_candidates.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
         L.cg_correct_files.argtypes = [P, P, ctypes.c_int, ctypes.c_char_p, P, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
+        L.cg_load_forest.argtypes = [P, P, ctypes.c_size_t, ctypes.c_uint32]
         for f in EXPORTED:
             if f not in ("cg_destroy", "cg_default_options", "cg_last_error"):
                 getattr(L, f).restype = ctypes.c_int
@@ -146,6 +147,10 @@ class CareGpu:
 
     def build_tables(self):
         self._check(self._L.cg_build_tables(self._h), "cg_build_tables")
+
+    def load_forest(self, data: bytes, max_trees: int = 0):
+        buf = np.frombuffer(data, np.uint8)
+        self._check(self._L.cg_load_forest(self._h, buf.ctypes.data, len(buf), max_trees), "cg_load_forest")
 
     def read_info(self):
         n, l = ctypes.c_uint64(), ctypes.c_int32()

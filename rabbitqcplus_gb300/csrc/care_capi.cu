@@ -91,9 +91,13 @@ struct cg_ctx {
     Params params{};
 
     // batch buffers
-    DevBuf qrange, rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, nfinal, flags, out, counters;
+    DevBuf qrange, rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, flen, nfinal, flags, out, counters;
     DevBuf scanTmp;
     uint32_t* hPinned = nullptr;  // 2 words: total raw, max raw
+
+    // forest classifier (CG_CORR_FOREST)
+    DevBuf forestNodes, treeOffsets;
+    int numTrees = 0;
 
     cg_stats stats{};
 };
@@ -166,6 +170,12 @@ void make_params(cg_ctx* c) {
     p.useQuality = o.use_quality_scores != 0;
     p.excludeAmbiguous = o.exclude_ambiguous_reads != 0;
     p.paired = o.pair_mode == CG_PAIR_PE;
+    p.correctionType = o.correction_type;
+    p.estimatedCoverage = o.estimated_coverage;
+    p.forestNodes = c->forestNodes.as<ForestNode>();
+    p.treeOffsets = c->treeOffsets.as<uint32_t>();
+    p.numTrees = c->numTrees;
+    p.forestThreshold = o.threshold_anchor;
     // include/qualityscoreweights.hpp:17-33
     for (int i = 0; i < 256; i++) {
         const float e = i < 33 ? 1.0f : std::pow(10.0f, -(i - 33) / 10.0f);
@@ -347,6 +357,7 @@ BatchArg batch_arg(cg_ctx* c, uint64_t first, int count) {
     b.fshift = c->fshift.as<int16_t>();
     b.forient = c->forient.as<uint8_t>();
     b.fweight = c->fweight.as<float>();
+    b.flen = c->flen.as<uint16_t>();
     b.nfinal = c->nfinal.as<uint32_t>();
     b.flags = c->flags.as<uint8_t>();
     b.out = c->out.as<char>();
@@ -382,6 +393,7 @@ int run_candidates(cg_ctx* c, uint64_t first, int count) {
     CG_CUDA(c, c->fshift.ensure(cap * sizeof(int16_t)));
     CG_CUDA(c, c->forient.ensure(cap));
     CG_CUDA(c, c->fweight.ensure(cap * sizeof(float)));
+    CG_CUDA(c, c->flen.ensure(cap * sizeof(uint16_t)));
     b = batch_arg(c, first, count);
     CG_CUDA(c, launch_gather_unique(st, c->tables, c->params, b, (int)std::max<uint32_t>(maxRaw, 1), c->stream));
     c->stats.kernel_launches += 1;
@@ -403,7 +415,7 @@ int run_batch(cg_ctx* c, uint64_t first, int count, uint8_t* hFlags, char* hOut,
     CG_CUDA(c, cudaEventRecord(c->st1, c->stream));
     CG_CUDA(c, launch_align_filter(st, c->params, b, c->stream));
     CG_CUDA(c, cudaEventRecord(c->st2, c->stream));
-    CG_CUDA(c, launch_msa_correct(st, c->params, b, c->stream));
+    CG_CUDA(c, launch_msa_correct(st, c->params, b, (int)std::max<uint32_t>(c->hPinned[1], 1), c->stream));
     CG_CUDA(c, cudaEventRecord(c->st3, c->stream));
     c->stats.kernel_launches += 2;
     c->stats.align_launches += 1;
@@ -451,7 +463,7 @@ int cg_create(const cg_options* o, cg_ctx** out) {
     if (!(o->estimated_coverage > 0.0f)) return CG_ERR_INVALID_ARGUMENT;
     if (o->pair_mode != CG_PAIR_SE && o->pair_mode != CG_PAIR_PE) return CG_ERR_INVALID_ARGUMENT;
     if (o->correct_candidates) return CG_ERR_UNSUPPORTED;
-    if (o->correction_type != CG_CORR_CLASSIC) return CG_ERR_UNSUPPORTED;
+    if (o->correction_type != CG_CORR_CLASSIC && o->correction_type != CG_CORR_FOREST) return CG_ERR_UNSUPPORTED;
     cg_ctx* c = new (std::nothrow) cg_ctx();
     if (!c) return CG_ERR_OUT_OF_MEMORY;
     c->o = *o;
@@ -482,8 +494,8 @@ void cg_destroy(cg_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     release_tables(c);
     for (DevBuf* b : {&c->enc, &c->len, &c->hilo, &c->qual, &c->ambig, &c->sig, &c->qrange, &c->rawCount, &c->cand,
-                      &c->ncand, &c->paired, &c->aln, &c->fid, &c->fshift, &c->forient, &c->fweight, &c->nfinal,
-                      &c->flags, &c->out, &c->counters, &c->scanTmp})
+                      &c->ncand, &c->paired, &c->aln, &c->fid, &c->fshift, &c->forient, &c->fweight, &c->flen, &c->nfinal,
+                      &c->flags, &c->out, &c->counters, &c->scanTmp, &c->forestNodes, &c->treeOffsets})
         b->release();
     if (c->hPinned) cudaFreeHost(c->hPinned);
     for (cudaEvent_t ev : {c->ev0, c->ev1, c->st0, c->st1, c->st2, c->st3})
@@ -554,6 +566,8 @@ int cg_correct(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* out_flags, char
     if (!out_flags || !out_seq || out_pitch < (size_t)c->lmax)
         return fail(c, CG_ERR_INVALID_ARGUMENT, "output buffers missing or pitch below %d", c->lmax);
     if (c->params.paired && ((first | num) & 1)) return fail(c, CG_ERR_INVALID_ARGUMENT, "paired mode needs even ranges");
+    if (c->o.correction_type == CG_CORR_FOREST && c->numTrees == 0)
+        return fail(c, CG_ERR_STATE, "forest correction requested but no forest loaded (cg_load_forest)");
     CG_CUDA(c, cudaSetDevice(c->device));
     int B = c->o.batch_anchors > 0 ? c->o.batch_anchors : 65536;
     if (c->params.paired && (B & 1)) B++;
@@ -609,6 +623,77 @@ int cg_get_signatures(cg_ctx* c, uint64_t first, uint64_t n, uint64_t* out) {
                               n * sizeof(uint64_t), cudaMemcpyDeviceToHost));
         for (uint64_t i = 0; i < n; i++) out[i * c->nmaps + h] = col[i];
     }
+    return CG_OK;
+}
+
+int cg_load_forest(cg_ctx* c, const void* data, size_t size, uint32_t max_trees) {
+    if (!c || !data) return CG_ERR_INVALID_ARGUMENT;
+    // reference file format: include/forest.hpp:38-55 (preorder nodes) and 141-162
+    const uint8_t* d = static_cast<const uint8_t*>(data);
+    size_t pos = 0;
+    auto rd = [&](void* dst, size_t n) {
+        if (pos + n > size) return false;
+        std::memcpy(dst, d + pos, n);
+        pos += n;
+        return true;
+    };
+    uint64_t dl = 0;
+    if (!rd(&dl, 8) || dl > 4096 || pos + dl > size) return fail(c, CG_ERR_INVALID_ARGUMENT, "forest: bad header");
+    const std::string desc(reinterpret_cast<const char*>(d + pos), dl);
+    pos += dl;
+    if (desc != "13 extract_anchor_v3")
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "forest: descriptor '%s' is not 13 extract_anchor_v3", desc.c_str());
+    uint32_t nt = 0;
+    if (!rd(&nt, 4) || nt == 0) return fail(c, CG_ERR_INVALID_ARGUMENT, "forest: no trees");
+    nt = std::min(nt, max_trees == 0 ? nt : max_trees);
+    std::vector<ForestNode> nodes;
+    std::vector<uint32_t> offsets;
+    for (uint32_t t = 0; t < nt; t++) {
+        uint32_t reserve = 0;
+        if (!rd(&reserve, 4)) return fail(c, CG_ERR_INVALID_ARGUMENT, "forest: truncated tree %u", t);
+        const uint32_t base = (uint32_t)nodes.size();
+        offsets.push_back(base);
+        // iterative preorder: node, then lhs (leaf prob or subtree), then rhs
+        std::vector<std::pair<uint32_t, int>> stack;
+        auto readNode = [&](uint32_t& idx) {
+            ForestNode n{};
+            if (!rd(&n.att, 1) || !rd(&n.split, 8) || !rd(&n.flag, 1) || n.att >= 13 || n.flag > 3) return false;
+            nodes.push_back(n);
+            idx = (uint32_t)nodes.size() - 1 - base;
+            return true;
+        };
+        uint32_t root;
+        if (!readNode(root)) return fail(c, CG_ERR_INVALID_ARGUMENT, "forest: bad node in tree %u", t);
+        stack.push_back({root, 0});
+        while (!stack.empty()) {
+            auto& top = stack.back();
+            if (top.second == 2) {
+                stack.pop_back();
+                continue;
+            }
+            const uint32_t cur = top.first;
+            const int side = top.second++;
+            const bool leaf = side == 0 ? (nodes[base + cur].flag & 2u) : (nodes[base + cur].flag & 1u);
+            if (leaf) {
+                uint32_t bits;
+                if (!rd(&bits, 4)) return fail(c, CG_ERR_INVALID_ARGUMENT, "forest: truncated leaf");
+                (side == 0 ? nodes[base + cur].lhs : nodes[base + cur].rhs) = bits;
+            } else {
+                uint32_t child;
+                if (!readNode(child)) return fail(c, CG_ERR_INVALID_ARGUMENT, "forest: bad node in tree %u", t);
+                (side == 0 ? nodes[base + cur].lhs : nodes[base + cur].rhs) = child;
+                stack.push_back({child, 0});
+            }
+        }
+    }
+    CG_CUDA(c, cudaSetDevice(c->device));
+    CG_CUDA(c, c->forestNodes.ensure(nodes.size() * sizeof(ForestNode)));
+    CG_CUDA(c, c->treeOffsets.ensure(offsets.size() * sizeof(uint32_t)));
+    CG_CUDA(c, cudaMemcpy(c->forestNodes.p, nodes.data(), nodes.size() * sizeof(ForestNode), cudaMemcpyHostToDevice));
+    CG_CUDA(c, cudaMemcpy(c->treeOffsets.p, offsets.data(), offsets.size() * sizeof(uint32_t),
+                          cudaMemcpyHostToDevice));
+    c->numTrees = (int)nt;
+    if (c->built) make_params(c);
     return CG_OK;
 }
 

@@ -81,8 +81,27 @@ struct Params {
     int useQuality;
     int excludeAmbiguous;
     int paired;
+    int correctionType;         // CG_CORR_*
+    float estimatedCoverage;
+    // forest decision (correctionType == CG_CORR_FOREST)
+    const struct ForestNode* forestNodes;
+    const uint32_t* treeOffsets;  // first node of each tree
+    int numTrees;
+    float forestThreshold;
     float qweight[256];
 };
+
+// One forest node (reference: include/forest.hpp:21-30): go left when
+// feature[att] <= split; flag bit 1 = lhs is a leaf, bit 0 = rhs is a leaf;
+// a leaf side holds the float probability's bits, an inner side the index of
+// the child within the tree.
+struct ForestNode {
+    double split;
+    uint32_t lhs, rhs;
+    uint8_t att, flag;
+    uint8_t pad[6];
+};
+static_assert(sizeof(ForestNode) == 24, "forest node layout");
 
 // ---------------------------------------------------------------- launches
 // Every launcher enqueues on `s` and returns the launch status.
@@ -130,6 +149,7 @@ struct BatchArg {
     int16_t* fshift;        // [totalRaw]
     uint8_t* forient;       // [totalRaw] 1 fwd, 2 rc
     float* fweight;         // [totalRaw]
+    uint16_t* flen;         // [totalRaw] candidate length
     uint32_t* nfinal;       // [count]
     uint8_t* flags;         // [count] CG_RESULT_*
     char* out;              // [count][outPitch]
@@ -153,8 +173,7 @@ cudaError_t launch_gather_unique(StoreArg st, TablesArg tb, Params p, BatchArg b
                                  cudaStream_t s);
 cudaError_t launch_pair_flags(BatchArg b, cudaStream_t s);
 cudaError_t launch_align_filter(StoreArg st, Params p, BatchArg b, cudaStream_t s);
-cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, cudaStream_t s);
-size_t msa_smem_bytes(int maxCols);
+cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, int maxRows, cudaStream_t s);
 
 }  // namespace cg
 

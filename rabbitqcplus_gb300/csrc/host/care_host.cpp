@@ -3,6 +3,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <fstream>
+#include <iterator>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -111,6 +113,13 @@ Corrected runCorrection(const ProgramOptions& o) {
               "cg_append_reads");
     }
     check(ctx.c, cg_build_tables(ctx.c), "cg_build_tables");
+    if (o.correctionType == CorrectionType::Forest) {
+        // src/main_correct_cpu.cpp:125-134: a forest file is required
+        std::ifstream is(o.mlForestfileAnchor, std::ios::binary);
+        if (!is) throw std::runtime_error("Loading classifier file failed! " + o.mlForestfileAnchor);
+        std::vector<char> bytes((std::istreambuf_iterator<char>(is)), std::istreambuf_iterator<char>());
+        check(ctx.c, cg_load_forest(ctx.c, bytes.data(), bytes.size(), o.maxForestTreesAnchor), "cg_load_forest");
+    }
     uint64_t nr = 0;
     int32_t lmax = 0;
     check(ctx.c, cg_get_read_info(ctx.c, &nr, &lmax), "cg_get_read_info");

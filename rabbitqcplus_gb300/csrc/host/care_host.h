@@ -51,6 +51,8 @@ struct ProgramOptions {
     CorrectionType correctionTypeCands = CorrectionType::Classic;
     float thresholdAnchor = .5f;
     float pairedFilterThreshold = 0.06f;
+    uint32_t maxForestTreesAnchor = 0xffffffffu;
+    std::string mlForestfileAnchor = "";
     bool showProgress = false;
     int threads = 1;
     std::vector<int> deviceIds;

@@ -22,62 +22,195 @@ namespace {
 // ---------------------------------------------------------------- alignment
 
 constexpr int kAlignWarps = 4;  // warps per block, one anchor per warp
-
-// mismatches between `sh` shifted left by `sl` bases and `ot`, over `ov` bases
-__device__ __forceinline__ int mismatches(const uint32_t* __restrict__ shHi, const uint32_t* __restrict__ shLo,
-                                          const uint32_t* __restrict__ otHi, const uint32_t* __restrict__ otLo,
-                                          int sl, int ov) {
-    const int parts = (ov + 31) >> 5;
-    const int rem = (parts << 5) - ov;
-    const int ws = sl >> 5, bs = sl & 31;
-    int m = 0;
-    for (int i = 0; i < parts; i++) {
-        const uint32_t hi = __funnelshift_l(shHi[i + ws + 1], shHi[i + ws], bs);
-        const uint32_t lo = __funnelshift_l(shLo[i + ws + 1], shLo[i + ws], bs);
-        uint32_t x = (hi ^ otHi[i]) | (lo ^ otLo[i]);
-        if (i == parts - 1 && rem != 0) x &= 0xffffffffu << rem;
-        m += __popc(x);
-    }
-    return m;
-}
+constexpr unsigned kFull = 0xffffffffu;
 
 struct AlnRes {
     int score, overlap, shift, nOps;
     bool valid;
 };
 
-// Warp-cooperative shifted Hamming alignment.  Every lane evaluates a subset
-// of the shifts; the winner is the first shift in the reference's scan order
-// (0, 1, .., La-minov, then -1, -2, .., -(Lc-minov)) among those with the
-// smallest score whose mismatch count is below int(overlap * maxErrorRate).
-// The reference's early exits only skip shifts that cannot win, so this
-// full evaluation returns the same (score, shift).
-__device__ AlnRes align_warp(const uint32_t* aHi, const uint32_t* aLo, int La, const uint32_t* cHi,
-                             const uint32_t* cLo, int Lc, int minov, float rate) {
+// Warp-cooperative shifted Hamming alignment of one candidate orientation.
+//
+// Each lane evaluates shifts t = lane, lane+32, ... in the reference's scan
+// order (0, 1, .., La-minov, then -1, -2, .., -(Lc-minov)).  The winner is the
+// first shift with the smallest score among those whose mismatch count stays
+// below int(overlap * maxErrorRate); the reference's early exits only skip
+// shifts that cannot win, so evaluating all of them returns its (score, shift).
+//
+// The non-shifted side of every comparison lives in registers (aR: anchor,
+// cR: candidate, hi and lo planes); the shifted side streams from shared
+// memory one word per step.  A lane stops once its mismatch count reaches its
+// limit (the count only grows), and the warp leaves the word loop when no lane
+// is still running.
+template <int MAXW>
+__device__ __forceinline__ AlnRes align_warp(const uint32_t* __restrict__ aS, const uint32_t* __restrict__ cS, int wp,
+                                             const uint32_t (&aR)[2][MAXW], const uint32_t (&cR)[2][MAXW], int La,
+                                             int Lc, int minov, float rate) {
     const int tb = La + Lc;
     const int n1 = max(0, La - minov + 1);
     const int n2 = max(0, Lc - minov);
+    const int lane = (int)lane_id();
     uint32_t best = 0xffffffffu;
-    for (int t = (int)lane_id(); t < n1 + n2; t += 32) {
-        int s, ov;
+    for (int t0 = 0; t0 < n1 + n2; t0 += 32) {
+        const int t = t0 + lane;
+        int s = 0, ov = 0;
         if (t < n1) {
             s = t;
             ov = min(La - s, Lc);
-        } else {
+        } else if (t < n1 + n2) {
             s = -(t - n1 + 1);
             ov = min(La, Lc + s);
         }
         const int maxErr = (int)__fmul_rn((float)ov, rate);
-        if (maxErr > 0 && ov > 0) {
-            const int m = s >= 0 ? mismatches(aHi, aLo, cHi, cLo, s, ov) : mismatches(cHi, cLo, aHi, aLo, -s, ov);
+        bool run = t < n1 + n2 && maxErr > 0 && ov > 0;
+        const bool fwdShift = s >= 0;
+        const int sl = fwdShift ? s : -s;
+        const int parts = (ov + 31) >> 5;
+        const int rem = (parts << 5) - ov;
+        const int ws = sl >> 5, bs = sl & 31;
+        const uint32_t* sh = fwdShift ? aS : cS;
+        uint32_t curH = 0, curL = 0;
+        if (run) {
+            curH = sh[ws];
+            curL = sh[wp + ws];
+        }
+        int m = 0;
+#pragma unroll
+        for (int i = 0; i < MAXW; i++) {
+            const bool act = run && i < parts;
+            if (!__any_sync(kFull, act)) break;
+            if (act) {
+                const uint32_t nxH = sh[ws + i + 1];
+                const uint32_t nxL = sh[wp + ws + i + 1];
+                const uint32_t hi = __funnelshift_l(nxH, curH, bs);
+                const uint32_t lo = __funnelshift_l(nxL, curL, bs);
+                const uint32_t oh = fwdShift ? cR[0][i] : aR[0][i];
+                const uint32_t ol = fwdShift ? cR[1][i] : aR[1][i];
+                uint32_t x = (hi ^ oh) | (lo ^ ol);
+                if (i == parts - 1 && rem != 0) x &= 0xffffffffu << rem;
+                m += __popc(x);
+                curH = nxH;
+                curL = nxL;
+                if (m >= maxErr) run = false;
+            }
+        }
+        if (run) {
             const int score = m + tb - 2 * ov;
-            if (m < maxErr && score < tb) {
+            if (score < tb) {
                 const uint32_t key = ((uint32_t)score << 16) | (uint32_t)t;
                 best = key < best ? key : best;
             }
         }
     }
-    best = __reduce_min_sync(0xffffffffu, best);
+    best = __reduce_min_sync(kFull, best);
+    AlnRes r;
+    int bestShift, bestScore;
+    if (best == 0xffffffffu) {
+        bestShift = -Lc;
+        bestScore = tb;
+    } else {
+        const int t = (int)(best & 0xffffu);
+        bestScore = (int)(best >> 16);
+        bestShift = t < n1 ? t : -(t - n1 + 1);
+    }
+    r.valid = bestShift != -Lc;
+    const int cb = max(-bestShift, 0);
+    const int ce = min(Lc, La - bestShift);
+    r.overlap = ce - cb;
+    r.score = bestScore;
+    r.shift = bestShift;
+    r.nOps = bestScore - tb + 2 * r.overlap;
+    return r;
+}
+
+// Register-resident variant for reads of at most 32*MAXW bases.
+//
+// Shifts are split by direction and lane l takes shifts 32k+l (right, anchor
+// shifted) and 32k+l+1 (left, candidate shifted), so a lane's bit offset is
+// the same in every iteration k and only its word offset advances.  Each lane
+// therefore funnel-shifts the shifted sequence once (SA: per anchor, SC: per
+// candidate orientation) and iteration k, word i reads SA[k+i] / SC[k+i]
+// from registers; the inner loop is XOR/OR/POPC only.  The words compared are
+// exactly those of align_warp (padding words are zero), so the result is the
+// same.  maxErrTab[ov] holds int(float(ov) * maxErrorRate).
+template <int MAXW>
+struct ShiftedRegs {
+    uint32_t h[2 * MAXW - 1], l[2 * MAXW - 1];
+};
+
+template <int MAXW>
+__device__ __forceinline__ void load_shifted(ShiftedRegs<MAXW>& r, const uint32_t* __restrict__ hi,
+                                             const uint32_t* __restrict__ lo, int wp, int wordOff, int bs) {
+#pragma unroll
+    for (int j = 0; j < 2 * MAXW - 1; j++) {
+        const int x = j + wordOff;
+        const uint32_t h0 = x < wp ? hi[x] : 0u, h1 = x + 1 < wp ? hi[x + 1] : 0u;
+        const uint32_t l0 = x < wp ? lo[x] : 0u, l1 = x + 1 < wp ? lo[x + 1] : 0u;
+        r.h[j] = __funnelshift_l(h1, h0, bs);
+        r.l[j] = __funnelshift_l(l1, l0, bs);
+    }
+}
+
+template <int MAXW, bool LEFT>
+__device__ __forceinline__ void scan_direction(const ShiftedRegs<MAXW>& S, const uint32_t (&O)[2][MAXW], int n,
+                                               int La, int Lc, int tb, int tBase, const int16_t* maxErrTab,
+                                               uint32_t& best) {
+    const int lane = (int)lane_id();
+#pragma unroll
+    for (int k = 0; k < MAXW; k++) {
+        if (32 * k >= n) break;
+        const int tl = 32 * k + lane;
+        const bool active = tl < n;
+        const int sl = LEFT ? tl + 1 : tl;
+        const int ov = active ? (LEFT ? min(La, Lc - sl) : min(La - sl, Lc)) : 0;
+        const int maxErr = maxErrTab[ov];
+        bool run = active && maxErr > 0 && ov > 0;
+        const int parts = (ov + 31) >> 5;
+        const int rem = (parts << 5) - ov;
+        int m = 0;
+#pragma unroll
+        for (int i = 0; i < MAXW; i++) {
+            const bool act = run && i < parts;
+            if (!__any_sync(kFull, act)) break;
+            if (act) {
+                uint32_t x = (S.h[k + i] ^ O[0][i]) | (S.l[k + i] ^ O[1][i]);
+                if (i == parts - 1 && rem != 0) x &= 0xffffffffu << rem;
+                m += __popc(x);
+                if (m >= maxErr) run = false;
+            }
+        }
+        if (run) {
+            const int score = m + tb - 2 * ov;
+            if (score < tb) {
+                const uint32_t key = ((uint32_t)score << 16) | (uint32_t)(tBase + tl);
+                best = key < best ? key : best;
+            }
+        }
+    }
+}
+
+template <int MAXW>
+__device__ __forceinline__ AlnRes align_regs(const ShiftedRegs<MAXW>& SA, const uint32_t (&A)[2][MAXW],
+                                             const uint32_t* __restrict__ cHi, const uint32_t* __restrict__ cLo,
+                                             int wp, int La, int Lc, int minov, const int16_t* maxErrTab) {
+    const int tb = La + Lc;
+    const int n1 = max(0, La - minov + 1);
+    const int n2 = max(0, Lc - minov);
+    const int lane = (int)lane_id();
+    uint32_t C[2][MAXW];
+#pragma unroll
+    for (int i = 0; i < MAXW; i++) {
+        C[0][i] = i < wp ? cHi[i] : 0u;
+        C[1][i] = i < wp ? cLo[i] : 0u;
+    }
+    uint32_t best = 0xffffffffu;
+    scan_direction<MAXW, false>(SA, C, n1, La, Lc, tb, 0, maxErrTab, best);
+    if (n2 > 0) {
+        ShiftedRegs<MAXW> SC;
+        load_shifted<MAXW>(SC, cHi, cLo, wp, lane == 31 ? 1 : 0, (lane + 1) & 31);
+        scan_direction<MAXW, true>(SC, A, n2, La, Lc, tb, n1, maxErrTab, best);
+    }
+    best = __reduce_min_sync(kFull, best);
     AlnRes r;
     int bestShift, bestScore;
     if (best == 0xffffffffu) {
@@ -131,16 +264,24 @@ __device__ __forceinline__ uint2 pack_aln(const AlnRes& r, int ori) {
 
 // One warp per anchor: align all candidates, choose orientations, apply the
 // mismatch-ratio filter and write the filtered candidate list in order.
-__global__ void __launch_bounds__(kAlignWarps * 32) align_filter_kernel(StoreArg st, Params p, BatchArg b,
+// Shared memory per warp: anchor hi/lo, candidate fwd hi/lo, rc hi/lo planes.
+template <int MAXW, bool REGS>
+__global__ void __launch_bounds__(kAlignWarps * 32, REGS ? 6 : 1) align_filter_kernel(StoreArg st, Params p, BatchArg b,
                                                                         const uint32_t* __restrict__ rawOff) {
     extern __shared__ uint32_t smem[];
     const int warp = threadIdx.x >> 5;
-    const uint32_t lane = lane_id();
+    const int lane = (int)lane_id();
+    const int wp = st.wp;
+    int16_t* maxErrTab = reinterpret_cast<int16_t*>(smem + kAlignWarps * 6 * wp);
+    if (REGS) {
+        for (int i = threadIdx.x; i <= st.lmax; i += blockDim.x)
+            maxErrTab[i] = (int16_t)(int)__fmul_rn((float)i, p.maxErrorRate);
+        __syncthreads();
+    }
     const int a = blockIdx.x * kAlignWarps + warp;
     if (a >= b.count) return;
-    const int wp = st.wp;
-    uint32_t* aHL = smem + warp * 6 * wp;  // anchor hi, lo; candidate fwd hi, lo, rc hi, lo
-    uint32_t* cHL = aHL + 2 * wp;
+    uint32_t* aS = smem + warp * 6 * wp;
+    uint32_t* cS = aS + 2 * wp;
     const uint64_t aid = b.first + (uint64_t)a;
     const int La = st.len[aid];
     const uint32_t nc = b.ncand[a];
@@ -150,17 +291,44 @@ __global__ void __launch_bounds__(kAlignWarps * 32) align_filter_kernel(StoreArg
         return;
     }
     const uint32_t* ahl = st.hilo + aid * 4 * (uint64_t)wp;  // forward planes
-    for (int i = (int)lane; i < 2 * wp; i += 32) aHL[i] = ahl[i];
+    for (int i = lane; i < 2 * wp; i += 32) aS[i] = ahl[i];
+    __syncwarp();
+    uint32_t aR[2][MAXW];
+#pragma unroll
+    for (int i = 0; i < MAXW; i++) {
+        aR[0][i] = i < wp ? aS[i] : 0u;
+        aR[1][i] = i < wp ? aS[wp + i] : 0u;
+    }
     const int minov = max(p.minOverlap, (int)__fmul_rn((float)La, p.minOverlapRatio));
+    ShiftedRegs<MAXW> SA;
+    if (REGS) load_shifted<MAXW>(SA, aS, aS + wp, wp, 0, lane);
     for (uint32_t j = 0; j < nc; j++) {
         const uint32_t id = b.cand[base + j];
         const int Lc = st.len[id];
         const uint32_t* chl = st.hilo + (uint64_t)id * 4 * wp;
         __syncwarp();
-        for (int i = (int)lane; i < 4 * wp; i += 32) cHL[i] = chl[i];
+        for (int i = lane; i < 4 * wp; i += 32) cS[i] = chl[i];
         __syncwarp();
-        const AlnRes f = align_warp(aHL, aHL + wp, La, cHL, cHL + wp, Lc, minov, p.maxErrorRate);
-        const AlnRes r = align_warp(aHL, aHL + wp, La, cHL + 2 * wp, cHL + 3 * wp, Lc, minov, p.maxErrorRate);
+        if (REGS) {
+            const AlnRes f = align_regs<MAXW>(SA, aR, cS, cS + wp, wp, La, Lc, minov, maxErrTab);
+            const AlnRes r = align_regs<MAXW>(SA, aR, cS + 2 * wp, cS + 3 * wp, wp, La, Lc, minov, maxErrTab);
+            const int ori = choose_orientation(f, r, La, p.minOverlapRatio, p.minOverlap, p.orientMaxErrorRate);
+            if (lane == 0) b.aln[base + j] = pack_aln(ori == 2 ? r : f, ori);
+            continue;
+        }
+        uint32_t cR[2][MAXW];
+#pragma unroll
+        for (int i = 0; i < MAXW; i++) {
+            cR[0][i] = i < wp ? cS[i] : 0u;
+            cR[1][i] = i < wp ? cS[wp + i] : 0u;
+        }
+        const AlnRes f = align_warp<MAXW>(aS, cS, wp, aR, cR, La, Lc, minov, p.maxErrorRate);
+#pragma unroll
+        for (int i = 0; i < MAXW; i++) {
+            cR[0][i] = i < wp ? cS[2 * wp + i] : 0u;
+            cR[1][i] = i < wp ? cS[3 * wp + i] : 0u;
+        }
+        const AlnRes r = align_warp<MAXW>(aS, cS + 2 * wp, wp, aR, cR, La, Lc, minov, p.maxErrorRate);
         const int ori = choose_orientation(f, r, La, p.minOverlapRatio, p.minOverlap, p.orientMaxErrorRate);
         if (lane == 0) b.aln[base + j] = pack_aln(ori == 2 ? r : f, ori);
     }
@@ -178,9 +346,9 @@ __global__ void __launch_bounds__(kAlignWarps * 32) align_filter_kernel(StoreArg
                 c2 += ratio < p.mm4;
             }
         }
-        c0 = __reduce_add_sync(0xffffffffu, c0);
-        c1 = __reduce_add_sync(0xffffffffu, c1);
-        c2 = __reduce_add_sync(0xffffffffu, c2);
+        c0 = __reduce_add_sync(kFull, c0);
+        c1 = __reduce_add_sync(kFull, c1);
+        c2 = __reduce_add_sync(kFull, c2);
         thr = -3.402823466e+38f;  // std::numeric_limits<float>::lowest()
         if (c0 > 0 || c1 > 0 || c2 > 0) {
             if ((float)c0 >= p.goodAlignmentsCountThreshold) thr = p.mm2;
@@ -207,15 +375,17 @@ __global__ void __launch_bounds__(kAlignWarps * 32) align_filter_kernel(StoreArg
                 if (p.paired && b.paired[base + j]) keep = true;
             }
         }
-        const uint32_t m = __ballot_sync(0xffffffffu, keep);
-        aligned += __popc(__ballot_sync(0xffffffffu, isAligned));
+        const uint32_t m = __ballot_sync(kFull, keep);
+        aligned += __popc(__ballot_sync(kFull, isAligned));
         if (keep) {
             const uint32_t pos = kept + __popc(m & ((1u << lane) - 1u));
             const int ov = (int)(v.x >> 16);
             const int nOps = (int)(int16_t)(v.y & 0xffffu);
-            b.fid[base + pos] = b.cand[base + j];
+            const uint32_t cid = b.cand[base + j];
+            b.fid[base + pos] = cid;
             b.fshift[base + pos] = (int16_t)(v.x & 0xffffu);
             b.forient[base + pos] = (uint8_t)(v.y >> 16);
+            b.flen[base + pos] = st.len[cid];
             // reference: include/hostdevicefunctions.cuh:93-95 (calculateOverlapWeight)
             b.fweight[base + pos] =
                 __fsub_rn(1.0f, __fsqrt_rn(__fdiv_rn((float)nOps, __fmul_rn((float)ov, p.maxErrorRate))));
@@ -231,55 +401,95 @@ __global__ void __launch_bounds__(kAlignWarps * 32) align_filter_kernel(StoreArg
 
 // ---------------------------------------------------------------- MSA
 
-constexpr int kMsaThreads = 128;
-constexpr uint8_t kRemoved = 0x80;
+constexpr int kMsaThreadsMin = 128;
+constexpr int kMsaCols = 4;  // columns owned per thread
+constexpr int kMsaChunkRows = 512;
 
-__device__ __forceinline__ float block_min_f(float v, float* red) {
-    for (int d = 16; d > 0; d >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, d));
-    const int warp = threadIdx.x >> 5;
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) red[warp] = v;
-    __syncthreads();
-    float r = red[0];
-    for (int w = 1; w < kMsaThreads / 32; w++) r = fminf(r, red[w]);
-    return r;
-}
+struct RowMeta {
+    const uint32_t* enc;  // candidate's 2-bit row
+    const uint8_t* qual;  // candidate's qualities (or null)
+    float weight;
+    int16_t shift;
+    uint16_t len;
+    uint8_t rc;
+    uint8_t pad[7];
+};
+static_assert(sizeof(RowMeta) == 32, "row meta layout");
 
-__device__ __forceinline__ int block_reduce_i(int v, int* red, int op /*0 min 1 max 2 sum*/) {
+template <class T>
+__device__ __forceinline__ T block_reduce(T v, T* red, int op /*0 min 1 max 2 sum*/) {
     for (int d = 16; d > 0; d >>= 1) {
-        const int o = __shfl_xor_sync(0xffffffffu, v, d);
-        v = op == 0 ? min(v, o) : op == 1 ? max(v, o) : v + o;
+        const T o = __shfl_xor_sync(kFull, v, d);
+        v = op == 0 ? (o < v ? o : v) : op == 1 ? (o > v ? o : v) : v + o;
     }
     const int warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
     __syncthreads();
     if ((threadIdx.x & 31) == 0) red[warp] = v;
     __syncthreads();
-    int r = red[0];
-    for (int w = 1; w < kMsaThreads / 32; w++) r = op == 0 ? min(r, red[w]) : op == 1 ? max(r, red[w]) : r + red[w];
+    T r = red[0];
+    for (int w = 1; w < nw; w++) r = op == 0 ? (red[w] < r ? red[w] : r) : op == 1 ? (red[w] > r ? red[w] : r) : r + red[w];
     return r;
 }
 
-// One block per anchor.  Columns are owned by threads (column c by thread
-// c % blockDim), and every column sums its rows in list order: anchor first,
-// then the kept candidates as the filters left them, so each float sum is
-// the reference's sequence of additions.
-__global__ void __launch_bounds__(kMsaThreads) msa_correct_kernel(StoreArg st, Params p, BatchArg b,
-                                                                  const uint32_t* __restrict__ rawOff, int maxCols) {
-    extern __shared__ unsigned char sm[];
-    int* cntA = reinterpret_cast<int*>(sm);
+// One block per anchor; column c belongs to thread c % blockDim (at most
+// kMsaCols columns per thread, kept in registers while the rows stream by).
+// Every column adds its rows in list order -- anchor first, then the kept
+// candidates as the filters left them -- so each float sum is the
+// reference's sequence of additions.  Row metadata is staged in shared memory
+// in chunks of kMsaChunkRows rows; removed rows are a shared bitset.
+// reference: include/classification.hpp:748-797 (extract_anchor_v3) and
+// include/forest.hpp:70-81,217-226 (tree walk; decide: running mean of the
+// trees' probabilities, true as soon as it reaches the threshold)
+__device__ bool forest_decide(const Params& p, const float* f) {
+    float sum = 0.0f;
+    for (int t = 0; t < p.numTrees; t++) {
+        const ForestNode* tree = p.forestNodes + p.treeOffsets[t];
+        uint32_t i = 0;
+        float prob = 0.0f;
+        for (int guard = 0; guard < (1 << 20); guard++) {
+            const ForestNode n = tree[i];
+            if ((double)f[n.att] <= n.split) {
+                if (n.flag & 2u) { prob = __uint_as_float(n.lhs); break; }
+                i = n.lhs;
+            } else {
+                if (n.flag & 1u) { prob = __uint_as_float(n.rhs); break; }
+                i = n.rhs;
+            }
+        }
+        sum = __fadd_rn(sum, prob);
+        if (__fdiv_rn(sum, (float)p.numTrees) >= p.forestThreshold) return true;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(1024) msa_correct_kernel(StoreArg st, Params p, BatchArg b,
+                                                          const uint32_t* __restrict__ rawOff, int maxCols,
+                                                          int bitsetWords, int storeWeights) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    RowMeta* rows = reinterpret_cast<RowMeta*>(sm);
+    uint32_t* removed = reinterpret_cast<uint32_t*>(rows + kMsaChunkRows);
+    float* qw = reinterpret_cast<float*>(removed + bitsetWords);
+    int* cntA = reinterpret_cast<int*>(qw + 256);
     int* cntC = cntA + maxCols;
     int* cntG = cntC + maxCols;
     int* cntT = cntG + maxCols;
     int* cov = cntT + maxCols;
     int* origCov = cov + maxCols;
     float* sup = reinterpret_cast<float*>(origCov + maxCols);
-    char* cons = reinterpret_cast<char*>(sup + maxCols);
-    __shared__ float redf[kMsaThreads / 32];
-    __shared__ int redi[kMsaThreads / 32];
-    __shared__ int sCol, sFound;
+    // column weights, kept only for the forest's features
+    float* colWA = storeWeights ? sup + maxCols : nullptr;
+    float* colWC = storeWeights ? colWA + maxCols : nullptr;
+    float* colWG = storeWeights ? colWC + maxCols : nullptr;
+    float* colWT = storeWeights ? colWG + maxCols : nullptr;
+    char* cons = reinterpret_cast<char*>(sup + maxCols + (storeWeights ? 4 * maxCols : 0));
+    __shared__ float redf[32];
+    __shared__ int redi[32];
+    __shared__ int sCol, sFound, sByConsensus;
 
     const int a = blockIdx.x;
     const int tid = threadIdx.x;
+    const int bd = blockDim.x;
     const uint64_t aid = b.first + (uint64_t)a;
     const uint32_t nf = b.nfinal[a];
     char* out = b.out + (uint64_t)a * b.outPitch;
@@ -288,82 +498,121 @@ __global__ void __launch_bounds__(kMsaThreads) msa_correct_kernel(StoreArg st, P
         return;
     }
     const uint32_t base = rawOff[a];
-    const uint32_t* fid = b.fid + base;
-    const int16_t* fshift = b.fshift + base;
-    uint8_t* forient = b.forient + base;
-    const float* fweight = b.fweight + base;
     const int La = st.len[aid];
     const uint32_t* aenc = st.enc + aid * (uint64_t)st.pitch;
     const uint8_t* aq = p.useQuality ? st.qual + aid * (uint64_t)st.lmax : nullptr;
+    for (int i = tid; i < bitsetWords; i += bd) removed[i] = 0u;
+    if (p.useQuality)
+        for (int i = tid; i < 256; i += bd) qw[i] = p.qweight[i];
+    const bool oneChunk = nf <= (uint32_t)kMsaChunkRows;
+    auto loadRows = [&](uint32_t j0, uint32_t cnt) {
+        for (uint32_t r = tid; r < cnt; r += bd) {
+            const uint32_t j = base + j0 + r;
+            const uint32_t id = b.fid[j];
+            RowMeta m;
+            m.enc = st.enc + (uint64_t)id * st.pitch;
+            m.qual = p.useQuality ? st.qual + (uint64_t)id * st.lmax : nullptr;
+            m.weight = b.fweight[j];
+            m.shift = b.fshift[j];
+            m.len = b.flen[j];
+            m.rc = b.forient[j] == 2;
+            rows[r] = m;
+        }
+    };
+    if (oneChunk) loadRows(0, nf);
+    __syncthreads();
+    auto isRemoved = [&](uint32_t j) { return (removed[j >> 5] >> (j & 31)) & 1u; };
 
-    int aBegin = 0, nCols = 0, nActive = (int)nf, builds = 0;
+    int aBegin = 0, nActive = (int)nf, builds = 0;
     for (int iter = 0;; iter++) {
         // columns of the current MSA (src/msa.cpp:19-33)
         int lo = 0, hi = La, act = 0;
-        for (uint32_t j = tid; j < nf; j += kMsaThreads) {
-            if (!(forient[j] & kRemoved)) {
-                const int s = fshift[j];
+        for (uint32_t j = tid; j < nf; j += bd) {
+            if (!isRemoved(j)) {
+                const int s = b.fshift[base + j];
                 lo = min(lo, s);
-                hi = max(hi, s + (int)st.len[fid[j]]);
+                hi = max(hi, s + (int)b.flen[base + j]);
                 act++;
             }
         }
-        lo = block_reduce_i(lo, redi, 0);
-        hi = block_reduce_i(hi, redi, 1);
-        nActive = block_reduce_i(act, redi, 2);
-        nCols = hi - lo;
+        lo = block_reduce<int>(lo, redi, 0);
+        hi = block_reduce<int>(hi, redi, 1);
+        nActive = block_reduce<int>(act, redi, 2);
+        const int nCols = hi - lo;
         aBegin = -lo;
         const int aEnd = aBegin + La;
-        // build: counts, weights, consensus, support, original-base coverage
-        for (int c = tid; c < nCols; c += kMsaThreads) {
-            int nA = 0, nC = 0, nG = 0, nT = 0, cv = 0;
-            float wA = 0.0f, wC = 0.0f, wG = 0.0f, wT = 0.0f;
-            auto add = [&](uint32_t bb, float w) {
-                switch (bb) {
-                    case 0: nA++; wA = __fadd_rn(wA, w); break;
-                    case 1: nC++; wC = __fadd_rn(wC, w); break;
-                    case 2: nG++; wG = __fadd_rn(wG, w); break;
-                    default: nT++; wT = __fadd_rn(wT, w); break;
-                }
-                cv++;
-            };
-            uint32_t anchorBase = 0;
+        // build: counts, weights (src/msa.cpp:93-112)
+        int nA[kMsaCols], nC[kMsaCols], nG[kMsaCols], nT[kMsaCols];
+        float wA[kMsaCols], wC[kMsaCols], wG[kMsaCols], wT[kMsaCols];
+#pragma unroll
+        for (int k = 0; k < kMsaCols; k++) {
+            nA[k] = nC[k] = nG[k] = nT[k] = 0;
+            wA[k] = wC[k] = wG[k] = wT[k] = 0.0f;
+        }
+        auto add = [&](int k, uint32_t bb, float w) {
+            if (bb == 0) { nA[k]++; wA[k] = __fadd_rn(wA[k], w); }
+            else if (bb == 1) { nC[k]++; wC[k] = __fadd_rn(wC[k], w); }
+            else if (bb == 2) { nG[k]++; wG[k] = __fadd_rn(wG[k], w); }
+            else { nT[k]++; wT[k] = __fadd_rn(wT[k], w); }
+        };
+#pragma unroll
+        for (int k = 0; k < kMsaCols; k++) {
+            const int c = tid + k * bd;
             if (c >= aBegin && c < aEnd) {
                 const int pos = c - aBegin;
-                anchorBase = get2bit(aenc, pos);
-                const float w = p.useQuality ? __fmul_rn(1.0f, p.qweight[aq[pos]]) : 1.0f;
-                add(anchorBase, w);
+                const float w = p.useQuality ? __fmul_rn(1.0f, qw[aq[pos]]) : 1.0f;
+                add(k, get2bit(aenc, pos), w);
             }
-            for (uint32_t j = 0; j < nf; j++) {
-                const uint8_t o = forient[j];
-                if (o & kRemoved) continue;
-                const int rb = aBegin + fshift[j];
-                const uint32_t id = fid[j];
-                const int Lc = st.len[id];
-                if (c < rb || c >= rb + Lc) continue;
-                const int pos = c - rb;
-                const bool rc = o == 2;
-                const uint32_t bb = oriented_base(st.enc + (uint64_t)id * st.pitch, Lc, rc, pos);
-                float w = fweight[j];
-                if (p.useQuality) {
-                    const uint8_t q = st.qual[(uint64_t)id * st.lmax + (rc ? Lc - 1 - pos : pos)];
-                    w = __fmul_rn(w, p.qweight[q]);
+        }
+        for (uint32_t j0 = 0; j0 < nf; j0 += kMsaChunkRows) {
+            const uint32_t cnt = min((uint32_t)kMsaChunkRows, nf - j0);
+            if (!oneChunk) {
+                __syncthreads();
+                loadRows(j0, cnt);
+                __syncthreads();
+            }
+            for (uint32_t r = 0; r < cnt; r++) {
+                if (isRemoved(j0 + r)) continue;
+                const RowMeta m = rows[r];
+                const int rb = aBegin + m.shift;
+                const int re = rb + (int)m.len;
+#pragma unroll
+                for (int k = 0; k < kMsaCols; k++) {
+                    const int c = tid + k * bd;
+                    if (c >= rb && c < re) {
+                        const int pos = c - rb;
+                        const int sp = m.rc ? (int)m.len - 1 - pos : pos;
+                        uint32_t bb = get2bit(m.enc, sp);
+                        if (m.rc) bb = 3u - bb;
+                        float w = m.weight;
+                        if (p.useQuality) w = __fmul_rn(w, qw[m.qual[sp]]);
+                        add(k, bb, w);
+                    }
                 }
-                add(bb, w);
             }
-            // findConsensus (src/msa.cpp:135-157)
-            char cs = 'A';
-            float cw = wA;
-            if (wC > cw) { cs = 'C'; cw = wC; }
-            if (wG > cw) { cs = 'G'; cw = wG; }
-            if (wT > cw) { cs = 'T'; cw = wT; }
-            const float colW = __fadd_rn(__fadd_rn(__fadd_rn(wA, wC), wG), wT);
-            cntA[c] = nA; cntC[c] = nC; cntG[c] = nG; cntT[c] = nT;
-            cov[c] = cv;
-            sup[c] = __fdiv_rn(cw, colW);
-            cons[c] = cs;
-            if (c >= aBegin && c < aEnd) {
-                origCov[c] = anchorBase == 0 ? nA : anchorBase == 1 ? nC : anchorBase == 2 ? nG : nT;
+        }
+        // findConsensus (src/msa.cpp:135-157), findOrigWeightAndCoverage (:159-173)
+#pragma unroll
+        for (int k = 0; k < kMsaCols; k++) {
+            const int c = tid + k * bd;
+            if (c < nCols) {
+                char cs = 'A';
+                float cw = wA[k];
+                if (wC[k] > cw) { cs = 'C'; cw = wC[k]; }
+                if (wG[k] > cw) { cs = 'G'; cw = wG[k]; }
+                if (wT[k] > cw) { cs = 'T'; cw = wT[k]; }
+                const float colW = __fadd_rn(__fadd_rn(__fadd_rn(wA[k], wC[k]), wG[k]), wT[k]);
+                cntA[c] = nA[k]; cntC[c] = nC[k]; cntG[c] = nG[k]; cntT[c] = nT[k];
+                cov[c] = nA[k] + nC[k] + nG[k] + nT[k];
+                sup[c] = __fdiv_rn(cw, colW);
+                cons[c] = cs;
+                if (storeWeights) {
+                    colWA[c] = wA[k]; colWC[c] = wC[k]; colWG[c] = wG[k]; colWT[c] = wT[k];
+                }
+                if (c >= aBegin && c < aEnd) {
+                    const uint32_t ab = get2bit(aenc, c - aBegin);
+                    origCov[c] = ab == 0 ? nA[k] : ab == 1 ? nC[k] : ab == 2 ? nG[k] : nT[k];
+                }
             }
         }
         builds++;
@@ -371,14 +620,11 @@ __global__ void __launch_bounds__(kMsaThreads) msa_correct_kernel(StoreArg st, P
         if (iter == 5 || nActive == 0) break;
         // findCandidatesOfDifferentRegion (src/msa.cpp:532-734)
         bool mism = false;
-        for (int c = aBegin + tid; c < aEnd; c += kMsaThreads) {
-            const char ab = "ACGT"[get2bit(aenc, c - aBegin)];
-            mism |= cons[c] != ab;
-        }
+        for (int c = aBegin + tid; c < aEnd; c += bd) mism |= cons[c] != "ACGT"[get2bit(aenc, c - aBegin)];
         if (!__syncthreads_or(mism)) break;
         if (tid == 0) sCol = 0x7fffffff;
         __syncthreads();
-        for (int c = aBegin + tid; c < aEnd; c += kMsaThreads) {
+        for (int c = aBegin + tid; c < aEnd; c += bd) {
             const int counts[4] = {cntA[c], cntC[c], cntG[c], cntT[c]};
             const int ci = cons[c] == 'A' ? 0 : cons[c] == 'C' ? 1 : cons[c] == 'G' ? 2 : 3;
             bool sig = false;
@@ -400,36 +646,31 @@ __global__ void __launch_bounds__(kMsaThreads) msa_correct_kernel(StoreArg st, P
         const uint32_t found = (uint32_t)sFound;
         const uint32_t orig = get2bit(aenc, col - aBegin);
         const bool keepMatching = orig == found;
+        auto differs = [&](uint32_t j) -> bool {  // row j lies on `col` and is to be removed
+            const uint32_t g = base + j;
+            const int rb = aBegin + b.fshift[g];
+            const int len = b.flen[g];
+            if (col < rb || col >= rb + len) return false;
+            const uint32_t* e = st.enc + (uint64_t)b.fid[g] * st.pitch;
+            const int pos = col - rb;
+            const bool rc = b.forient[g] == 2;
+            uint32_t bb = get2bit(e, rc ? len - 1 - pos : pos);
+            if (rc) bb = 3u - bb;
+            return keepMatching ? (bb != found) : (bb == found);
+        };
         bool veto = false, any = false;
-        for (uint32_t j = tid; j < nf; j += kMsaThreads) {
-            const uint8_t o = forient[j];
-            if (o & kRemoved) continue;
-            const int rb = aBegin + fshift[j];
-            const uint32_t id = fid[j];
-            const int Lc = st.len[id];
-            if (col < rb || col >= rb + Lc) continue;
-            const uint32_t bb = oriented_base(st.enc + (uint64_t)id * st.pitch, Lc, o == 2, col - rb);
-            const bool rm = keepMatching ? (bb != found) : (bb == found);
-            if (rm) {
-                any = true;
-                veto |= fweight[j] >= 0.90f;
-            }
+        for (uint32_t j = tid; j < nf; j += bd) {
+            if (isRemoved(j) || !differs(j)) continue;
+            any = true;
+            veto |= b.fweight[base + j] >= 0.90f;
         }
         const bool anyVeto = __syncthreads_or(veto);
         const bool anyRemove = __syncthreads_or(any);
         // a veto (or nothing to remove) leaves the MSA as it is; the
         // reference then rebuilds the same MSA and reaches the same decision
         if (anyVeto || !anyRemove) break;
-        for (uint32_t j = tid; j < nf; j += kMsaThreads) {
-            const uint8_t o = forient[j];
-            if (o & kRemoved) continue;
-            const int rb = aBegin + fshift[j];
-            const uint32_t id = fid[j];
-            const int Lc = st.len[id];
-            if (col < rb || col >= rb + Lc) continue;
-            const uint32_t bb = oriented_base(st.enc + (uint64_t)id * st.pitch, Lc, o == 2, col - rb);
-            const bool rm = keepMatching ? (bb != found) : (bb == found);
-            if (rm) forient[j] = o | kRemoved;
+        for (uint32_t j = tid; j < nf; j += bd) {
+            if (!isRemoved(j) && differs(j)) atomicOr(&removed[j >> 5], 1u << (j & 31));
         }
         __syncthreads();
     }
@@ -437,15 +678,16 @@ __global__ void __launch_bounds__(kMsaThreads) msa_correct_kernel(StoreArg st, P
     const int aEnd = aBegin + La;
     float mins = 3.402823466e+38f;
     int minc = 0x7fffffff, maxc = -1;
-    for (int c = aBegin + tid; c < aEnd; c += kMsaThreads) {
+    for (int c = aBegin + tid; c < aEnd; c += bd) {
         mins = fminf(mins, sup[c]);
         minc = min(minc, cov[c]);
         maxc = max(maxc, cov[c]);
     }
-    mins = block_min_f(mins, redf);
-    minc = block_reduce_i(minc, redi, 0);
-    maxc = block_reduce_i(maxc, redi, 1);
-    __shared__ int sByConsensus, sHQ;
+    mins = block_reduce<float>(mins, redf, 0);
+    minc = block_reduce<int>(minc, redi, 0);
+    maxc = block_reduce<int>(maxc, redi, 1);
+    __shared__ float sAvg;
+    __shared__ int sHQ;
     if (tid == 0) {
         float sum = 0.0f;
         for (int c = aBegin; c < aEnd; c++) sum = __fadd_rn(sum, sup[c]);
@@ -461,19 +703,54 @@ __global__ void __launch_bounds__(kMsaThreads) msa_correct_kernel(StoreArg st, P
             hq = fgeq((float)minc, p.minCoverageThreshold) && fleq((float)smallest, p.hqPercentLimit);
         }
         sByConsensus = good;
+        sAvg = avg;
         sHQ = hq;
-        if (nActive > 0) {
+        // the forest decision corrects every anchor that reached the MSA
+        // (include/corrector.hpp:1448-1472); the classic one needs candidates
+        const bool corrected = p.correctionType == CG_CORR_FOREST || nActive > 0;
+        if (corrected) {
             atomicAdd(&b.counters[kCounterCorrected], 1ull);
             if (hq) atomicAdd(&b.counters[kCounterHQ], 1ull);
         }
         atomicAdd(&b.counters[kCounterMsaBuilds], (unsigned long long)builds);
-        b.flags[a] = nActive > 0 ? (uint8_t)(CG_RESULT_CORRECTED | (hq ? CG_RESULT_HQ : 0)) : (uint8_t)0;
+        b.flags[a] = corrected ? (uint8_t)(CG_RESULT_CORRECTED | (hq ? CG_RESULT_HQ : 0)) : (uint8_t)0;
     }
     __syncthreads();
-    (void)maxc;
+    if (p.correctionType == CG_CORR_FOREST) {
+        const bool hq = sHQ;
+        const float avg = sAvg;
+        for (int i = tid; i < La; i += bd) {
+            const int c = aBegin + i;
+            const uint32_t ab = get2bit(aenc, i);
+            const char orig = "ACGT"[ab];
+            char r = cons[c];
+            if (!hq && r != orig) {
+                const float wsum = __fadd_rn(__fadd_rn(__fadd_rn(colWA[c], colWC[c]), colWG[c]), colWT[c]);
+                float wCons, nCons;
+                switch (r) {
+                    case 'A': wCons = colWA[c]; nCons = (float)cntA[c]; break;
+                    case 'C': wCons = colWC[c]; nCons = (float)cntC[c]; break;
+                    case 'G': wCons = colWG[c]; nCons = (float)cntG[c]; break;
+                    default: wCons = colWT[c]; nCons = (float)cntT[c]; break;
+                }
+                const float wOrig = ab == 0 ? colWA[c] : ab == 1 ? colWC[c] : ab == 2 ? colWG[c] : colWT[c];
+                const float cv = (float)cov[c];
+                const float oc = (float)origCov[c];
+                const float ec = p.estimatedCoverage;
+                const float f[13] = {__fdiv_rn(oc, cv),           __fdiv_rn(wOrig, wsum), __fdiv_rn(wOrig, oc),
+                                     __fdiv_rn(nCons, cv),        sup[c],                 __fdiv_rn(wCons, nCons),
+                                     __fdiv_rn(wsum, cv),         __fdiv_rn(cv, ec),      __fdiv_rn(wsum, ec),
+                                     avg,                         mins,                   __fdiv_rn((float)maxc, ec),
+                                     __fdiv_rn((float)minc, ec)};
+                if (!forest_decide(p, f)) r = orig;
+            }
+            out[i] = r;
+        }
+        return;
+    }
     if (nActive == 0) return;
     const bool byCons = sByConsensus;
-    for (int i = tid; i < La; i += kMsaThreads) {
+    for (int i = tid; i < La; i += bd) {
         const int c = aBegin + i;
         char r;
         if (byCons) {
@@ -485,26 +762,48 @@ __global__ void __launch_bounds__(kMsaThreads) msa_correct_kernel(StoreArg st, P
     }
 }
 
-}  // namespace
-
-cudaError_t launch_align_filter(StoreArg st, Params p, BatchArg b, cudaStream_t s) {
-    const size_t smem = (size_t)kAlignWarps * 6 * st.wp * sizeof(uint32_t);
+template <int MAXW, bool REGS>
+cudaError_t launch_align_t(StoreArg st, Params p, BatchArg b, cudaStream_t s) {
+    const size_t smem = (size_t)kAlignWarps * 6 * st.wp * sizeof(uint32_t) +
+                        (REGS ? ((size_t)st.lmax + 2) * sizeof(int16_t) : 0);
     const unsigned blocks = (unsigned)((b.count + kAlignWarps - 1) / kAlignWarps);
-    align_filter_kernel<<<blocks, kAlignWarps * 32, smem, s>>>(st, p, b, b.rawCount);
+    align_filter_kernel<MAXW, REGS><<<blocks, kAlignWarps * 32, smem, s>>>(st, p, b, b.rawCount);
     return cudaGetLastError();
 }
 
-size_t msa_smem_bytes(int maxCols) { return (size_t)maxCols * (7 * sizeof(int) + 1); }
+}  // namespace
 
-cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, cudaStream_t s) {
+cudaError_t launch_align_filter(StoreArg st, Params p, BatchArg b, cudaStream_t s) {
+    const int need = st.wp - 1;  // words per plane that hold bases
+    if (need <= 5) return launch_align_t<5, true>(st, p, b, s);
+    if (need <= 8) return launch_align_t<8, true>(st, p, b, s);
+    if (need <= 16) return launch_align_t<16, false>(st, p, b, s);
+    return launch_align_t<32, false>(st, p, b, s);
+}
+
+int msa_threads(int maxCols) {
+    int t = kMsaThreadsMin;
+    while (t * kMsaCols < maxCols) t += 32;
+    return t;
+}
+
+size_t msa_smem_bytes(int maxCols, int bitsetWords, int storeWeights) {
+    return sizeof(RowMeta) * kMsaChunkRows + sizeof(uint32_t) * bitsetWords + 256 * sizeof(float) +
+           (size_t)maxCols * (7 * sizeof(int) + 1 + (storeWeights ? 4 * sizeof(float) : 0));
+}
+
+cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, int maxRows, cudaStream_t s) {
     const int maxCols = 3 * st.lmax + 4;
-    const size_t smem = msa_smem_bytes(maxCols);
+    const int bitsetWords = (maxRows + 31) / 32 + 1;
+    const int storeWeights = p.correctionType == CG_CORR_FOREST;
+    const size_t smem = msa_smem_bytes(maxCols, bitsetWords, storeWeights);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(msa_correct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
     }
-    msa_correct_kernel<<<b.count, kMsaThreads, smem, s>>>(st, p, b, b.rawCount, maxCols);
+    msa_correct_kernel<<<b.count, msa_threads(maxCols), smem, s>>>(st, p, b, b.rawCount, maxCols, bitsetWords,
+                                                                    storeWeights);
     return cudaGetLastError();
 }
 

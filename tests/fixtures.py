@@ -33,7 +33,16 @@ def options_for(entry: dict) -> capi.CareOptions:
         float(o["coverage"]), kmerlength=int(o["k"]),
         use_quality_scores=int(bool(o.get("quality"))),
         exclude_ambiguous_reads=int(bool(o.get("exclude_ambiguous"))),
-        pair_mode=capi.CG_PAIR_PE if o.get("paired") else capi.CG_PAIR_SE)
+        pair_mode=capi.CG_PAIR_PE if o.get("paired") else capi.CG_PAIR_SE,
+        correction_type=capi.CG_CORR_FOREST if o.get("forest") else capi.CG_CORR_CLASSIC)
+
+
+def forest_bytes(entry: dict) -> bytes | None:
+    name = entry["options"].get("forest")
+    if not name:
+        return None
+    with open(os.path.join(GOLDEN, name), "rb") as f:
+        return f.read()
 
 
 def reads_for(entry: dict) -> sim.SimReads:

@@ -14,11 +14,13 @@ from rabbitqcplus_gb300 import capi, sim
 pytestmark = pytest.mark.gpu
 
 
-def run_gpu(opts, reads, quality=False, batch=0):
+def run_gpu(opts, reads, quality=False, batch=0, forest=None):
     opts.batch_anchors = batch
     g = capi.CareGpu(opts)
     g.append_reads(reads.sequences, reads.offsets, reads.qualities if quality else None)
     g.build_tables()
+    if forest:
+        g.load_forest(forest)
     flags, seqs = g.correct()
     stats = g.stats()
     return g, flags, seqs, stats
@@ -37,7 +39,7 @@ def test_gpu_matches_reference_fixture(name):
     e = fx.manifest()[name]
     r = fx.reads_for(e)
     q = bool(e["options"].get("quality"))
-    g, flags, seqs, _ = run_gpu(fx.options_for(e), r, quality=q)
+    g, flags, seqs, _ = run_gpu(fx.options_for(e), r, quality=q, forest=fx.forest_bytes(e))
     out = capi.apply_corrections(r.sequences, r.offsets, flags, seqs)
     exp = fx.expected_output(name, r)
     bad = np.nonzero(out != exp)[0]
@@ -121,6 +123,28 @@ def test_gpu_paired_end_matches_oracle():
     oflags, oseqs, _ = orc.correct()
     assert_same_results(r, flags, seqs, oflags, oseqs)
     g.close()
+
+
+def test_gpu_forest_matches_oracle_with_quality_and_tree_limit():
+    e = fx.manifest()["forest_se"]
+    forest = fx.forest_bytes(e)
+    cfg = sim.SimConfig(seed=45, genome_length=40_000, num_reads=8_000, repeat_families=3, repeat_copies=3,
+                        read_len_min=100, read_len_max=150, sub_rate_5p=0.004, sub_rate_3p=0.03)
+    r = sim.SimReads(cfg)
+    for q, trees in ((0, 0), (1, 5)):
+        kw = dict(use_quality_scores=q, correction_type=capi.CG_CORR_FOREST, threshold_anchor=0.6)
+        opts = capi.CareOptions.defaults(30.0, **kw)
+        opts.batch_anchors = 0
+        g = capi.CareGpu(opts)
+        g.append_reads(r.sequences, r.offsets, r.qualities if q else None)
+        g.build_tables()
+        g.load_forest(forest, trees)
+        flags, seqs = g.correct()
+        orc = oracle.Oracle(capi.CareOptions.defaults(30.0, **kw), r.sequences, r.offsets, r.qualities if q else None)
+        orc.load_forest(forest, trees if trees else 0xFFFFFFFF, 0.6)
+        oflags, oseqs, _ = orc.correct()
+        assert_same_results(r, flags, seqs, oflags, oseqs)
+        g.close()
 
 
 def test_gpu_quality_scores_match_oracle():

@@ -40,6 +40,8 @@ def test_oracle_output_matches_reference(name, cases):
     opts = fx.options_for(e)
     q = r.qualities if e["options"].get("quality") else None
     orc = oracle.Oracle(opts, r.sequences, r.offsets, q, threads=4)
+    if fx.forest_bytes(e):
+        orc.load_forest(fx.forest_bytes(e))
     flags, seqs, _ = orc.correct()
     out = capi.apply_corrections(r.sequences, r.offsets, flags, seqs)
     exp = fx.expected_output(name, r)
