@@ -92,7 +92,7 @@ struct cg_ctx {
 
     // batch buffers
     DevBuf qrange, rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, flen, nfinal, flags, out, counters;
-    DevBuf scanTmp;
+    DevBuf scanTmp, uoff;
     uint32_t* hPinned = nullptr;  // 2 words: total raw, max raw
 
     // forest classifier (CG_CORR_FOREST)
@@ -412,8 +412,18 @@ int run_batch(cg_ctx* c, uint64_t first, int count, uint8_t* hFlags, char* hOut,
         CG_CUDA(c, launch_pair_flags(b, c->stream));
         c->stats.kernel_launches += 1;
     }
+    // dense candidate numbering for the thread-per-candidate alignment
+    CG_CUDA(c, c->uoff.ensure((size_t)(count + 1) * sizeof(uint32_t)));
+    CG_CUDA(c, cudaMemsetAsync(c->uoff.as<uint32_t>() + count, 0, sizeof(uint32_t), c->stream));
+    CG_CUDA(c, cudaMemcpyAsync(c->uoff.p, b.ncand, (size_t)count * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                               c->stream));
+    CG_CUDA(c, scan_exclusive_u32(c->uoff.as<uint32_t>(), (size_t)count + 1, c->scanTmp.p, c->stream));
+    CG_CUDA(c, cudaMemcpyAsync(c->hPinned + 2, c->uoff.as<uint32_t>() + count, sizeof(uint32_t),
+                               cudaMemcpyDeviceToHost, c->stream));
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->stats.kernel_launches += scan_launches(count + 1) + 1;
     CG_CUDA(c, cudaEventRecord(c->st1, c->stream));
-    CG_CUDA(c, launch_align_filter(st, c->params, b, c->stream));
+    CG_CUDA(c, launch_align_filter(st, c->params, b, c->uoff.as<uint32_t>(), c->hPinned[2], c->stream));
     CG_CUDA(c, cudaEventRecord(c->st2, c->stream));
     CG_CUDA(c, launch_msa_correct(st, c->params, b, (int)std::max<uint32_t>(c->hPinned[1], 1), c->stream));
     CG_CUDA(c, cudaEventRecord(c->st3, c->stream));
@@ -495,7 +505,7 @@ void cg_destroy(cg_ctx* c) {
     release_tables(c);
     for (DevBuf* b : {&c->enc, &c->len, &c->hilo, &c->qual, &c->ambig, &c->sig, &c->qrange, &c->rawCount, &c->cand,
                       &c->ncand, &c->paired, &c->aln, &c->fid, &c->fshift, &c->forient, &c->fweight, &c->flen, &c->nfinal,
-                      &c->flags, &c->out, &c->counters, &c->scanTmp, &c->forestNodes, &c->treeOffsets})
+                      &c->flags, &c->out, &c->counters, &c->scanTmp, &c->uoff, &c->forestNodes, &c->treeOffsets})
         b->release();
     if (c->hPinned) cudaFreeHost(c->hPinned);
     for (cudaEvent_t ev : {c->ev0, c->ev1, c->st0, c->st1, c->st2, c->st3})

@@ -164,19 +164,26 @@ __device__ __forceinline__ void scan_direction(const ShiftedRegs<MAXW>& S, const
         const int sl = LEFT ? tl + 1 : tl;
         const int ov = active ? (LEFT ? min(La, Lc - sl) : min(La - sl, Lc)) : 0;
         const int maxErr = maxErrTab[ov];
-        bool run = active && maxErr > 0 && ov > 0;
         const int parts = (ov + 31) >> 5;
         const int rem = (parts << 5) - ov;
-        int m = 0;
+        const uint32_t last = 0xffffffffu << rem;  // rem < 32
+        // words 0 and 1 without branches: a word past the overlap has mask 0
+        const uint32_t mask0 = parts > 1 ? 0xffffffffu : (parts == 1 ? last : 0u);
+        const uint32_t mask1 = parts > 2 ? 0xffffffffu : (parts == 2 ? last : 0u);
+        int m = __popc(((S.h[k] ^ O[0][0]) | (S.l[k] ^ O[1][0])) & mask0) +
+                __popc(((S.h[k + 1] ^ O[0][1]) | (S.l[k + 1] ^ O[1][1])) & mask1);
+        bool run = active && maxErr > 0 && m < maxErr;
+        // the rest only while some lane of the warp can still be valid
+        if (__any_sync(kFull, run && parts > 2)) {
 #pragma unroll
-        for (int i = 0; i < MAXW; i++) {
-            const bool act = run && i < parts;
-            if (!__any_sync(kFull, act)) break;
-            if (act) {
-                uint32_t x = (S.h[k + i] ^ O[0][i]) | (S.l[k + i] ^ O[1][i]);
-                if (i == parts - 1 && rem != 0) x &= 0xffffffffu << rem;
-                m += __popc(x);
-                if (m >= maxErr) run = false;
+            for (int i = 2; i < MAXW; i++) {
+                const bool act = run && i < parts;
+                if (!__any_sync(kFull, act)) break;
+                if (act) {
+                    const uint32_t mask = i == parts - 1 ? last : 0xffffffffu;
+                    m += __popc(((S.h[k + i] ^ O[0][i]) | (S.l[k + i] ^ O[1][i])) & mask);
+                    run = m < maxErr;
+                }
             }
         }
         if (run) {
@@ -262,11 +269,82 @@ __device__ __forceinline__ uint2 pack_aln(const AlnRes& r, int ori) {
                       (uint32_t)(uint16_t)r.nOps | ((uint32_t)ori << 16));
 }
 
+// Mismatch-ratio filter of one anchor (include/corrector.hpp:1053-1149 single
+// end, 1151-1211 paired end) over its aligned candidates b.aln[base, base+nc),
+// writing the kept candidates in order; one warp.
+__device__ void filter_anchor(const StoreArg& st, const Params& p, const BatchArg& b, int a, uint32_t base,
+                              uint32_t nc) {
+    const int lane = (int)lane_id();
+    float thr;
+    if (!p.paired) {
+        uint32_t c0 = 0, c1 = 0, c2 = 0;
+        for (uint32_t j = lane; j < nc; j += 32) {
+            const uint2 v = b.aln[base + j];
+            if ((v.y >> 16) != 3u) {
+                const float ratio = __fdiv_rn((float)(int)(int16_t)(v.y & 0xffffu), (float)(v.x >> 16));
+                c0 += ratio < p.mm2;
+                c1 += ratio < p.mm3;
+                c2 += ratio < p.mm4;
+            }
+        }
+        c0 = __reduce_add_sync(kFull, c0);
+        c1 = __reduce_add_sync(kFull, c1);
+        c2 = __reduce_add_sync(kFull, c2);
+        thr = -3.402823466e+38f;  // std::numeric_limits<float>::lowest()
+        if (c0 > 0 || c1 > 0 || c2 > 0) {
+            if ((float)c0 >= p.goodAlignmentsCountThreshold) thr = p.mm2;
+            else if ((float)c1 >= p.goodAlignmentsCountThreshold) thr = p.mm3;
+            else if ((float)c2 >= p.goodAlignmentsCountThreshold) thr = p.mm4;
+        }
+    } else {
+        thr = p.pairedThreshold;
+    }
+    uint32_t kept = 0, aligned = 0;
+    for (uint32_t j0 = 0; j0 < nc; j0 += 32) {
+        const uint32_t j = j0 + lane;
+        bool keep = false, isAligned = false;
+        uint2 v = make_uint2(0, 0);
+        if (j < nc) {
+            v = b.aln[base + j];
+            const int ori = (int)(v.y >> 16);
+            if (ori != 3) {
+                isAligned = true;
+                const int ov = (int)(v.x >> 16);
+                const int nOps = (int)(int16_t)(v.y & 0xffffu);
+                const float ratio = __fdiv_rn((float)nOps, (float)ov);
+                keep = ratio < thr;
+                if (p.paired && b.paired[base + j]) keep = true;
+            }
+        }
+        const uint32_t m = __ballot_sync(kFull, keep);
+        aligned += __popc(__ballot_sync(kFull, isAligned));
+        if (keep) {
+            const uint32_t pos = kept + __popc(m & ((1u << lane) - 1u));
+            const int ov = (int)(v.x >> 16);
+            const int nOps = (int)(int16_t)(v.y & 0xffffu);
+            const uint32_t cid = b.cand[base + j];
+            b.fid[base + pos] = cid;
+            b.fshift[base + pos] = (int16_t)(v.x & 0xffffu);
+            b.forient[base + pos] = (uint8_t)(v.y >> 16);
+            b.flen[base + pos] = st.len[cid];
+            // reference: include/hostdevicefunctions.cuh:93-95 (calculateOverlapWeight)
+            b.fweight[base + pos] =
+                __fsub_rn(1.0f, __fsqrt_rn(__fdiv_rn((float)nOps, __fmul_rn((float)ov, p.maxErrorRate))));
+        }
+        kept += __popc(m);
+    }
+    if (lane == 0) {
+        b.nfinal[a] = kept;
+        atomicAdd(&b.counters[kCounterAligned], (unsigned long long)aligned);
+        atomicAdd(&b.counters[kCounterMsaCands], (unsigned long long)kept);
+    }
+}
+
 // One warp per anchor: align all candidates, choose orientations, apply the
 // mismatch-ratio filter and write the filtered candidate list in order.
 // Shared memory per warp: anchor hi/lo, candidate fwd hi/lo, rc hi/lo planes.
 template <int MAXW, bool REGS>
-__global__ void __launch_bounds__(kAlignWarps * 32, REGS ? 6 : 1) align_filter_kernel(StoreArg st, Params p, BatchArg b,
+__global__ void __launch_bounds__(kAlignWarps * 32, REGS ? (MAXW <= 5 ? 6 : 4) : 1) align_filter_kernel(StoreArg st, Params p, BatchArg b,
                                                                         const uint32_t* __restrict__ rawOff) {
     extern __shared__ uint32_t smem[];
     const int warp = threadIdx.x >> 5;
@@ -333,70 +411,145 @@ __global__ void __launch_bounds__(kAlignWarps * 32, REGS ? 6 : 1) align_filter_k
         if (lane == 0) b.aln[base + j] = pack_aln(ori == 2 ? r : f, ori);
     }
     __syncwarp();
-    // mismatch-ratio filter (include/corrector.hpp:1053-1149 single end, 1151-1211 paired end)
-    float thr;
-    if (!p.paired) {
-        uint32_t c0 = 0, c1 = 0, c2 = 0;
-        for (uint32_t j = lane; j < nc; j += 32) {
-            const uint2 v = b.aln[base + j];
-            if ((v.y >> 16) != 3u) {
-                const float ratio = __fdiv_rn((float)(int)(int16_t)(v.y & 0xffffu), (float)(v.x >> 16));
-                c0 += ratio < p.mm2;
-                c1 += ratio < p.mm3;
-                c2 += ratio < p.mm4;
+    filter_anchor(st, p, b, a, base, nc);
+}
+
+// ---------------------------------------------------------------- lane per candidate
+
+// One direction of the reference's sequential shift scan for one lane.
+// S: words of the shifted sequence, O: words of the other one (hi, lo planes,
+// zero past the read).  Right scan (LEFT false): shift sl = 0..n-1 moves the
+// anchor; left scan: sl = 1..n moves the candidate.  max_errors and the break
+// follow src/cpu_alignment.cpp:324-397 / 408-481 exactly; the first two words
+// are evaluated without branches, later ones only while under max_errors.
+template <int MAXW, bool LEFT>
+__device__ __forceinline__ void seq_scan(const uint32_t (&S)[2][2 * MAXW], const uint32_t (&O)[2][2 * MAXW],
+                                         int La, int Lc, int n, int tb, const int16_t* __restrict__ maxErrTab,
+                                         int& bestScore, int& bestShift) {
+    bool done = false;
+#pragma unroll
+    for (int W = 0; W < MAXW; W++) {
+        if (done) break;
+        for (int bb = 0; bb < 32; bb++) {
+            const int sl = 32 * W + bb;
+            if (LEFT && sl == 0) continue;
+            if (LEFT ? sl > n : sl >= n) {
+                done = true;
+                break;
+            }
+            const int ov = LEFT ? min(La, Lc - sl) : min(La - sl, Lc);
+            const int maxErr = min((int)maxErrTab[ov], bestScore - tb + 2 * ov);
+            if (maxErr <= 0) {
+                done = true;
+                break;
+            }
+            const int parts = (ov + 31) >> 5;
+            const int rem = (parts << 5) - ov;
+            const uint32_t last = 0xffffffffu << rem;
+            const uint32_t mask0 = parts > 1 ? 0xffffffffu : last;
+            const uint32_t mask1 = parts > 2 ? 0xffffffffu : (parts == 2 ? last : 0u);
+            const uint32_t h0 = __funnelshift_l(S[0][W + 1], S[0][W], bb), l0 = __funnelshift_l(S[1][W + 1], S[1][W], bb);
+            const uint32_t h1 = __funnelshift_l(S[0][W + 2], S[0][W + 1], bb),
+                           l1 = __funnelshift_l(S[1][W + 2], S[1][W + 1], bb);
+            int m = __popc(((h0 ^ O[0][0]) | (l0 ^ O[1][0])) & mask0) + __popc(((h1 ^ O[0][1]) | (l1 ^ O[1][1])) & mask1);
+            if (m < maxErr && parts > 2) {
+#pragma unroll
+                for (int i = 2; i < MAXW; i++) {
+                    if (i >= parts || m >= maxErr) break;
+                    const uint32_t mask = i == parts - 1 ? last : 0xffffffffu;
+                    const uint32_t hi = __funnelshift_l(S[0][W + i + 1], S[0][W + i], bb);
+                    const uint32_t lo = __funnelshift_l(S[1][W + i + 1], S[1][W + i], bb);
+                    m += __popc(((hi ^ O[0][i]) | (lo ^ O[1][i])) & mask);
+                }
+            }
+            if (m < maxErr) {
+                const int score = m + tb - 2 * ov;
+                if (score < bestScore) {
+                    bestScore = score;
+                    bestShift = LEFT ? -sl : sl;
+                }
             }
         }
-        c0 = __reduce_add_sync(kFull, c0);
-        c1 = __reduce_add_sync(kFull, c1);
-        c2 = __reduce_add_sync(kFull, c2);
-        thr = -3.402823466e+38f;  // std::numeric_limits<float>::lowest()
-        if (c0 > 0 || c1 > 0 || c2 > 0) {
-            if ((float)c0 >= p.goodAlignmentsCountThreshold) thr = p.mm2;
-            else if ((float)c1 >= p.goodAlignmentsCountThreshold) thr = p.mm3;
-            else if ((float)c2 >= p.goodAlignmentsCountThreshold) thr = p.mm4;
-        }
-    } else {
-        thr = p.pairedThreshold;
     }
-    uint32_t kept = 0, aligned = 0;
-    for (uint32_t j0 = 0; j0 < nc; j0 += 32) {
-        const uint32_t j = j0 + lane;
-        bool keep = false, isAligned = false;
-        uint2 v = make_uint2(0, 0);
-        if (j < nc) {
-            v = b.aln[base + j];
-            const int ori = (int)(v.y >> 16);
-            if (ori != 3) {
-                isAligned = true;
-                const int ov = (int)(v.x >> 16);
-                const int nOps = (int)(int16_t)(v.y & 0xffffu);
-                const float ratio = __fdiv_rn((float)nOps, (float)ov);
-                keep = ratio < thr;
-                if (p.paired && b.paired[base + j]) keep = true;
-            }
-        }
-        const uint32_t m = __ballot_sync(kFull, keep);
-        aligned += __popc(__ballot_sync(kFull, isAligned));
-        if (keep) {
-            const uint32_t pos = kept + __popc(m & ((1u << lane) - 1u));
-            const int ov = (int)(v.x >> 16);
-            const int nOps = (int)(int16_t)(v.y & 0xffffu);
-            const uint32_t cid = b.cand[base + j];
-            b.fid[base + pos] = cid;
-            b.fshift[base + pos] = (int16_t)(v.x & 0xffffu);
-            b.forient[base + pos] = (uint8_t)(v.y >> 16);
-            b.flen[base + pos] = st.len[cid];
-            // reference: include/hostdevicefunctions.cuh:93-95 (calculateOverlapWeight)
-            b.fweight[base + pos] =
-                __fsub_rn(1.0f, __fsqrt_rn(__fdiv_rn((float)nOps, __fmul_rn((float)ov, p.maxErrorRate))));
-        }
-        kept += __popc(m);
+}
+
+template <int MAXW>
+__device__ __forceinline__ AlnRes align_seq(const uint32_t (&A)[2][2 * MAXW], const uint32_t (&C)[2][2 * MAXW],
+                                            int La, int Lc, int minov, const int16_t* maxErrTab) {
+    const int tb = La + Lc;
+    int bestScore = tb, bestShift = -Lc;
+    seq_scan<MAXW, false>(A, C, La, Lc, La - minov + 1, tb, maxErrTab, bestScore, bestShift);
+    seq_scan<MAXW, true>(C, A, La, Lc, Lc - minov, tb, maxErrTab, bestScore, bestShift);
+    AlnRes r;
+    r.valid = bestShift != -Lc;
+    const int cb = max(-bestShift, 0);
+    const int ce = min(Lc, La - bestShift);
+    r.overlap = ce - cb;
+    r.score = bestScore;
+    r.shift = bestShift;
+    r.nOps = bestScore - tb + 2 * r.overlap;
+    return r;
+}
+
+template <int MAXW>
+__device__ __forceinline__ void load_planes(uint32_t (&R)[2][2 * MAXW], const uint32_t* __restrict__ hilo, int wp) {
+#pragma unroll
+    for (int i = 0; i < 2 * MAXW; i++) {
+        R[0][i] = i < wp ? hilo[i] : 0u;
+        R[1][i] = i < wp ? hilo[wp + i] : 0u;
     }
-    if (lane == 0) {
-        b.nfinal[a] = kept;
-        atomicAdd(&b.counters[kCounterAligned], (unsigned long long)aligned);
-        atomicAdd(&b.counters[kCounterMsaCands], (unsigned long long)kept);
+}
+
+constexpr int kLaneThreads = 128;
+
+// One thread per (anchor, candidate): both orientations with the reference's
+// sequential scan, the orientation choice, the packed result at the
+// candidate's slot.  uoff = exclusive scan of the per-anchor candidate counts.
+template <int MAXW>
+__global__ void __launch_bounds__(kLaneThreads) align_lane_kernel(StoreArg st, Params p, BatchArg b,
+                                                                  const uint32_t* __restrict__ rawOff,
+                                                                  const uint32_t* __restrict__ uoff, uint32_t total) {
+    __shared__ int16_t maxErrTab[CG_MAX_READ_LENGTH + 2];
+    for (int i = threadIdx.x; i <= st.lmax; i += blockDim.x)
+        maxErrTab[i] = (int16_t)(int)__fmul_rn((float)i, p.maxErrorRate);
+    __syncthreads();
+    const uint32_t t = blockIdx.x * kLaneThreads + threadIdx.x;
+    if (t >= total) return;
+    int lo = 0, hi = b.count;  // last anchor with uoff[a] <= t
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (uoff[mid] <= t) lo = mid;
+        else hi = mid;
     }
+    const int a = lo;
+    const uint32_t j = t - uoff[a];
+    const uint32_t slot = rawOff[a] + j;
+    const uint64_t aid = b.first + (uint64_t)a;
+    const uint32_t id = b.cand[slot];
+    const int La = st.len[aid], Lc = st.len[id];
+    const int wp = st.wp;
+    uint32_t A[2][2 * MAXW], C[2][2 * MAXW];
+    load_planes<MAXW>(A, st.hilo + aid * 4 * (uint64_t)wp, wp);
+    const int minov = max(p.minOverlap, (int)__fmul_rn((float)La, p.minOverlapRatio));
+    load_planes<MAXW>(C, st.hilo + (uint64_t)id * 4 * wp, wp);
+    const AlnRes f = align_seq<MAXW>(A, C, La, Lc, minov, maxErrTab);
+    load_planes<MAXW>(C, st.hilo + (uint64_t)id * 4 * wp + 2 * wp, wp);
+    const AlnRes r = align_seq<MAXW>(A, C, La, Lc, minov, maxErrTab);
+    const int ori = choose_orientation(f, r, La, p.minOverlapRatio, p.minOverlap, p.orientMaxErrorRate);
+    b.aln[slot] = pack_aln(ori == 2 ? r : f, ori);
+}
+
+// one warp per anchor: the mismatch-ratio filter after align_lane_kernel
+__global__ void __launch_bounds__(128) filter_kernel(StoreArg st, Params p, BatchArg b,
+                                                     const uint32_t* __restrict__ rawOff) {
+    const int a = (int)(((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (a >= b.count) return;
+    const uint32_t nc = b.ncand[a];
+    if (nc == 0) {
+        if (lane_id() == 0) b.nfinal[a] = 0;
+        return;
+    }
+    filter_anchor(st, p, b, a, rawOff[a], nc);
 }
 
 // ---------------------------------------------------------------- MSA
@@ -773,8 +926,22 @@ cudaError_t launch_align_t(StoreArg st, Params p, BatchArg b, cudaStream_t s) {
 
 }  // namespace
 
-cudaError_t launch_align_filter(StoreArg st, Params p, BatchArg b, cudaStream_t s) {
+cudaError_t launch_align_filter(StoreArg st, Params p, BatchArg b, const uint32_t* uoff, uint32_t totalUnique,
+                                cudaStream_t s) {
     const int need = st.wp - 1;  // words per plane that hold bases
+    if (need <= 8 && uoff) {
+        if (totalUnique > 0) {
+            const unsigned blocks = (totalUnique + kLaneThreads - 1) / kLaneThreads;
+            if (need <= 5)
+                align_lane_kernel<5><<<blocks, kLaneThreads, 0, s>>>(st, p, b, b.rawCount, uoff, totalUnique);
+            else
+                align_lane_kernel<8><<<blocks, kLaneThreads, 0, s>>>(st, p, b, b.rawCount, uoff, totalUnique);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+        filter_kernel<<<(unsigned)(((uint64_t)b.count * 32 + 127) / 128), 128, 0, s>>>(st, p, b, b.rawCount);
+        return cudaGetLastError();
+    }
     if (need <= 5) return launch_align_t<5, true>(st, p, b, s);
     if (need <= 8) return launch_align_t<8, true>(st, p, b, s);
     if (need <= 16) return launch_align_t<16, false>(st, p, b, s);
