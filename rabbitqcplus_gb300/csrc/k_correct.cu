@@ -915,6 +915,257 @@ __global__ void __launch_bounds__(1024) msa_correct_kernel(StoreArg st, Params p
     }
 }
 
+// ---------------------------------------------------------------- MSA, warp per anchor
+
+// Column statistics derived from a column's weights (src/msa.cpp:135-157).
+struct ColInfo {
+    char cons;
+    float consW, colW;
+};
+
+__device__ __forceinline__ ColInfo col_info(const float* w, int cp, int c) {
+    ColInfo r;
+    const float wA = w[c], wC = w[cp + c], wG = w[2 * cp + c], wT = w[3 * cp + c];
+    r.cons = 'A';
+    r.consW = wA;
+    if (wC > r.consW) { r.cons = 'C'; r.consW = wC; }
+    if (wG > r.consW) { r.cons = 'G'; r.consW = wG; }
+    if (wT > r.consW) { r.cons = 'T'; r.consW = wT; }
+    r.colW = __fadd_rn(__fadd_rn(__fadd_rn(wA, wC), wG), wT);
+    return r;
+}
+
+__device__ __forceinline__ int base_index(char c) { return c == 'A' ? 0 : c == 'C' ? 1 : c == 'G' ? 2 : 3; }
+
+// One warp per anchor (one warp per block) for reads up to 256 bp.
+//
+// Everything the path reads from an MSA -- the different-region search, the
+// properties and both decisions -- lies in the anchor's columns, so only the
+// part of each row that overlaps the anchor is accumulated, in anchor
+// coordinates (column = anchor position).  Shared memory holds per anchor
+// position the four counts and four weights; rows are added one at a time
+// (anchor, then the kept candidates in list order) with the lanes over the
+// row's positions, so every column receives its additions in the reference's
+// order.  Candidate metadata of 32 rows is held one row per lane and the rows'
+// 2-bit words are staged in shared memory per chunk.
+__global__ void __launch_bounds__(32) msa_warp_kernel(StoreArg st, Params p, BatchArg b,
+                                                      const uint32_t* __restrict__ rawOff, int lp) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int lane = (int)lane_id();
+    float* w = reinterpret_cast<float*>(sm);                     // [4][lp]
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(w + 4 * lp);     // [4][lp]
+    float* sup = reinterpret_cast<float*>(cnt + 4 * lp);         // [lp]
+    uint32_t* stage = reinterpret_cast<uint32_t*>(sup + lp);     // [32][pitch]
+    float* qw = reinterpret_cast<float*>(stage + 32 * st.pitch); // [256] (quality scores only)
+    if (p.useQuality) {
+        for (int i = lane; i < 256; i += 32) qw[i] = p.qweight[i];
+    }
+    const int a = blockIdx.x;
+    const uint64_t aid = b.first + (uint64_t)a;
+    const uint32_t nf = b.nfinal[a];
+    char* out = b.out + (uint64_t)a * b.outPitch;
+    if (nf == 0) {
+        if (lane == 0) b.flags[a] = 0;
+        return;
+    }
+    const uint32_t base = rawOff[a];
+    const int La = st.len[aid];
+    const int pitch = st.pitch;
+    const uint32_t* aenc = st.enc + aid * (uint64_t)pitch;
+    const uint8_t* aq = p.useQuality ? st.qual + aid * (uint64_t)st.lmax : nullptr;
+    constexpr uint8_t kRm = 0x80;
+    auto covAt = [&](int c) { return (int)(cnt[c] + cnt[lp + c] + cnt[2 * lp + c] + cnt[3 * lp + c]); };
+
+    int nActive = (int)nf, builds = 0;
+    for (int iter = 0;; iter++) {
+        int act = 0;
+        for (uint32_t j = lane; j < nf; j += 32) act += !(b.forient[base + j] & kRm);
+        nActive = __reduce_add_sync(kFull, act);
+        // anchor row (weight 1 times the quality weight) initialises the columns
+        for (int pos = lane; pos < La; pos += 32) {
+            const uint32_t bb = get2bit(aenc, pos);
+            const float wt = p.useQuality ? __fmul_rn(1.0f, qw[aq[pos]]) : 1.0f;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                w[q * lp + pos] = (uint32_t)q == bb ? __fadd_rn(0.0f, wt) : 0.0f;
+                cnt[q * lp + pos] = (uint32_t)q == bb ? 1u : 0u;
+            }
+        }
+        __syncwarp();
+        for (uint32_t j0 = 0; j0 < nf; j0 += 32) {
+            const uint32_t jr = j0 + lane;
+            const int rows = (int)min(32u, nf - j0);
+            uint32_t mo = kRm, mid = 0;
+            int mshift = 0, mlen = 0;
+            float mw = 0.0f;
+            if (jr < nf) {
+                mo = b.forient[base + jr];
+                mshift = b.fshift[base + jr];
+                mlen = b.flen[base + jr];
+                mid = b.fid[base + jr];
+                mw = b.fweight[base + jr];
+            }
+            for (int i0 = 0; i0 < rows * pitch; i0 += 32) {  // warp-uniform trip count
+                const int idx = i0 + lane;
+                const int r = min(idx / pitch, rows - 1);
+                const uint32_t rid = __shfl_sync(kFull, mid, r);
+                if (idx < rows * pitch) stage[idx] = st.enc[(uint64_t)rid * pitch + (idx - r * pitch)];
+            }
+            __syncwarp();
+            for (int r = 0; r < rows; r++) {
+                const uint32_t o = __shfl_sync(kFull, mo, r);
+                if (o & kRm) continue;
+                const int shift = __shfl_sync(kFull, mshift, r);
+                const int len = __shfl_sync(kFull, mlen, r);
+                const float weight = __shfl_sync(kFull, mw, r);
+                const bool rc = o == 2;
+                const uint32_t* e = stage + r * pitch;
+                const uint8_t* q = nullptr;
+                if (p.useQuality) q = st.qual + (uint64_t)__shfl_sync(kFull, mid, r) * st.lmax;
+                const int c0 = max(shift, 0), c1 = min(La, shift + len);  // overlap with the anchor
+                for (int c = c0 + lane; c < c1; c += 32) {
+                    const int pos = c - shift;
+                    const int sp = rc ? len - 1 - pos : pos;
+                    uint32_t bb = get2bit(e, sp);
+                    if (rc) bb = 3u - bb;
+                    const float wt = p.useQuality ? __fmul_rn(weight, qw[q[sp]]) : weight;
+                    w[bb * lp + c] = __fadd_rn(w[bb * lp + c], wt);
+                    cnt[bb * lp + c]++;
+                }
+                __syncwarp();
+            }
+        }
+        builds++;
+        if (iter == 5 || nActive == 0) break;
+        // findCandidatesOfDifferentRegion (src/msa.cpp:532-734), in anchor coordinates
+        bool mism = false;
+        int firstSig = 0x7fffffff;
+        for (int c = lane; c < La; c += 32) {
+            const ColInfo ci = col_info(w, lp, c);
+            mism |= ci.cons != "ACGT"[get2bit(aenc, c)];
+            const int cidx = base_index(ci.cons);
+            bool sig = false;
+            for (int i = 0; i < 4; i++) sig |= (i != cidx && p.significantCount <= (int)cnt[i * lp + c]);
+            if (sig && c < firstSig) firstSig = c;
+        }
+        if (!__any_sync(kFull, mism)) break;
+        const int col = __reduce_min_sync(kFull, firstSig);
+        if (col == 0x7fffffff) break;
+        int found;
+        {
+            const ColInfo ci = col_info(w, lp, col);
+            const int cidx = base_index(ci.cons);
+            found = -1;
+            for (int i = 0; i < 4; i++)
+                if (i != cidx && p.significantCount <= (int)cnt[i * lp + col]) found = i;
+        }
+        const uint32_t orig = get2bit(aenc, col);
+        const bool keepMatching = orig == (uint32_t)found;
+        auto differs = [&](uint32_t j) -> bool {
+            const uint32_t g = base + j;
+            const int sh = b.fshift[g];
+            const int len = b.flen[g];
+            if (col < sh || col >= sh + len) return false;
+            const uint32_t* e = st.enc + (uint64_t)b.fid[g] * pitch;
+            const int pos = col - sh;
+            const bool rc = (b.forient[g] & 3) == 2;
+            uint32_t bb = get2bit(e, rc ? len - 1 - pos : pos);
+            if (rc) bb = 3u - bb;
+            return keepMatching ? (bb != (uint32_t)found) : (bb == (uint32_t)found);
+        };
+        bool veto = false, any = false;
+        for (uint32_t j = lane; j < nf; j += 32) {
+            if ((b.forient[base + j] & kRm) || !differs(j)) continue;
+            any = true;
+            veto |= b.fweight[base + j] >= 0.90f;
+        }
+        // a veto (or nothing to remove) leaves the MSA as it is; the
+        // reference then rebuilds the same MSA and reaches the same decision
+        if (__any_sync(kFull, veto) || !__any_sync(kFull, any)) break;
+        for (uint32_t j = lane; j < nf; j += 32) {
+            const uint8_t o = b.forient[base + j];
+            if (!(o & kRm) && differs(j)) b.forient[base + j] = o | kRm;
+        }
+        __syncwarp();
+    }
+    // getMSAProperties (src/msa.cpp:304-376) and the decision
+    float mins = 3.402823466e+38f;
+    int minc = 0x7fffffff, maxc = -1;
+    for (int c = lane; c < La; c += 32) {
+        const ColInfo ci = col_info(w, lp, c);
+        const float s = __fdiv_rn(ci.consW, ci.colW);
+        sup[c] = s;
+        mins = fminf(mins, s);
+        const int cv = covAt(c);
+        minc = min(minc, cv);
+        maxc = max(maxc, cv);
+    }
+    for (int d = 16; d > 0; d >>= 1) mins = fminf(mins, __shfl_xor_sync(kFull, mins, d));
+    minc = __reduce_min_sync(kFull, minc);
+    maxc = __reduce_max_sync(kFull, maxc);
+    __syncwarp();
+    float avg = 0.0f;
+    if (lane == 0) {
+        float sum = 0.0f;
+        for (int i = 0; i < La; i++) sum = __fadd_rn(sum, sup[i]);
+        avg = __fdiv_rn(sum, (float)La);
+    }
+    avg = __shfl_sync(kFull, avg, 0);
+    const bool good = fgeq(avg, p.avgSupportThreshold) && fgeq(mins, p.minSupportThreshold) &&
+                      fgeq((float)minc, p.minCoverageThreshold);
+    bool hq = false;
+    if (good) {
+        int smallest = 100;
+        for (int percent = p.errPercent; percent >= 0; percent--) {
+            if (fgeq(avg, p.hqAvg[percent]) && fgeq(mins, p.hqMin[percent])) smallest = percent;
+        }
+        hq = fgeq((float)minc, p.minCoverageThreshold) && fleq((float)smallest, p.hqPercentLimit);
+    }
+    const bool forest = p.correctionType == CG_CORR_FOREST;
+    const bool corrected = forest || nActive > 0;
+    if (lane == 0) {
+        if (corrected) {
+            atomicAdd(&b.counters[kCounterCorrected], 1ull);
+            if (hq) atomicAdd(&b.counters[kCounterHQ], 1ull);
+        }
+        atomicAdd(&b.counters[kCounterMsaBuilds], (unsigned long long)builds);
+        b.flags[a] = corrected ? (uint8_t)(CG_RESULT_CORRECTED | (hq ? CG_RESULT_HQ : 0)) : (uint8_t)0;
+    }
+    if (!corrected) return;
+    for (int c = lane; c < La; c += 32) {
+        const uint32_t ab = get2bit(aenc, c);
+        const char orig = "ACGT"[ab];
+        const ColInfo ci = col_info(w, lp, c);
+        const int origCov = (int)cnt[ab * lp + c];
+        char r;
+        if (forest) {
+            // correctAnchorClf (include/corrector.hpp:1448-1472), features of
+            // include/classification.hpp:748-797
+            r = ci.cons;
+            if (!hq && r != orig) {
+                const int ci_ = base_index(ci.cons);
+                const float wCons = w[ci_ * lp + c];
+                const float nCons = (float)cnt[ci_ * lp + c];
+                const float wOrig = w[ab * lp + c];
+                const float cv = (float)covAt(c);
+                const float oc = (float)origCov;
+                const float ec = p.estimatedCoverage;
+                const float f[13] = {__fdiv_rn(oc, cv),      __fdiv_rn(wOrig, ci.colW), __fdiv_rn(wOrig, oc),
+                                     __fdiv_rn(nCons, cv),   sup[c],                    __fdiv_rn(wCons, nCons),
+                                     __fdiv_rn(ci.colW, cv), __fdiv_rn(cv, ec),         __fdiv_rn(ci.colW, ec),
+                                     avg,                    mins,                      __fdiv_rn((float)maxc, ec),
+                                     __fdiv_rn((float)minc, ec)};
+                if (!forest_decide(p, f)) r = orig;
+            }
+        } else if (good) {
+            r = ci.cons;
+        } else {
+            r = (sup[c] > 0.90f && origCov <= 2) ? ci.cons : orig;
+        }
+        out[c] = r;
+    }
+}
+
 template <int MAXW, bool REGS>
 cudaError_t launch_align_t(StoreArg st, Params p, BatchArg b, cudaStream_t s) {
     const size_t smem = (size_t)kAlignWarps * 6 * st.wp * sizeof(uint32_t) +
@@ -961,6 +1212,17 @@ size_t msa_smem_bytes(int maxCols, int bitsetWords, int storeWeights) {
 
 cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, int maxRows, cudaStream_t s) {
     const int maxCols = 3 * st.lmax + 4;
+    if (st.lmax <= 256) {
+        const int lp = (st.lmax + 31) / 32 * 32;
+        const size_t smem = (size_t)lp * (9 * sizeof(float)) + (size_t)32 * st.pitch * sizeof(uint32_t) +
+                            (p.useQuality ? 256 * sizeof(float) : 0);
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(msa_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        msa_warp_kernel<<<b.count, 32, smem, s>>>(st, p, b, b.rawCount, lp);
+        return cudaGetLastError();
+    }
     const int bitsetWords = (maxRows + 31) / 32 + 1;
     const int storeWeights = p.correctionType == CG_CORR_FOREST;
     const size_t smem = msa_smem_bytes(maxCols, bitsetWords, storeWeights);
