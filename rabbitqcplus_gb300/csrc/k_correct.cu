@@ -1216,7 +1216,7 @@ cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, int maxRows, c
         const int lp = (st.lmax + 31) / 32 * 32;
         const size_t smem = (size_t)lp * (9 * sizeof(float)) + (size_t)32 * st.pitch * sizeof(uint32_t) +
                             (p.useQuality ? 256 * sizeof(float) : 0);
-        if (smem > 48 * 1024) {
+        if (smem > 40 * 1024) {  // leaves room for the kernel's static shared memory
             cudaError_t e = cudaFuncSetAttribute(msa_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
         }
@@ -1226,7 +1226,7 @@ cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, int maxRows, c
     const int bitsetWords = (maxRows + 31) / 32 + 1;
     const int storeWeights = p.correctionType == CG_CORR_FOREST;
     const size_t smem = msa_smem_bytes(maxCols, bitsetWords, storeWeights);
-    if (smem > 48 * 1024) {
+    if (smem > 40 * 1024) {  // leaves room for the kernel's static shared memory
         cudaError_t e = cudaFuncSetAttribute(msa_correct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;

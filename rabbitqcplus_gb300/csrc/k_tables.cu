@@ -164,16 +164,20 @@ __global__ void query_count_kernel(StoreArg st, TablesArg tb, Params p, BatchArg
 
 constexpr int kGatherThreads = 128;
 
-// One block per anchor: gather the bucket contents into shared memory, bitonic
-// sort, keep first occurrences, drop the anchor itself (and ambiguous reads
-// if requested).  rawOff = exclusive scan of the raw counts.
+// One block per anchor: the union of the anchor's buckets, ascending, without
+// the anchor itself (and without ambiguous reads if requested).  The raw ids
+// go into a shared-memory hash set (duplicates vanish on insert); the unique
+// ids are then put in ascending order by rank (or a bitonic sort when there
+// are many).  rawOff = exclusive scan of the raw counts; the table holds
+// tableSize >= 2 * raw slots.
 __global__ void __launch_bounds__(kGatherThreads) gather_unique_kernel(StoreArg st, TablesArg tb, Params p,
                                                                        BatchArg b, const uint32_t* __restrict__ rawOff,
-                                                                       int sortSize) {
-    extern __shared__ uint32_t buf[];
+                                                                       int tableSize) {
+    extern __shared__ uint32_t table[];        // [tableSize], then list[tableSize / 2]
+    uint32_t* list = table + tableSize;
     __shared__ uint2 rng[kMaxMaps];
     __shared__ uint32_t pre[kMaxMaps + 1];
-    __shared__ uint32_t warpSum[kGatherThreads / 32];
+    __shared__ uint32_t nUnique;
     const int a = blockIdx.x;
     const uint64_t aid = b.first + (uint64_t)a;
     const uint32_t raw = rawOff[a + 1] - rawOff[a];
@@ -182,7 +186,12 @@ __global__ void __launch_bounds__(kGatherThreads) gather_unique_kernel(StoreArg 
         if (tid == 0) b.ncand[a] = 0;
         return;
     }
+    uint32_t T = 64;
+    while (T < 2 * raw) T <<= 1;
+    const uint32_t mask = T - 1;
     if (tid < tb.nmaps) rng[tid] = b.qrange[(uint64_t)a * tb.nmaps + tid];
+    for (uint32_t i = tid; i < T; i += kGatherThreads) table[i] = 0xffffffffu;
+    if (tid == 0) nUnique = 0;
     __syncthreads();
     if (tid == 0) {
         uint32_t acc = 0;
@@ -193,67 +202,81 @@ __global__ void __launch_bounds__(kGatherThreads) gather_unique_kernel(StoreArg 
         pre[tb.nmaps] = acc;
     }
     __syncthreads();
-    for (int m = 0; m < tb.nmaps; m++) {
-        const uint32_t c = rng[m].y;
-        const uint32_t* src = tb.values[m] + rng[m].x;
-        for (uint32_t j = tid; j < c; j += kGatherThreads) buf[pre[m] + j] = src[j];
-    }
-    int S = 32;
-    while ((uint32_t)S < raw) S <<= 1;
-    for (int j = (int)raw + tid; j < S; j += kGatherThreads) buf[j] = 0xffffffffu;
-    __syncthreads();
-    for (int k = 2; k <= S; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = tid; i < S; i += kGatherThreads) {
-                const int ixj = i ^ j;
-                if (ixj > i) {
-                    const uint32_t x = buf[i], y = buf[ixj];
-                    const bool asc = (i & k) == 0;
-                    if ((x > y) == asc) {
-                        buf[i] = y;
-                        buf[ixj] = x;
-                    }
+    // every thread loads its raw ids first (independent loads), then inserts them
+    constexpr int kPer = 8;
+    for (uint32_t i0 = 0; i0 < raw; i0 += kGatherThreads * kPer) {
+        uint32_t vals[kPer];
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            const uint32_t i = i0 + (uint32_t)k * kGatherThreads + tid;
+            vals[k] = 0xffffffffu;
+            if (i < raw) {
+                int lo = 0, hi = tb.nmaps;  // last map with pre[m] <= i
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (pre[mid] <= i) lo = mid;
+                    else hi = mid;
                 }
+                vals[k] = tb.values[lo][rng[lo].x + (i - pre[lo])];
             }
-            __syncthreads();
+        }
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            const uint32_t v = vals[k];
+            if (v == 0xffffffffu) continue;
+            uint32_t h = (v * 0x9E3779B1u) & mask;
+            for (uint32_t probe = 0; probe < T; probe++) {
+                const uint32_t old = atomicCAS(&table[h], 0xffffffffu, v);
+                if (old == 0xffffffffu || old == v) break;
+                h = (h + 1) & mask;
+            }
         }
     }
-    // keep flags over contiguous chunks, block scan, compact
-    const int per = S / kGatherThreads > 0 ? S / kGatherThreads : 1;
-    const int lo = tid * per;
-    auto keep = [&](int j) -> bool {
-        if (j >= S) return false;
-        const uint32_t v = buf[j];
-        if (v == 0xffffffffu) return false;
-        if (j > 0 && buf[j - 1] == v) return false;
-        if ((uint64_t)v == aid) return false;
-        if (p.excludeAmbiguous && st.ambig[v]) return false;
-        return true;
-    };
-    uint32_t mine = 0;
-    for (int j = lo; j < lo + per; j++) mine += keep(j);
-    const int lane = tid & 31, warp = tid >> 5;
-    uint32_t incl = mine;
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= d) incl += y;
-    }
-    if (lane == 31) warpSum[warp] = incl;
     __syncthreads();
-    uint32_t before = 0, total = 0;
-    for (int w = 0; w < kGatherThreads / 32; w++) {
-        if (w < warp) before += warpSum[w];
-        total += warpSum[w];
+    for (uint32_t i = tid; i < T; i += kGatherThreads) {
+        const uint32_t v = table[i];
+        if (v == 0xffffffffu || (uint64_t)v == aid) continue;
+        if (p.excludeAmbiguous && st.ambig[v]) continue;
+        list[atomicAdd(&nUnique, 1u)] = v;
     }
-    uint32_t pos = before + incl - mine;
+    __syncthreads();
+    const uint32_t U = nUnique;
     uint32_t* out = b.cand + rawOff[a];
-    for (int j = lo; j < lo + per; j++) {
-        if (keep(j)) out[pos++] = buf[j];
+    if (U <= 512) {
+        // rank of each id among the unique ids = its position in ascending order
+        for (uint32_t i = tid; i < U; i += kGatherThreads) {
+            const uint32_t v = list[i];
+            uint32_t rank = 0;
+            for (uint32_t k = 0; k < U; k++) rank += list[k] < v;
+            out[rank] = v;
+        }
+    } else {
+        uint32_t S = 1;
+        while (S < U) S <<= 1;  // S <= T: the hash table's space becomes the sort buffer
+        for (uint32_t i = tid; i < S; i += kGatherThreads) table[i] = i < U ? list[i] : 0xffffffffu;
+        __syncthreads();
+        for (uint32_t k = 2; k <= S; k <<= 1) {
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                for (uint32_t i = tid; i < S; i += kGatherThreads) {
+                    const uint32_t ixj = i ^ j;
+                    if (ixj > i) {
+                        const uint32_t x = table[i], y = table[ixj];
+                        const bool asc = (i & k) == 0;
+                        if ((x > y) == asc) {
+                            table[i] = y;
+                            table[ixj] = x;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (uint32_t i = tid; i < U; i += kGatherThreads) out[i] = table[i];
     }
     if (tid == 0) {
-        b.ncand[a] = total;
+        b.ncand[a] = U;
         atomicAdd(&b.counters[kCounterRaw], (unsigned long long)raw);
-        atomicAdd(&b.counters[kCounterUnique], (unsigned long long)total);
+        atomicAdd(&b.counters[kCounterUnique], (unsigned long long)U);
     }
 }
 
@@ -385,15 +408,15 @@ cudaError_t launch_query_count(StoreArg st, TablesArg tb, Params p, BatchArg b, 
 
 cudaError_t launch_gather_unique(StoreArg st, TablesArg tb, Params p, BatchArg b, int maxRawPerAnchor,
                                  cudaStream_t s) {
-    int S = 32;
-    while (S < maxRawPerAnchor) S <<= 1;
-    const size_t smem = (size_t)S * sizeof(uint32_t);
-    if (smem > 48 * 1024) {
+    int T = 64;
+    while (T < 2 * maxRawPerAnchor) T <<= 1;
+    const size_t smem = (size_t)T * sizeof(uint32_t) * 3 / 2;  // table + unique list
+    if (smem > 40 * 1024) {  // leaves room for the kernel's static shared memory
         cudaError_t e = cudaFuncSetAttribute(gather_unique_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
     }
-    gather_unique_kernel<<<b.count, kGatherThreads, smem, s>>>(st, tb, p, b, b.rawCount, S);
+    gather_unique_kernel<<<b.count, kGatherThreads, smem, s>>>(st, tb, p, b, b.rawCount, T);
     return cudaGetLastError();
 }
 
