@@ -194,6 +194,21 @@ int cg_correct_files(const cg_options* options, const char* const* inputs, int n
                      int quality_labels, int gz_output, uint64_t* num_records);
 int cg_get_candidates(cg_ctx* ctx, uint64_t anchor, uint32_t* out, uint32_t capacity, uint32_t* count);
 
+/*
+ * No counterpart in the reference: cg_get_candidates for callers that cannot
+ * allocate device memory (an application that gives its whole device budget
+ * to its own pool, or one that looks up single reads in a latency-sensitive
+ * loop and must not pay the synchronisation cudaMalloc/cudaFree can imply).
+ * Same arguments and result as cg_get_candidates; allocates nothing.  Its
+ * scratch is a fixed 33 KiB device array inside the library, held by every
+ * GPU that loads it until the process exits, shared by all calls and left
+ * holding the last call's data; so calls must not overlap on the GPU.  The
+ * first call on a device looks the array up (do it before any stream capture).
+ * An anchor with more than 8192 raw bucket hits is rejected with
+ * CG_ERR_INVALID_ARGUMENT (cg_get_candidates handles it).
+ */
+int cg_get_candidates_noalloc(cg_ctx* ctx, uint64_t anchor, uint32_t* out, uint32_t capacity, uint32_t* count);
+
 #ifdef __cplusplus
 }
 #endif

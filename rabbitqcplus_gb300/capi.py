@@ -88,7 +88,7 @@ class CgStats(ctypes.Structure):
 # every symbol include/care_gpu.h declares
 EXPORTED = ["cg_default_options", "cg_create", "cg_destroy", "cg_last_error", "cg_append_reads",
             "cg_build_tables", "cg_correct", "cg_get_stats", "cg_get_read_info", "cg_get_signatures",
-            "cg_get_candidates", "cg_correct_files", "cg_load_forest"]
+            "cg_get_candidates", "cg_correct_files", "cg_load_forest", "cg_get_candidates_noalloc"]
 
 
 def gpu_lib() -> ctypes.CDLL:
@@ -110,6 +110,8 @@ def gpu_lib() -> ctypes.CDLL:
         L.cg_correct_files.argtypes = [P, P, ctypes.c_int, ctypes.c_char_p, P, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
         L.cg_load_forest.argtypes = [P, P, ctypes.c_size_t, ctypes.c_uint32]
+        L.cg_get_candidates_noalloc.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32,
+                                                ctypes.POINTER(ctypes.c_uint32)]
         for f in EXPORTED:
             if f not in ("cg_destroy", "cg_default_options", "cg_last_error"):
                 getattr(L, f).restype = ctypes.c_int
@@ -187,6 +189,14 @@ class CareGpu:
         self._check(self._L.cg_get_candidates(self._h, anchor, out.ctypes.data, cap, ctypes.byref(cnt)),
                     "cg_get_candidates")
         return out[:cnt.value].copy()
+
+    def candidates_noalloc(self, anchor: int, out: np.ndarray) -> int:
+        """cg_get_candidates_noalloc into a caller-owned uint32 array; returns the count."""
+        assert out.dtype == np.uint32 and out.flags["C_CONTIGUOUS"]
+        cnt = ctypes.c_uint32()
+        self._check(self._L.cg_get_candidates_noalloc(self._h, anchor, out.ctypes.data, out.size, ctypes.byref(cnt)),
+                    "cg_get_candidates_noalloc")
+        return cnt.value
 
     def close(self):
         if getattr(self, "_h", None):

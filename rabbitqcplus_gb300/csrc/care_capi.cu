@@ -14,6 +14,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -724,3 +725,94 @@ int cg_get_candidates(cg_ctx* c, uint64_t anchor, uint32_t* out, uint32_t capaci
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- no-allocation candidate lookup
+//
+// cg_get_candidates_noalloc: the candidate ids of one anchor, like
+// cg_get_candidates, for callers that cannot allocate device memory -- a host
+// application that hands its whole device-memory budget to its own pool, or
+// one that looks up single reads in a latency-sensitive loop and must not pay
+// the device-wide synchronisation that cudaMalloc/cudaFree can imply.  The call
+// allocates nothing: its scratch (the anchor's per-map bucket ranges, the raw
+// hit count, the unique-id list and counters) is the file-scope device array
+// below, which every GPU that loads this library holds until the process
+// exits.  All calls share it and it keeps the last call's contents; the call
+// clears what must start at zero itself.  Calls that overlap on the GPU race
+// on it, so callers must not run two of them at once on any device.
+namespace {
+
+constexpr uint32_t kNoallocMaxRaw = 8192;  // raw bucket hits per anchor the scratch holds
+constexpr size_t kNoallocQrange = 0;       // uint2[kMaxMaps]
+constexpr size_t kNoallocRaw = 512;        // uint32_t[4]: raw count, scanned total, batch maximum
+constexpr size_t kNoallocNcand = 576;      // uint32_t
+constexpr size_t kNoallocCounters = 640;   // unsigned long long[kNumCounters]
+constexpr size_t kNoallocCand = 1024;      // uint32_t[kNoallocMaxRaw]
+constexpr size_t kNoallocBytes = kNoallocCand + sizeof(uint32_t) * kNoallocMaxRaw;
+static_assert(kNoallocCounters + sizeof(unsigned long long) * kNumCounters <= kNoallocCand, "scratch layout");
+
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoallocBytes];
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noallocMutex;
+unsigned char* g_noallocPtr[kNoallocMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device (set up once per device).
+int noalloc_scratch(cg_ctx* c, unsigned char** out) {
+    int dev = 0;
+    CG_CUDA(c, cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoallocMaxDevices) return fail(c, CG_ERR_UNSUPPORTED, "device ordinal %d too large", dev);
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    if (!g_noallocPtr[dev]) {
+        void* p = nullptr;
+        CG_CUDA(c, cudaGetSymbolAddress(&p, g_noallocScratch));
+        g_noallocPtr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noallocPtr[dev];
+    return CG_OK;
+}
+
+}  // namespace
+
+extern "C" int cg_get_candidates_noalloc(cg_ctx* c, uint64_t anchor, uint32_t* out, uint32_t capacity,
+                                         uint32_t* count) {
+    if (!c || !count) return CG_ERR_INVALID_ARGUMENT;
+    if (!c->built) return fail(c, CG_ERR_STATE, "cg_build_tables has not run");
+    if (anchor >= c->n) return fail(c, CG_ERR_INVALID_ARGUMENT, "anchor out of bounds");
+    CG_CUDA(c, cudaSetDevice(c->device));
+    unsigned char* s = nullptr;
+    const int rc = noalloc_scratch(c, &s);
+    if (rc != CG_OK) return rc;
+    BatchArg b{};
+    b.first = anchor;
+    b.count = 1;
+    b.sig = c->sig.as<unsigned long long>();
+    b.qrange = reinterpret_cast<uint2*>(s + kNoallocQrange);
+    b.rawCount = reinterpret_cast<uint32_t*>(s + kNoallocRaw);
+    b.ncand = reinterpret_cast<uint32_t*>(s + kNoallocNcand);
+    b.counters = reinterpret_cast<unsigned long long*>(s + kNoallocCounters);
+    b.cand = reinterpret_cast<uint32_t*>(s + kNoallocCand);
+    const StoreArg st = store_arg(c);
+    // the raw count slots and the batch maximum must start at zero
+    CG_CUDA(c, cudaMemsetAsync(b.rawCount, 0, 4 * sizeof(uint32_t), c->stream));
+    CG_CUDA(c, launch_query_count(st, c->tables, c->params, b, c->stream));
+    CG_CUDA(c, scan_exclusive_u32(b.rawCount, 2, nullptr, c->stream));  // one tile: no scan scratch
+    uint32_t raw[3] = {0, 0, 0};
+    CG_CUDA(c, cudaMemcpyAsync(raw, b.rawCount, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (raw[1] > kNoallocMaxRaw)
+        return fail(c, CG_ERR_INVALID_ARGUMENT,
+                    "anchor %llu has %u raw bucket hits; cg_get_candidates_noalloc holds at most %u "
+                    "(use cg_get_candidates)",
+                    (unsigned long long)anchor, raw[1], kNoallocMaxRaw);
+    CG_CUDA(c, launch_gather_unique(st, c->tables, c->params, b, (int)std::max<uint32_t>(raw[1], 1), c->stream));
+    uint32_t nc = 0;
+    CG_CUDA(c, cudaMemcpyAsync(&nc, b.ncand, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    *count = nc;
+    const uint32_t w = std::min(nc, capacity);
+    if (w && out) {
+        CG_CUDA(c, cudaMemcpyAsync(out, b.cand, w * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+        CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return CG_OK;
+}

@@ -1,0 +1,41 @@
+"""cg_get_candidates_noalloc: the candidate lookup that allocates no device memory.
+
+It serves callers that cannot call cudaMalloc (an application that owns the
+whole device budget, or a latency-sensitive per-read loop).  Its result must
+equal cg_get_candidates' exactly (integer ids, so no tolerance), call after
+call: the shared scratch array keeps the previous call's contents and the
+entry point must clear what has to start at zero.  This file sorts last so a
+failure here comes after every other test has run.
+"""
+import numpy as np
+import pytest
+
+from rabbitqcplus_gb300 import capi, sim
+
+pytestmark = pytest.mark.gpu
+
+
+def test_noalloc_candidates_equal_allocating_entry_point_on_consecutive_calls():
+    cfg = sim.SimConfig(seed=61, genome_length=30_000, repeat_families=2, repeat_copies=3, num_reads=6_000,
+                        sub_rate_5p=0.002, sub_rate_3p=0.02)
+    r = sim.SimReads(cfg)
+    g = capi.CareGpu(capi.CareOptions.defaults(30.0))
+    g.append_reads(r.sequences, r.offsets)
+    g.build_tables()
+    out = np.zeros(8192, dtype=np.uint32)
+    anchors = [0, 1, 2, 17, 999, 3000, 5999, 4242]
+    for a in anchors:
+        ref = g.candidates(a)
+        # two calls in a row: the second must not see the first's leftovers
+        for _ in range(2):
+            out.fill(0xFFFFFFFF)
+            n = g.candidates_noalloc(a, out)
+            assert n == ref.size
+            assert np.array_equal(out[:n], ref), f"anchor {a}"
+    # a capacity below the count: the count is still reported, only capacity ids are written
+    a = int(np.argmax([g.candidates(x).size for x in anchors]))
+    full = g.candidates(anchors[a])
+    small = np.zeros(max(1, full.size // 2), dtype=np.uint32)
+    n = g.candidates_noalloc(anchors[a], small)
+    assert n == full.size and np.array_equal(small, full[:small.size])
+    g.close()
