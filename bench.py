@@ -209,6 +209,7 @@ def main():
 
     # roofline of the dominant kernel (by device time in the timed region)
     stages = {"align": st1["seconds_align"] - st0["seconds_align"],
+              "filter": st1["seconds_filter"] - st0["seconds_filter"],
               "msa": st1["seconds_msa"] - st0["seconds_msa"],
               "candidates": st1["seconds_candidates"] - st0["seconds_candidates"]}
     dom = max(stages, key=stages.get)
@@ -216,17 +217,22 @@ def main():
     per_step_cands = (st1["unique_candidates"] - st0["unique_candidates"]) / args.steps
     per_step_msa = (st1["msa_candidates"] - st0["msa_candidates"]) / args.steps
     wp = (lmax + 31) // 32 + 1
+    pitch = (lmax + 15) // 16
     if dom == "align":
-        # per candidate: its fwd+rc hi/lo planes, its id, the packed result (write + reread),
-        # the filtered record; per anchor: its planes and counters
-        bytes_step = per_step_cands * (16 * wp + 4 + 8 + 8) + per_step_msa * 11 + n * (8 * wp + 16)
+        # align_lane_kernel, per candidate: its id (4 B) and length (2 B), its forward and
+        # reverse-complement hi/lo planes (4*wp words), the packed result (8 B);
+        # per anchor: its forward planes (2*wp words), length and two offsets (10 B)
+        bytes_step = per_step_cands * (4 + 2 + 16 * wp + 8) + n * (8 * wp + 10)
         launches_k = (st1["align_launches"] - st0["align_launches"])
     elif dom == "msa":
-        bytes_step = per_step_msa * (11 + 4 * ((lmax + 15) // 16)) + n * (4 * ((lmax + 15) // 16) + lmax + 8)
+        # msa_warp_kernel, per kept candidate: its record (id, shift, length, orientation,
+        # weight = 13 B) and its 2-bit row; per anchor: its 2-bit row, length, the
+        # corrected bases and flags written
+        bytes_step = per_step_msa * (13 + 4 * pitch) + n * (4 * pitch + 2 + lmax + 1)
         launches_k = (st1["msa_launches"] - st0["msa_launches"])
     else:
-        bytes_step = (st1["raw_candidate_ids"] - st0["raw_candidate_ids"]) / args.steps * 8 + n * 48 * 24
-        launches_k = launches
+        bytes_step = (st1["raw_candidate_ids"] - st0["raw_candidate_ids"]) / args.steps * 4 + n * 48 * 24
+        launches_k = max(st1["align_launches"] - st0["align_launches"], 1)
     dur = stages[dom] / max(launches_k, 1)
     bytes_launch = bytes_step * args.steps / max(launches_k, 1)
     achieved = bytes_launch / dur / 1e9

@@ -111,6 +111,7 @@ typedef struct cg_stats {
     uint64_t kernel_launches;         /* kernels this context launched, accumulated */
     uint64_t align_launches;          /* launches of the alignment/filter kernel */
     uint64_t msa_launches;            /* launches of the MSA/correction kernel */
+    double seconds_filter;            /* device time in the mismatch-ratio filter kernel, accumulated */
 } cg_stats;
 
 /* Fill *o with the reference defaults. */

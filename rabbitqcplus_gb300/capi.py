@@ -79,7 +79,8 @@ class CgStats(ctypes.Structure):
         ("kmerlength", ctypes.c_int32), ("num_maps", ctypes.c_int32), ("max_read_length", ctypes.c_int32),
         ("reserved", ctypes.c_int32), ("seconds_build", ctypes.c_double), ("seconds_correct", ctypes.c_double),
         ("seconds_candidates", ctypes.c_double), ("seconds_align", ctypes.c_double), ("seconds_msa", ctypes.c_double),
-        ("kernel_launches", ctypes.c_uint64), ("align_launches", ctypes.c_uint64), ("msa_launches", ctypes.c_uint64)]
+        ("kernel_launches", ctypes.c_uint64), ("align_launches", ctypes.c_uint64), ("msa_launches", ctypes.c_uint64),
+        ("seconds_filter", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}

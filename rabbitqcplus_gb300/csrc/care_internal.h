@@ -175,7 +175,7 @@ cudaError_t launch_pair_flags(BatchArg b, cudaStream_t s);
 // uoff: exclusive scan of the per-anchor candidate counts (count+1 entries),
 // totalUnique = uoff[count]; with uoff null the warp-per-anchor kernel runs
 cudaError_t launch_align_filter(StoreArg st, Params p, BatchArg b, const uint32_t* uoff, uint32_t totalUnique,
-                                cudaStream_t s);
+                                cudaEvent_t between, cudaStream_t s);  // `between` (optional) after the alignment
 cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, int maxRows, cudaStream_t s);
 
 }  // namespace cg

@@ -1178,7 +1178,7 @@ cudaError_t launch_align_t(StoreArg st, Params p, BatchArg b, cudaStream_t s) {
 }  // namespace
 
 cudaError_t launch_align_filter(StoreArg st, Params p, BatchArg b, const uint32_t* uoff, uint32_t totalUnique,
-                                cudaStream_t s) {
+                                cudaEvent_t between, cudaStream_t s) {
     const int need = st.wp - 1;  // words per plane that hold bases
     if (need <= 8 && uoff) {
         if (totalUnique > 0) {
@@ -1190,8 +1190,16 @@ cudaError_t launch_align_filter(StoreArg st, Params p, BatchArg b, const uint32_
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) return e;
         }
+        if (between) {
+            cudaError_t e = cudaEventRecord(between, s);
+            if (e != cudaSuccess) return e;
+        }
         filter_kernel<<<(unsigned)(((uint64_t)b.count * 32 + 127) / 128), 128, 0, s>>>(st, p, b, b.rawCount);
         return cudaGetLastError();
+    }
+    if (between) {
+        cudaError_t e = cudaEventRecord(between, s);  // the fused kernel below aligns and filters
+        if (e != cudaSuccess) return e;
     }
     if (need <= 5) return launch_align_t<5, true>(st, p, b, s);
     if (need <= 8) return launch_align_t<8, true>(st, p, b, s);

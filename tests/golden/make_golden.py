@@ -124,10 +124,21 @@ def run_case(name: str, cfg: sim.SimConfig, opts: dict, stage_anchors: int, work
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), read=np.diff(rid, prepend=np.uint32(0)).astype(np.uint32),
                         pos=pos, base=out_all[diff])
     changed = np.unique(rid)
+    out_files = [os.path.join(d, f"out_{i}.fq") for i in range(len(inputs))]
+    in_files_md5 = []
+    for pth in inputs:
+        with open(pth, "rb") as f:
+            in_files_md5.append(md5(f.read()))
+    out_files_md5 = []
+    for pth in out_files:
+        with open(pth, "rb") as f:
+            out_files_md5.append(md5(f.read()))
     entry = {
         "config": dataclasses.asdict(cfg),
         "options": opts,
         "num_reads": reads.n,
+        "input_file_md5": in_files_md5,
+        "output_file_md5": out_files_md5,
         "input_md5": md5(reads.sequences.tobytes()),
         "input_qual_md5": md5(reads.qualities.tobytes()),
         "output_md5": md5(out_all.tobytes()),
@@ -144,7 +155,8 @@ def run_case(name: str, cfg: sim.SimConfig, opts: dict, stage_anchors: int, work
         r = subprocess.run(scmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"stage dump failed on {name}:\n{r.stdout[-3000:]}")
-        with open(st, "rb") as f, gzip.open(os.path.join(HERE, f"{name}.stages.txt.gz"), "wb", compresslevel=9) as g:
+        with open(st, "rb") as f, gzip.GzipFile(os.path.join(HERE, f"{name}.stages.txt.gz"), "wb", compresslevel=9,
+                                                mtime=0) as g:
             shutil.copyfileobj(f, g)
         entry["stage_anchors"] = stage_anchors
     return entry
