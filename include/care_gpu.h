@@ -80,8 +80,23 @@ typedef struct cg_options {
     float threshold_anchor;           /* thresholdAnchor for the learned decision (0.5) */
     int32_t device;                   /* CUDA device ordinal */
     int32_t batch_anchors;            /* anchors per device batch; 0 = automatic */
-    int32_t reserved[8];
+    /* Driver of cg_correct (no reference counterpart; both give identical
+     * results).  CG_DRIVER_PLAIN runs each batch as stage kernels with host
+     * round trips for its sizes.  CG_DRIVER_BATCHED replays one captured CUDA
+     * graph per batch (candidates, alignment, filter, MSA and correction with
+     * persistent work-stealing kernels) on up to two streams, with buffers
+     * sized once per call from the raw candidate counts of the range; the
+     * launch shapes below that are 0 are picked by an autotuner on the first
+     * batched call of the process for this kind of data. */
+    int32_t driver;                   /* CG_DRIVER_* */
+    int32_t align_blocks;             /* batched: persistent alignment blocks (128 threads); 0 = tuned */
+    int32_t msa_warps;                /* batched: anchors in flight per MSA block, 1..8; 0 = tuned */
+    int32_t streams;                  /* batched: batches in flight, 1 or 2; 0 = tuned */
+    int32_t reserved[4];
 } cg_options;
+
+#define CG_DRIVER_PLAIN 0
+#define CG_DRIVER_BATCHED 1
 
 typedef struct cg_ctx cg_ctx;
 
@@ -112,6 +127,13 @@ typedef struct cg_stats {
     uint64_t align_launches;          /* launches of the alignment/filter kernel */
     uint64_t msa_launches;            /* launches of the MSA/correction kernel */
     double seconds_filter;            /* device time in the mismatch-ratio filter kernel, accumulated */
+    /* batched driver: the shape in use and the time its tuning took */
+    int32_t batch_anchors;
+    int32_t align_blocks;
+    int32_t msa_warps;
+    int32_t streams;
+    double seconds_tune;
+    uint64_t graph_replays;           /* batches run as graph replays, accumulated */
 } cg_stats;
 
 /* Fill *o with the reference defaults. */

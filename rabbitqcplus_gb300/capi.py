@@ -20,6 +20,7 @@ CG_MAX_HASHMAPS = 48
 CG_PAIR_SE, CG_PAIR_PE = 0, 1
 CG_CORR_CLASSIC, CG_CORR_FOREST, CG_CORR_PRINT, CG_CORR_LEARNED = 0, 1, 2, 3
 CG_RESULT_CORRECTED, CG_RESULT_HQ = 1, 2
+CG_DRIVER_PLAIN, CG_DRIVER_BATCHED = 0, 1
 
 
 class CareOptions(ctypes.Structure):
@@ -42,7 +43,11 @@ class CareOptions(ctypes.Structure):
         ("threshold_anchor", ctypes.c_float),
         ("device", ctypes.c_int32),
         ("batch_anchors", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 8),
+        ("driver", ctypes.c_int32),
+        ("align_blocks", ctypes.c_int32),
+        ("msa_warps", ctypes.c_int32),
+        ("streams", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 4),
     ]
 
     @classmethod
@@ -80,7 +85,9 @@ class CgStats(ctypes.Structure):
         ("reserved", ctypes.c_int32), ("seconds_build", ctypes.c_double), ("seconds_correct", ctypes.c_double),
         ("seconds_candidates", ctypes.c_double), ("seconds_align", ctypes.c_double), ("seconds_msa", ctypes.c_double),
         ("kernel_launches", ctypes.c_uint64), ("align_launches", ctypes.c_uint64), ("msa_launches", ctypes.c_uint64),
-        ("seconds_filter", ctypes.c_double)]
+        ("seconds_filter", ctypes.c_double), ("batch_anchors", ctypes.c_int32), ("align_blocks", ctypes.c_int32),
+        ("msa_warps", ctypes.c_int32), ("streams", ctypes.c_int32), ("seconds_tune", ctypes.c_double),
+        ("graph_replays", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}

@@ -13,8 +13,11 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <chrono>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <new>
 #include <string>
 #include <vector>
@@ -65,6 +68,51 @@ struct MapTable {
     uint64_t nvalues = 0;
 };
 
+// What a captured batch graph depends on; a change means a new capture.
+struct GraphSig {
+    int count = 0;
+    unsigned long long stride = 0;
+    Shape shape{};
+    int tableRaw = 0, maxRows = 0;
+    std::vector<const void*> ptrs;
+    bool operator==(const GraphSig& o) const {
+        return count == o.count && stride == o.stride && shape.alignBlocks == o.shape.alignBlocks &&
+               shape.msaWarps == o.shape.msaWarps && shape.msaBlocks == o.shape.msaBlocks &&
+               tableRaw == o.tableRaw && maxRows == o.maxRows && ptrs == o.ptrs;
+    }
+};
+
+// One batch pipeline of the batched driver: its buffers, stream and graph.
+struct BatchSet {
+    DevBuf rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, flen, nfinal, uoff, scanTmp, cursor,
+        work;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t joined = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    GraphSig sig;
+    int kernels = 0;  // kernel nodes of one replay
+    void release() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        if (joined) cudaEventDestroy(joined);
+        joined = nullptr;
+        for (DevBuf* b : {&rawCount, &cand, &ncand, &paired, &aln, &fid, &fshift, &forient, &fweight, &flen, &nfinal,
+                          &uoff, &scanTmp, &cursor, &work})
+            b->release();
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
+
+// Batch size and launch shapes of the batched driver.
+struct Plan {
+    int batch = 0;
+    Shape shape{};
+    int streams = 0;
+};
+
+constexpr int kMaxSets = 2;
+
 }  // namespace
 
 struct cg_ctx {
@@ -90,11 +138,21 @@ struct cg_ctx {
     std::vector<MapTable> maps;
     TablesArg tables{};
     Params params{};
+    uint64_t paramsVersion = 0;
 
     // batch buffers
     DevBuf qrange, rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, flen, nfinal, flags, out, counters;
     DevBuf scanTmp, uoff;
     uint32_t* hPinned = nullptr;  // 2 words: total raw, max raw
+
+    // batched driver
+    BatchSet sets[kMaxSets];
+    DevBuf rawAll, rangeOff, rangeTmp, maxima, outRange, flagsRange, counterSave;
+    unsigned long long* hBatched = nullptr;  // pinned: [0..1] maxima, then two cursor words per set
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t evPro = nullptr, evStart = nullptr;
+    std::vector<cudaEvent_t> batchDone;
+    bool haveRawAll = false;
 
     // forest classifier (CG_CORR_FOREST)
     DevBuf forestNodes, treeOffsets;
@@ -143,6 +201,7 @@ uint64_t pow2_at_least(uint64_t x) {
 
 // Float constants in the reference's operand order (host, no contraction).
 void make_params(cg_ctx* c) {
+    c->paramsVersion++;  // captured batch graphs hold the parameters by value
     Params& p = c->params;
     const cg_options& o = c->o;
     p.k = c->k;
@@ -346,6 +405,7 @@ int build_tables(cg_ctx* c) {
 BatchArg batch_arg(cg_ctx* c, uint64_t first, int count) {
     BatchArg b{};
     b.first = first;
+    b.outFirst = first;
     b.count = count;
     b.sig = c->sig.as<unsigned long long>();
     b.qrange = c->qrange.as<uint2>();
@@ -447,6 +507,419 @@ int run_batch(cg_ctx* c, uint64_t first, int count, uint8_t* hFlags, char* hOut,
     return CG_OK;
 }
 
+// ---------------------------------------------------------------- batched driver
+//
+// One CUDA graph per batch pipeline, captured once per shape and replayed for
+// every batch: the candidate kernel (bucket lookup, gather, unique), the
+// candidate numbering scan, the persistent alignment kernel, the filter, the
+// persistent MSA/correction kernel and a one-thread kernel that advances the
+// pipeline's device cursor to its next batch.  Nothing in a replay depends on
+// a host value: the batch's first anchor is read from the cursor, its raw id
+// offsets come from one scan over the whole range (raw counts per read are
+// computed once, with the tables), and the buffers are sized before the
+// replays from the range's largest batch.  With two pipelines, batches
+// alternate between two streams so that one batch's memory-bound candidate
+// stage runs beside the other's compute-bound alignment.
+
+BatchArg set_arg(cg_ctx* c, BatchSet& s, int count) {
+    BatchArg b{};
+    b.count = count;
+    b.sig = c->sig.as<unsigned long long>();
+    b.rawCount = s.rawCount.as<uint32_t>();
+    b.cand = s.cand.as<uint32_t>();
+    b.ncand = s.ncand.as<uint32_t>();
+    b.paired = s.paired.as<uint8_t>();
+    b.aln = s.aln.as<uint2>();
+    b.fid = s.fid.as<uint32_t>();
+    b.fshift = s.fshift.as<int16_t>();
+    b.forient = s.forient.as<uint8_t>();
+    b.fweight = s.fweight.as<float>();
+    b.flen = s.flen.as<uint16_t>();
+    b.nfinal = s.nfinal.as<uint32_t>();
+    b.flags = c->flagsRange.as<uint8_t>();
+    b.out = c->outRange.as<char>();
+    b.outPitch = c->lmax;
+    b.counters = c->counters.as<unsigned long long>();
+    b.cursor = s.cursor.as<unsigned long long>();
+    b.rangeOff = c->rangeOff.as<unsigned long long>();
+    b.work = s.work.as<unsigned int>();
+    return b;
+}
+
+int ensure_set(cg_ctx* c, BatchSet& s, int count, uint64_t capRaw) {
+    if (!s.stream) CG_CUDA(c, cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
+    if (!s.joined) CG_CUDA(c, cudaEventCreateWithFlags(&s.joined, cudaEventDisableTiming));
+    const size_t n = (size_t)count;
+    CG_CUDA(c, s.rawCount.ensure((n + 2) * sizeof(uint32_t)));
+    CG_CUDA(c, s.ncand.ensure(n * sizeof(uint32_t)));
+    CG_CUDA(c, s.uoff.ensure((n + 1) * sizeof(uint32_t)));
+    CG_CUDA(c, s.nfinal.ensure(n * sizeof(uint32_t)));
+    CG_CUDA(c, s.scanTmp.ensure(scan_tmp_bytes(n + 1)));
+    CG_CUDA(c, s.cand.ensure(capRaw * sizeof(uint32_t)));
+    CG_CUDA(c, s.paired.ensure(capRaw));
+    CG_CUDA(c, s.aln.ensure(capRaw * sizeof(uint2)));
+    CG_CUDA(c, s.fid.ensure(capRaw * sizeof(uint32_t)));
+    CG_CUDA(c, s.fshift.ensure(capRaw * sizeof(int16_t)));
+    CG_CUDA(c, s.forient.ensure(capRaw));
+    CG_CUDA(c, s.fweight.ensure(capRaw * sizeof(float)));
+    CG_CUDA(c, s.flen.ensure(capRaw * sizeof(uint16_t)));
+    CG_CUDA(c, s.cursor.ensure(2 * sizeof(unsigned long long)));
+    CG_CUDA(c, s.work.ensure(2 * sizeof(unsigned int)));
+    return CG_OK;
+}
+
+// The kernels of one batch, enqueued on the set's stream (captured).
+cudaError_t enqueue_batch(cg_ctx* c, BatchSet& s, int count, unsigned long long stride, const Shape& sh,
+                          int tableRaw, int maxRows, int* kernels) {
+    const StoreArg st = store_arg(c);
+    const BatchArg b = set_arg(c, s, count);
+    uint32_t* uoff = s.uoff.as<uint32_t>();
+    int k = 0;
+    cudaError_t e = launch_gather_unique(st, c->tables, c->params, b, tableRaw, s.stream);
+    k++;
+    if (e == cudaSuccess && c->params.paired) {
+        e = launch_pair_flags(b, s.stream);
+        k++;
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(uoff, b.ncand, (size_t)count * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(uoff + count, 0, sizeof(uint32_t), s.stream);
+    if (e == cudaSuccess) {
+        e = scan_exclusive_u32(uoff, (size_t)count + 1, s.scanTmp.p, s.stream);
+        k += (int)scan_launches((uint64_t)count + 1);
+    }
+    if (e == cudaSuccess) {
+        e = launch_align_filter(st, c->params, b, uoff, 0, nullptr, s.stream, &sh);
+        k += st.wp - 1 <= 8 ? 2 : 1;
+    }
+    if (e == cudaSuccess) {
+        e = launch_msa_correct(st, c->params, b, maxRows, s.stream, &sh);
+        k++;
+    }
+    if (e == cudaSuccess) {
+        e = launch_batch_advance(s.cursor.as<unsigned long long>(), s.work.as<unsigned int>(), stride, s.stream);
+        k++;
+    }
+    *kernels = k;
+    return e;
+}
+
+int capture_set(cg_ctx* c, BatchSet& s, int count, unsigned long long stride, const Shape& sh, int tableRaw,
+                int maxRows) {
+    GraphSig g;
+    g.count = count;
+    g.stride = stride;
+    g.shape = sh;
+    g.tableRaw = tableRaw;
+    g.maxRows = maxRows;
+    for (const DevBuf* d : {&s.rawCount, &s.cand, &s.ncand, &s.paired, &s.aln, &s.fid, &s.fshift, &s.forient,
+                            &s.fweight, &s.flen, &s.nfinal, &s.uoff, &s.scanTmp, &s.cursor, &s.work, &c->outRange,
+                            &c->flagsRange, &c->rangeOff, &c->counters, &c->sig})
+        g.ptrs.push_back(d->p);
+    g.ptrs.push_back(reinterpret_cast<const void*>(static_cast<uintptr_t>(c->paramsVersion)));
+    if (s.exec && g == s.sig) return CG_OK;
+    if (s.exec) cudaGraphExecDestroy(s.exec);
+    s.exec = nullptr;
+    CG_CUDA(c, cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
+    int kernels = 0;
+    const cudaError_t e = enqueue_batch(c, s, count, stride, sh, tableRaw, maxRows, &kernels);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(s.stream, &graph);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return fail(c, CG_ERR_CUDA, "batch graph capture failed: %s",
+                    cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    const cudaError_t e3 = cudaGraphInstantiate(&s.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e3 != cudaSuccess) {
+        s.exec = nullptr;
+        return fail(c, CG_ERR_CUDA, "batch graph instantiation failed: %s", cudaGetErrorString(e3));
+    }
+    s.sig = g;
+    s.kernels = kernels;
+    return CG_OK;
+}
+
+int ensure_batched_state(cg_ctx* c) {
+    if (!c->hBatched) CG_CUDA(c, cudaMallocHost(&c->hBatched, (2 + 2 * kMaxSets) * sizeof(unsigned long long)));
+    if (!c->copyStream) CG_CUDA(c, cudaStreamCreateWithFlags(&c->copyStream, cudaStreamNonBlocking));
+    if (!c->evPro) CG_CUDA(c, cudaEventCreateWithFlags(&c->evPro, cudaEventDisableTiming));
+    if (!c->evStart) CG_CUDA(c, cudaEventCreate(&c->evStart));
+    if (!c->haveRawAll) {
+        CG_CUDA(c, c->rawAll.ensure(c->n * sizeof(uint32_t)));
+        CG_CUDA(c, launch_raw_count(store_arg(c), c->tables, c->params, c->sig.as<unsigned long long>(),
+                                    c->rawAll.as<uint32_t>(), c->stream));
+        c->stats.kernel_launches += 1;
+        c->haveRawAll = true;
+    }
+    return CG_OK;
+}
+
+// Enqueue the `nb` full batches of `pl.batch` anchors starting at `first`:
+// prologue on c->stream (one host round trip for the buffer sizes), then the
+// graph replays on the sets' streams.  Batch j's outputs land in rows
+// j * batch .. of c->outRange / c->flagsRange; if `done` is given, event
+// done[j] follows batch j.  The caller orders c->stream after the sets.
+int run_batched(cg_ctx* c, uint64_t first, uint64_t nb, const Plan& pl, const std::vector<cudaEvent_t>* done) {
+    const uint64_t B = (uint64_t)pl.batch;
+    const uint64_t num = nb * B;
+    CG_CUDA(c, c->rangeOff.ensure((num + 1) * sizeof(unsigned long long)));
+    CG_CUDA(c, c->rangeTmp.ensure(scan_tmp_bytes(num + 1)));
+    CG_CUDA(c, c->maxima.ensure(2 * sizeof(unsigned long long)));
+    CG_CUDA(c, launch_range_offsets(c->rawAll.as<uint32_t>() + first, num, B, c->rangeOff.as<unsigned long long>(),
+                                    c->rangeTmp.p, c->maxima.as<unsigned long long>(), c->stream));
+    c->stats.kernel_launches += 2 + scan_launches(num + 1);
+    CG_CUDA(c, cudaMemcpyAsync(c->hBatched, c->maxima.p, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                               c->stream));
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    const uint64_t capRaw = std::max<unsigned long long>(c->hBatched[0], 1);
+    const int maxRaw = (int)std::max<unsigned long long>(c->hBatched[1], 1);
+    if (capRaw > 0xffffffffull) return fail(c, CG_ERR_UNSUPPORTED, "batch of %llu raw ids exceeds 2^32",
+                                            (unsigned long long)capRaw);
+    CG_CUDA(c, c->outRange.ensure(num * c->lmax));
+    CG_CUDA(c, c->flagsRange.ensure(num));
+    const int S = pl.streams;
+    for (int k = 0; k < S; k++) {
+        BatchSet& s = c->sets[k];
+        int rc = ensure_set(c, s, pl.batch, capRaw);
+        if (rc != CG_OK) return rc;
+        rc = capture_set(c, s, pl.batch, B * S, pl.shape, maxRaw, maxRaw);
+        if (rc != CG_OK) return rc;
+        c->hBatched[2 + 2 * k] = first + (uint64_t)k * B;
+        c->hBatched[3 + 2 * k] = first;
+        CG_CUDA(c, cudaMemcpyAsync(s.cursor.p, c->hBatched + 2 + 2 * k, 2 * sizeof(unsigned long long),
+                                   cudaMemcpyHostToDevice, c->stream));
+        CG_CUDA(c, cudaMemsetAsync(s.work.p, 0, 2 * sizeof(unsigned int), c->stream));
+    }
+    CG_CUDA(c, cudaEventRecord(c->evPro, c->stream));
+    CG_CUDA(c, cudaEventRecord(c->evStart, c->stream));  // replays start (after any capture)
+    for (int k = 0; k < S; k++) CG_CUDA(c, cudaStreamWaitEvent(c->sets[k].stream, c->evPro, 0));
+    for (uint64_t j = 0; j < nb; j++) {
+        BatchSet& s = c->sets[j % S];
+        CG_CUDA(c, cudaGraphLaunch(s.exec, s.stream));
+        if (done) CG_CUDA(c, cudaEventRecord((*done)[j], s.stream));
+        c->stats.kernel_launches += (uint64_t)s.kernels;
+        c->stats.align_launches += 1;
+        c->stats.msa_launches += 1;
+        c->stats.graph_replays += 1;
+    }
+    return CG_OK;
+}
+
+// `to` waits for everything enqueued so far on the first S sets' streams
+int join_sets(cg_ctx* c, int S, cudaStream_t to) {
+    for (int k = 0; k < S; k++) {
+        CG_CUDA(c, cudaEventRecord(c->sets[k].joined, c->sets[k].stream));
+        CG_CUDA(c, cudaStreamWaitEvent(to, c->sets[k].joined, 0));
+    }
+    return CG_OK;
+}
+
+// ---- autotuner
+//
+// The batch size, the persistent grids and the number of pipelines change
+// only the speed (every candidate and anchor is computed the same way in any
+// shape), so they are picked by timing: coordinate descent over a few values
+// per dimension, each trial running the same sample of anchors (the first
+// anchors of the range) end to end through run_batched.  The counters are
+// saved before and restored after.  The result is kept for the process, keyed
+// by what decides the kernels' cost.
+
+using TuneKey = std::tuple<int, int, int, int, int, int, int, int>;
+std::mutex gTuneMu;
+std::map<TuneKey, Plan> gTuned;
+
+TuneKey tune_key(const cg_ctx* c) {
+    int lg = 0;
+    while ((1ull << lg) < c->n) lg++;
+    return TuneKey(c->device, c->lmax, c->params.useQuality, c->params.correctionType, c->params.paired, c->nmaps,
+                   c->maxValuesPerKey, lg);
+}
+
+int sm_count(cg_ctx* c) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) sms = 1;
+    return std::max(sms, 1);
+}
+
+// complete a shape: unset grids become the resident maximum
+Plan fill_plan(cg_ctx* c, Plan p) {
+    const StoreArg st = store_arg(c);
+    const int sms = sm_count(c);
+    if (p.batch <= 0) p.batch = 65536;
+    if (c->params.paired && (p.batch & 1)) p.batch++;
+    if (p.streams <= 0) p.streams = 2;
+    p.streams = std::min(p.streams, kMaxSets);
+    if (p.shape.msaWarps <= 0) p.shape.msaWarps = 4;
+    p.shape.msaWarps = std::min(std::max(p.shape.msaWarps, 1), 8);
+    if (p.shape.alignBlocks <= 0) p.shape.alignBlocks = sms * std::max(align_lane_occupancy(st), 1);
+    if (p.shape.msaBlocks <= 0) p.shape.msaBlocks = sms * std::max(msa_warp_occupancy(st, c->params, p.shape.msaWarps), 1);
+    return p;
+}
+
+// device seconds of one run of `pl` over the sample [first, first + sample)
+int time_plan(cg_ctx* c, uint64_t first, uint64_t sample, const Plan& pl, double* sec) {
+    const uint64_t nb = sample / (uint64_t)pl.batch;
+    if (nb == 0) {
+        *sec = 1e30;
+        return CG_OK;
+    }
+    int rc = run_batched(c, first, nb, pl, nullptr);
+    if (rc != CG_OK) return rc;
+    rc = join_sets(c, pl.streams, c->stream);
+    if (rc != CG_OK) return rc;
+    CG_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    CG_CUDA(c, cudaEventSynchronize(c->ev1));
+    float ms = 0;  // the replays only: the graph capture of a new shape is not timed
+    CG_CUDA(c, cudaEventElapsedTime(&ms, c->evStart, c->ev1));
+    *sec = ms / 1000.0 / (double)(nb * (uint64_t)pl.batch);  // per anchor
+    return CG_OK;
+}
+
+int plan_for(cg_ctx* c, uint64_t first, uint64_t num, Plan* out) {
+    Plan want;
+    want.batch = c->o.batch_anchors;
+    want.shape.alignBlocks = c->o.align_blocks;
+    want.shape.msaWarps = c->o.msa_warps;
+    want.streams = c->o.streams;
+    const bool fixed = want.batch > 0 && want.shape.alignBlocks > 0 && want.shape.msaWarps > 0 && want.streams > 0;
+    const uint64_t sample = std::min<uint64_t>(num, 262144);
+    if (fixed || sample < 2 * 32768) {
+        *out = fill_plan(c, want);
+        return CG_OK;
+    }
+    const TuneKey key = tune_key(c);
+    {
+        std::lock_guard<std::mutex> lk(gTuneMu);
+        auto it = gTuned.find(key);
+        if (it != gTuned.end()) {
+            Plan p = it->second;
+            if (want.batch > 0) p.batch = want.batch;
+            if (want.shape.alignBlocks > 0) p.shape.alignBlocks = want.shape.alignBlocks;
+            if (want.shape.msaWarps > 0) {
+                p.shape.msaWarps = want.shape.msaWarps;
+                p.shape.msaBlocks = 0;
+            }
+            if (want.streams > 0) p.streams = want.streams;
+            *out = fill_plan(c, p);
+            return CG_OK;
+        }
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    const size_t cbytes = kNumCounters * sizeof(unsigned long long);
+    CG_CUDA(c, c->counterSave.ensure(cbytes));
+    CG_CUDA(c, cudaMemcpyAsync(c->counterSave.p, c->counters.p, cbytes, cudaMemcpyDeviceToDevice, c->stream));
+    const StoreArg st = store_arg(c);
+    const int sms = sm_count(c);
+    const int occA = std::max(align_lane_occupancy(st), 1);
+    Plan best = fill_plan(c, want);
+    double bestSec = 0;
+    int rc = time_plan(c, first, sample, best, &bestSec);
+    auto trial = [&](Plan p) -> int {
+        p = fill_plan(c, p);
+        double sec = 0;
+        const int r = time_plan(c, first, sample, p, &sec);
+        if (r == CG_OK && sec < bestSec) {
+            best = p;
+            bestSec = sec;
+        }
+        return r;
+    };
+    if (rc == CG_OK && want.shape.msaWarps <= 0) {
+        for (int w : {1, 2, 8}) {
+            Plan p = best;
+            p.shape.msaWarps = w;
+            p.shape.msaBlocks = 0;
+            if ((rc = trial(p)) != CG_OK) break;
+        }
+    }
+    if (rc == CG_OK && want.shape.alignBlocks <= 0 && occA > 1) {
+        Plan p = best;
+        p.shape.alignBlocks = sms * std::max(occA / 2, 1);
+        rc = trial(p);
+    }
+    if (rc == CG_OK && want.streams <= 0) {
+        Plan p = best;
+        p.streams = 1;
+        rc = trial(p);
+    }
+    if (rc == CG_OK && want.batch <= 0) {
+        for (int bsz : {32768, 131072}) {
+            Plan p = best;
+            p.batch = bsz;
+            if ((rc = trial(p)) != CG_OK) break;
+        }
+    }
+    CG_CUDA(c, cudaMemcpyAsync(c->counters.p, c->counterSave.p, cbytes, cudaMemcpyDeviceToDevice, c->stream));
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (rc != CG_OK) return rc;
+    c->stats.seconds_tune += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    {
+        std::lock_guard<std::mutex> lk(gTuneMu);
+        gTuned[key] = best;
+    }
+    *out = best;
+    return CG_OK;
+}
+
+// cg_correct with the batched driver: full batches as graph replays, the
+// remainder (fewer anchors than a batch) through the plain driver on the
+// context's own stream, concurrently.
+int correct_batched(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* out_flags, char* out_seq, size_t out_pitch) {
+    int rc = ensure_batched_state(c);
+    if (rc != CG_OK) return rc;
+    Plan pl;
+    rc = plan_for(c, first, num, &pl);
+    if (rc != CG_OK) return rc;
+    c->stats.batch_anchors = pl.batch;
+    c->stats.align_blocks = pl.shape.alignBlocks;
+    c->stats.msa_warps = pl.shape.msaWarps;
+    c->stats.streams = pl.streams;
+    const uint64_t B = (uint64_t)pl.batch;
+    const uint64_t nb = num / B;
+    const uint64_t done = nb * B;
+    CG_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    if (nb > 0) {
+        while (c->batchDone.size() < nb) {
+            cudaEvent_t ev = nullptr;
+            CG_CUDA(c, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            c->batchDone.push_back(ev);
+        }
+        rc = run_batched(c, first, nb, pl, &c->batchDone);
+        if (rc != CG_OK) return rc;
+    }
+    if (done < num) {
+        // the remainder runs beside the replays; its own syncs wait only for it
+        int B2 = pl.batch;
+        for (uint64_t a = done; a < num; a += (uint64_t)B2) {
+            const int cnt = (int)std::min<uint64_t>((uint64_t)B2, num - a);
+            rc = run_batch(c, first + a, cnt, out_flags + a, out_seq + a * out_pitch, out_pitch);
+            if (rc != CG_OK) return rc;
+        }
+    }
+    // results of each batch to the host as soon as the batch is done
+    for (uint64_t j = 0; j < nb; j++) {
+        CG_CUDA(c, cudaStreamWaitEvent(c->copyStream, c->batchDone[j], 0));
+        CG_CUDA(c, cudaMemcpyAsync(out_flags + j * B, c->flagsRange.as<uint8_t>() + j * B, B, cudaMemcpyDeviceToHost,
+                                   c->copyStream));
+        CG_CUDA(c, cudaMemcpy2DAsync(out_seq + j * B * out_pitch, out_pitch, c->outRange.as<char>() + j * B * c->lmax,
+                                     (size_t)c->lmax, (size_t)c->lmax, B, cudaMemcpyDeviceToHost, c->copyStream));
+    }
+    rc = join_sets(c, pl.streams, c->stream);
+    if (rc != CG_OK) return rc;
+    CG_CUDA(c, cudaEventRecord(c->evPro, c->copyStream));
+    CG_CUDA(c, cudaStreamWaitEvent(c->stream, c->evPro, 0));
+    CG_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    CG_CUDA(c, cudaEventSynchronize(c->ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->stats.seconds_correct = ms / 1000.0;
+    c->stats.num_anchors_processed += num;
+    return CG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -477,6 +950,10 @@ int cg_create(const cg_options* o, cg_ctx** out) {
     if (o->pair_mode != CG_PAIR_SE && o->pair_mode != CG_PAIR_PE) return CG_ERR_INVALID_ARGUMENT;
     if (o->correct_candidates) return CG_ERR_UNSUPPORTED;
     if (o->correction_type != CG_CORR_CLASSIC && o->correction_type != CG_CORR_FOREST) return CG_ERR_UNSUPPORTED;
+    if (o->driver != CG_DRIVER_PLAIN && o->driver != CG_DRIVER_BATCHED) return CG_ERR_INVALID_ARGUMENT;
+    if (o->batch_anchors < 0 || o->align_blocks < 0 || o->msa_warps < 0 || o->msa_warps > 8 || o->streams < 0 ||
+        o->streams > kMaxSets)
+        return CG_ERR_INVALID_ARGUMENT;
     cg_ctx* c = new (std::nothrow) cg_ctx();
     if (!c) return CG_ERR_OUT_OF_MEMORY;
     c->o = *o;
@@ -510,6 +987,15 @@ void cg_destroy(cg_ctx* c) {
                       &c->ncand, &c->paired, &c->aln, &c->fid, &c->fshift, &c->forient, &c->fweight, &c->flen, &c->nfinal,
                       &c->flags, &c->out, &c->counters, &c->scanTmp, &c->uoff, &c->forestNodes, &c->treeOffsets})
         b->release();
+    for (BatchSet& bs : c->sets) bs.release();
+    for (DevBuf* b : {&c->rawAll, &c->rangeOff, &c->rangeTmp, &c->maxima, &c->outRange, &c->flagsRange,
+                      &c->counterSave})
+        b->release();
+    for (cudaEvent_t ev : c->batchDone) cudaEventDestroy(ev);
+    if (c->evPro) cudaEventDestroy(c->evPro);
+    if (c->evStart) cudaEventDestroy(c->evStart);
+    if (c->copyStream) cudaStreamDestroy(c->copyStream);
+    if (c->hBatched) cudaFreeHost(c->hBatched);
     if (c->hPinned) cudaFreeHost(c->hPinned);
     for (cudaEvent_t ev : {c->ev0, c->ev1, c->st0, c->st1, c->st1b, c->st2, c->st3})
         if (ev) cudaEventDestroy(ev);
@@ -555,6 +1041,11 @@ int cg_build_tables(cg_ctx* c) {
     rc = build_tables(c);
     if (rc != CG_OK) return rc;
     make_params(c);
+    if (c->o.driver == CG_DRIVER_BATCHED) {
+        // raw id counts per read: part of the index the batched driver reads
+        rc = ensure_batched_state(c);
+        if (rc != CG_OK) return rc;
+    }
     CG_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     CG_CUDA(c, cudaEventSynchronize(c->ev1));
     float ms = 0;
@@ -582,6 +1073,7 @@ int cg_correct(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* out_flags, char
     if (c->o.correction_type == CG_CORR_FOREST && c->numTrees == 0)
         return fail(c, CG_ERR_STATE, "forest correction requested but no forest loaded (cg_load_forest)");
     CG_CUDA(c, cudaSetDevice(c->device));
+    if (c->o.driver == CG_DRIVER_BATCHED) return correct_batched(c, first, num, out_flags, out_seq, out_pitch);
     int B = c->o.batch_anchors > 0 ? c->o.batch_anchors : 65536;
     if (c->params.paired && (B & 1)) B++;
     CG_CUDA(c, cudaEventRecord(c->ev0, c->stream));

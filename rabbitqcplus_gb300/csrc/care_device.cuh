@@ -43,6 +43,11 @@ __device__ __forceinline__ bool fgeq(float l, float r) { return (l > r) || feq(l
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
+// first anchor of the batch and anchor id of output row 0: kernel parameters,
+// or device memory in graph replays
+__device__ __forceinline__ uint64_t batch_first(const BatchArg& b) { return b.cursor ? b.cursor[0] : b.first; }
+__device__ __forceinline__ uint64_t out_first(const BatchArg& b) { return b.cursor ? b.cursor[1] : b.outFirst; }
+
 }  // namespace cg
 
 #endif

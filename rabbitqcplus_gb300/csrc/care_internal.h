@@ -155,6 +155,20 @@ struct BatchArg {
     char* out;              // [count][outPitch]
     int outPitch;
     unsigned long long* counters;  // device counters, see kCounter*
+    // Output rows: anchor first + a goes to row (first - outFirst) + a of out
+    // and flags.  The plain form sets outFirst = first.
+    unsigned long long outFirst;
+    // Batched form (graph replays), null in the plain form:
+    //   cursor[0] = the batch's first anchor id, cursor[1] = outFirst, both
+    //     read on the device so that one captured graph serves every batch
+    //   rangeOff = exclusive scan of the raw id counts of the anchors
+    //     outFirst, outFirst+1, ...; the candidate kernel takes the batch's raw
+    //     offsets from it instead of a count pass and a scan per batch
+    //   work[0], work[1] = the persistent alignment and MSA kernels'
+    //     work-stealing counters (zero at the start of a batch)
+    const unsigned long long* cursor;
+    const unsigned long long* rangeOff;
+    unsigned int* work;
 };
 enum {
     kCounterRaw = 0,
@@ -169,14 +183,44 @@ enum {
 };
 
 cudaError_t launch_query_count(StoreArg st, TablesArg tb, Params p, BatchArg b, cudaStream_t s);
+// with b.rangeOff set the kernel looks the buckets up itself and writes the
+// batch's raw offsets into b.rawCount (no query_count pass, no scan)
 cudaError_t launch_gather_unique(StoreArg st, TablesArg tb, Params p, BatchArg b, int maxRawPerAnchor,
                                  cudaStream_t s);
 cudaError_t launch_pair_flags(BatchArg b, cudaStream_t s);
+// raw id count of every read as an anchor, out[N]
+cudaError_t launch_raw_count(StoreArg st, TablesArg tb, Params p, const unsigned long long* sig, uint32_t* out,
+                             cudaStream_t s);
+// off[num+1] = exclusive scan of raw[0..num); maxima[0] = the largest raw
+// total of a batch of `batch` anchors, maxima[1] = the largest raw count of
+// one anchor; tmp needs scan_tmp_bytes(num + 1) bytes
+cudaError_t launch_range_offsets(const uint32_t* raw, uint64_t num, uint64_t batch, unsigned long long* off,
+                                 void* tmp, unsigned long long* maxima, cudaStream_t s);
+
+// Launch shapes of the batched form's persistent kernels (b.work set).
+struct Shape {
+    int alignBlocks;  // persistent alignment blocks of 128 threads
+    int msaWarps;     // warps (anchors in flight) per MSA block
+    int msaBlocks;    // persistent MSA blocks
+};
+
 // uoff: exclusive scan of the per-anchor candidate counts (count+1 entries),
-// totalUnique = uoff[count]; with uoff null the warp-per-anchor kernel runs
+// totalUnique = uoff[count] (unused with a shape: the persistent kernel reads
+// uoff[count]); with uoff null the warp-per-anchor kernel runs
 cudaError_t launch_align_filter(StoreArg st, Params p, BatchArg b, const uint32_t* uoff, uint32_t totalUnique,
-                                cudaEvent_t between, cudaStream_t s);  // `between` (optional) after the alignment
-cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, int maxRows, cudaStream_t s);
+                                cudaEvent_t between, cudaStream_t s,  // `between` (optional) after the alignment
+                                const Shape* shape = nullptr);
+cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, int maxRows, cudaStream_t s,
+                               const Shape* shape = nullptr);
+// resident 128-thread blocks per SM of the thread-per-candidate alignment
+// (0: it does not apply to this store's read length)
+int align_lane_occupancy(StoreArg st);
+// warp-per-anchor MSA blocks of `warps` warps that fit one SM (0: the warp
+// MSA does not apply to this store)
+int msa_warp_occupancy(StoreArg st, Params p, int warps);
+// cursor[0] += stride, work[0] = work[1] = 0 (the last node of a batch)
+cudaError_t launch_batch_advance(unsigned long long* cursor, unsigned int* work, unsigned long long stride,
+                                 cudaStream_t s);
 
 }  // namespace cg
 

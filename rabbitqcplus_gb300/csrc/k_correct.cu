@@ -360,7 +360,7 @@ __global__ void __launch_bounds__(kAlignWarps * 32, REGS ? (MAXW <= 5 ? 6 : 4) :
     if (a >= b.count) return;
     uint32_t* aS = smem + warp * 6 * wp;
     uint32_t* cS = aS + 2 * wp;
-    const uint64_t aid = b.first + (uint64_t)a;
+    const uint64_t aid = batch_first(b) + (uint64_t)a;
     const int La = st.len[aid];
     const uint32_t nc = b.ncand[a];
     const uint32_t base = rawOff[a];
@@ -510,33 +510,50 @@ __global__ void __launch_bounds__(kLaneThreads) align_lane_kernel(StoreArg st, P
                                                                   const uint32_t* __restrict__ rawOff,
                                                                   const uint32_t* __restrict__ uoff, uint32_t total) {
     __shared__ int16_t maxErrTab[CG_MAX_READ_LENGTH + 2];
+    __shared__ uint32_t chunk;
     for (int i = threadIdx.x; i <= st.lmax; i += blockDim.x)
         maxErrTab[i] = (int16_t)(int)__fmul_rn((float)i, p.maxErrorRate);
     __syncthreads();
-    const uint32_t t = blockIdx.x * kLaneThreads + threadIdx.x;
-    if (t >= total) return;
-    int lo = 0, hi = b.count;  // last anchor with uoff[a] <= t
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (uoff[mid] <= t) lo = mid;
-        else hi = mid;
+    const uint64_t first = batch_first(b);
+    // persistent form: blocks take 128-candidate chunks from a shared counter
+    // until the batch's candidates (uoff[count], on the device) are done
+    if (b.work) total = uoff[b.count];
+    uint32_t t0 = blockIdx.x * kLaneThreads;
+    while (true) {
+        if (b.work) {
+            if (threadIdx.x == 0) chunk = atomicAdd(&b.work[0], (uint32_t)kLaneThreads);
+            __syncthreads();
+            t0 = chunk;
+            __syncthreads();
+        }
+        if (t0 >= total) return;
+        const uint32_t t = t0 + threadIdx.x;
+        if (t < total) {
+            int lo = 0, hi = b.count;  // last anchor with uoff[a] <= t
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (uoff[mid] <= t) lo = mid;
+                else hi = mid;
+            }
+            const int a = lo;
+            const uint32_t j = t - uoff[a];
+            const uint32_t slot = rawOff[a] + j;
+            const uint64_t aid = first + (uint64_t)a;
+            const uint32_t id = b.cand[slot];
+            const int La = st.len[aid], Lc = st.len[id];
+            const int wp = st.wp;
+            uint32_t A[2][2 * MAXW], C[2][2 * MAXW];
+            load_planes<MAXW>(A, st.hilo + aid * 4 * (uint64_t)wp, wp);
+            const int minov = max(p.minOverlap, (int)__fmul_rn((float)La, p.minOverlapRatio));
+            load_planes<MAXW>(C, st.hilo + (uint64_t)id * 4 * wp, wp);
+            const AlnRes f = align_seq<MAXW>(A, C, La, Lc, minov, maxErrTab);
+            load_planes<MAXW>(C, st.hilo + (uint64_t)id * 4 * wp + 2 * wp, wp);
+            const AlnRes r = align_seq<MAXW>(A, C, La, Lc, minov, maxErrTab);
+            const int ori = choose_orientation(f, r, La, p.minOverlapRatio, p.minOverlap, p.orientMaxErrorRate);
+            b.aln[slot] = pack_aln(ori == 2 ? r : f, ori);
+        }
+        if (!b.work) return;
     }
-    const int a = lo;
-    const uint32_t j = t - uoff[a];
-    const uint32_t slot = rawOff[a] + j;
-    const uint64_t aid = b.first + (uint64_t)a;
-    const uint32_t id = b.cand[slot];
-    const int La = st.len[aid], Lc = st.len[id];
-    const int wp = st.wp;
-    uint32_t A[2][2 * MAXW], C[2][2 * MAXW];
-    load_planes<MAXW>(A, st.hilo + aid * 4 * (uint64_t)wp, wp);
-    const int minov = max(p.minOverlap, (int)__fmul_rn((float)La, p.minOverlapRatio));
-    load_planes<MAXW>(C, st.hilo + (uint64_t)id * 4 * wp, wp);
-    const AlnRes f = align_seq<MAXW>(A, C, La, Lc, minov, maxErrTab);
-    load_planes<MAXW>(C, st.hilo + (uint64_t)id * 4 * wp + 2 * wp, wp);
-    const AlnRes r = align_seq<MAXW>(A, C, La, Lc, minov, maxErrTab);
-    const int ori = choose_orientation(f, r, La, p.minOverlapRatio, p.minOverlap, p.orientMaxErrorRate);
-    b.aln[slot] = pack_aln(ori == 2 ? r : f, ori);
 }
 
 // one warp per anchor: the mismatch-ratio filter after align_lane_kernel
@@ -643,11 +660,13 @@ __global__ void __launch_bounds__(1024) msa_correct_kernel(StoreArg st, Params p
     const int a = blockIdx.x;
     const int tid = threadIdx.x;
     const int bd = blockDim.x;
-    const uint64_t aid = b.first + (uint64_t)a;
+    const uint64_t first = batch_first(b);
+    const uint64_t aid = first + (uint64_t)a;
+    const uint64_t oi = (first - out_first(b)) + (uint64_t)a;  // output row
     const uint32_t nf = b.nfinal[a];
-    char* out = b.out + (uint64_t)a * b.outPitch;
+    char* out = b.out + oi * b.outPitch;
     if (nf == 0) {
-        if (tid == 0) b.flags[a] = 0;
+        if (tid == 0) b.flags[oi] = 0;
         return;
     }
     const uint32_t base = rawOff[a];
@@ -866,7 +885,7 @@ __global__ void __launch_bounds__(1024) msa_correct_kernel(StoreArg st, Params p
             if (hq) atomicAdd(&b.counters[kCounterHQ], 1ull);
         }
         atomicAdd(&b.counters[kCounterMsaBuilds], (unsigned long long)builds);
-        b.flags[a] = corrected ? (uint8_t)(CG_RESULT_CORRECTED | (hq ? CG_RESULT_HQ : 0)) : (uint8_t)0;
+        b.flags[oi] = corrected ? (uint8_t)(CG_RESULT_CORRECTED | (hq ? CG_RESULT_HQ : 0)) : (uint8_t)0;
     }
     __syncthreads();
     if (p.correctionType == CG_CORR_FOREST) {
@@ -948,24 +967,23 @@ __device__ __forceinline__ int base_index(char c) { return c == 'A' ? 0 : c == '
 // row's positions, so every column receives its additions in the reference's
 // order.  Candidate metadata of 32 rows is held one row per lane and the rows'
 // 2-bit words are staged in shared memory per chunk.
-__global__ void __launch_bounds__(32) msa_warp_kernel(StoreArg st, Params p, BatchArg b,
-                                                      const uint32_t* __restrict__ rawOff, int lp) {
-    extern __shared__ __align__(16) unsigned char sm[];
+//
+// `sm` is the warp's own slice of shared memory (msa_warp_slice_bytes), `qw`
+// the block's quality weights.
+__device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params& p, const BatchArg& b,
+                                             const uint32_t* __restrict__ rawOff, int lp, int a, uint64_t first,
+                                             unsigned char* sm, const float* qw) {
     const int lane = (int)lane_id();
     float* w = reinterpret_cast<float*>(sm);                     // [4][lp]
     uint32_t* cnt = reinterpret_cast<uint32_t*>(w + 4 * lp);     // [4][lp]
     float* sup = reinterpret_cast<float*>(cnt + 4 * lp);         // [lp]
     uint32_t* stage = reinterpret_cast<uint32_t*>(sup + lp);     // [32][pitch]
-    float* qw = reinterpret_cast<float*>(stage + 32 * st.pitch); // [256] (quality scores only)
-    if (p.useQuality) {
-        for (int i = lane; i < 256; i += 32) qw[i] = p.qweight[i];
-    }
-    const int a = blockIdx.x;
-    const uint64_t aid = b.first + (uint64_t)a;
+    const uint64_t aid = first + (uint64_t)a;
+    const uint64_t oi = (first - out_first(b)) + (uint64_t)a;   // output row
     const uint32_t nf = b.nfinal[a];
-    char* out = b.out + (uint64_t)a * b.outPitch;
+    char* out = b.out + oi * b.outPitch;
     if (nf == 0) {
-        if (lane == 0) b.flags[a] = 0;
+        if (lane == 0) b.flags[oi] = 0;
         return;
     }
     const uint32_t base = rawOff[a];
@@ -1129,7 +1147,7 @@ __global__ void __launch_bounds__(32) msa_warp_kernel(StoreArg st, Params p, Bat
             if (hq) atomicAdd(&b.counters[kCounterHQ], 1ull);
         }
         atomicAdd(&b.counters[kCounterMsaBuilds], (unsigned long long)builds);
-        b.flags[a] = corrected ? (uint8_t)(CG_RESULT_CORRECTED | (hq ? CG_RESULT_HQ : 0)) : (uint8_t)0;
+        b.flags[oi] = corrected ? (uint8_t)(CG_RESULT_CORRECTED | (hq ? CG_RESULT_HQ : 0)) : (uint8_t)0;
     }
     if (!corrected) return;
     for (int c = lane; c < La; c += 32) {
@@ -1166,6 +1184,41 @@ __global__ void __launch_bounds__(32) msa_warp_kernel(StoreArg st, Params p, Bat
     }
 }
 
+// Bytes of shared memory one warp of msa_warp_kernel works in.
+__host__ __device__ inline size_t msa_warp_slice_bytes(int lp, int pitch) {
+    return (size_t)lp * (9 * sizeof(float)) + (size_t)32 * pitch * sizeof(uint32_t);
+}
+
+// `warps` warps per block, each on its own anchors.  Plain form: anchor
+// blockIdx.x * warps + warp.  Persistent form (b.work set): warps take the
+// next anchor from the counter b.work[1] until the batch is done.
+__global__ void __launch_bounds__(256, 4) msa_warp_kernel(StoreArg st, Params p, BatchArg b,
+                                                       const uint32_t* __restrict__ rawOff, int lp) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    float* qw = reinterpret_cast<float*>(sm);  // [256] (quality scores only)
+    const int warp = (int)(threadIdx.x >> 5), warps = (int)(blockDim.x >> 5);
+    const size_t qbytes = p.useQuality ? 256 * sizeof(float) : 0;
+    unsigned char* slice = sm + qbytes + (size_t)warp * msa_warp_slice_bytes(lp, st.pitch);
+    if (p.useQuality) {
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) qw[i] = p.qweight[i];
+        __syncthreads();
+    }
+    const uint64_t first = batch_first(b);
+    if (!b.work) {
+        const int a = blockIdx.x * warps + warp;
+        if (a < b.count) msa_warp_anchor(st, p, b, rawOff, lp, a, first, slice, qw);
+        return;
+    }
+    while (true) {
+        int a = 0;
+        if (lane_id() == 0) a = (int)atomicAdd(&b.work[1], 1u);
+        a = __shfl_sync(kFull, a, 0);
+        if (a >= b.count) return;
+        msa_warp_anchor(st, p, b, rawOff, lp, a, first, slice, qw);
+        __syncwarp();
+    }
+}
+
 template <int MAXW, bool REGS>
 cudaError_t launch_align_t(StoreArg st, Params p, BatchArg b, cudaStream_t s) {
     const size_t smem = (size_t)kAlignWarps * 6 * st.wp * sizeof(uint32_t) +
@@ -1178,11 +1231,14 @@ cudaError_t launch_align_t(StoreArg st, Params p, BatchArg b, cudaStream_t s) {
 }  // namespace
 
 cudaError_t launch_align_filter(StoreArg st, Params p, BatchArg b, const uint32_t* uoff, uint32_t totalUnique,
-                                cudaEvent_t between, cudaStream_t s) {
+                                cudaEvent_t between, cudaStream_t s, const Shape* shape) {
     const int need = st.wp - 1;  // words per plane that hold bases
     if (need <= 8 && uoff) {
-        if (totalUnique > 0) {
-            const unsigned blocks = (totalUnique + kLaneThreads - 1) / kLaneThreads;
+        const bool persistent = shape && b.work;
+        if (persistent || totalUnique > 0) {
+            // persistent: the blocks take 128-candidate chunks until uoff[count]
+            const unsigned blocks =
+                persistent ? (unsigned)shape->alignBlocks : (totalUnique + kLaneThreads - 1) / kLaneThreads;
             if (need <= 5)
                 align_lane_kernel<5><<<blocks, kLaneThreads, 0, s>>>(st, p, b, b.rawCount, uoff, totalUnique);
             else
@@ -1218,17 +1274,52 @@ size_t msa_smem_bytes(int maxCols, int bitsetWords, int storeWeights) {
            (size_t)maxCols * (7 * sizeof(int) + 1 + (storeWeights ? 4 * sizeof(float) : 0));
 }
 
-cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, int maxRows, cudaStream_t s) {
+namespace {
+
+size_t msa_warp_smem(StoreArg st, Params p, int warps) {
+    const int lp = (st.lmax + 31) / 32 * 32;
+    return (p.useQuality ? 256 * sizeof(float) : 0) + (size_t)warps * msa_warp_slice_bytes(lp, st.pitch);
+}
+
+cudaError_t msa_warp_prepare(size_t smem) {
+    if (smem <= 40 * 1024) return cudaSuccess;  // leaves room for the kernel's static shared memory
+    return cudaFuncSetAttribute(msa_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+}  // namespace
+
+int align_lane_occupancy(StoreArg st) {
+    const int need = st.wp - 1;
+    if (need > 8) return 0;
+    int blocks = 0;
+    const cudaError_t e = need <= 5
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, align_lane_kernel<5>, kLaneThreads, 0)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, align_lane_kernel<8>, kLaneThreads, 0);
+    return e == cudaSuccess ? blocks : 0;
+}
+
+int msa_warp_occupancy(StoreArg st, Params p, int warps) {
+    if (st.lmax > 256 || warps < 1 || warps > 8) return 0;
+    const size_t smem = msa_warp_smem(st, p, warps);
+    if (msa_warp_prepare(smem) != cudaSuccess) return 0;
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, msa_warp_kernel, warps * 32, smem) != cudaSuccess)
+        return 0;
+    return blocks;
+}
+
+cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, int maxRows, cudaStream_t s, const Shape* shape) {
     const int maxCols = 3 * st.lmax + 4;
     if (st.lmax <= 256) {
         const int lp = (st.lmax + 31) / 32 * 32;
-        const size_t smem = (size_t)lp * (9 * sizeof(float)) + (size_t)32 * st.pitch * sizeof(uint32_t) +
-                            (p.useQuality ? 256 * sizeof(float) : 0);
-        if (smem > 40 * 1024) {  // leaves room for the kernel's static shared memory
-            cudaError_t e = cudaFuncSetAttribute(msa_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-        }
-        msa_warp_kernel<<<b.count, 32, smem, s>>>(st, p, b, b.rawCount, lp);
+        const bool persistent = shape && b.work;
+        const int warps = persistent ? shape->msaWarps : 1;
+        const size_t smem = msa_warp_smem(st, p, warps);
+        cudaError_t e = msa_warp_prepare(smem);
+        if (e != cudaSuccess) return e;
+        const unsigned blocks = persistent ? (unsigned)shape->msaBlocks : (unsigned)b.count;
+        if (blocks == 0) return cudaSuccess;
+        msa_warp_kernel<<<blocks, warps * 32, smem, s>>>(st, p, b, b.rawCount, lp);
         return cudaGetLastError();
     }
     const int bitsetWords = (maxRows + 31) / 32 + 1;
@@ -1239,8 +1330,23 @@ cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, int maxRows, c
                                              (int)smem);
         if (e != cudaSuccess) return e;
     }
+    if (b.count == 0) return cudaSuccess;
     msa_correct_kernel<<<b.count, msa_threads(maxCols), smem, s>>>(st, p, b, b.rawCount, maxCols, bitsetWords,
                                                                     storeWeights);
+    return cudaGetLastError();
+}
+
+namespace {
+__global__ void batch_advance_kernel(unsigned long long* cursor, unsigned int* work, unsigned long long stride) {
+    cursor[0] += stride;
+    work[0] = 0;
+    work[1] = 0;
+}
+}  // namespace
+
+cudaError_t launch_batch_advance(unsigned long long* cursor, unsigned int* work, unsigned long long stride,
+                                 cudaStream_t s) {
+    batch_advance_kernel<<<1, 1, 0, s>>>(cursor, work, stride);
     return cudaGetLastError();
 }
 

@@ -143,7 +143,7 @@ __global__ void query_count_kernel(StoreArg st, TablesArg tb, Params p, BatchArg
     const int a = (int)(((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     if (a >= b.count) return;
     const uint32_t lane = lane_id();
-    const uint64_t aid = b.first + (uint64_t)a;
+    const uint64_t aid = batch_first(b) + (uint64_t)a;
     const bool active = st.len[aid] >= p.k && !(p.excludeAmbiguous && st.ambig[aid]);
     uint32_t total = 0;
     for (int m = (int)lane; m < tb.nmaps; m += 32) {
@@ -160,6 +160,47 @@ __global__ void query_count_kernel(StoreArg st, TablesArg tb, Params p, BatchArg
         b.rawCount[a] = total;
         atomicMax(&b.rawCount[b.count + 1], total);  // batch maximum
     }
+}
+
+// One warp per read: the raw id count of every read as an anchor (the sum
+// of query_count_kernel), for the batched form's range offsets.
+__global__ void raw_count_kernel(StoreArg st, TablesArg tb, Params p, const unsigned long long* __restrict__ sig,
+                                 uint32_t* __restrict__ out) {
+    const uint64_t aid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (aid >= st.n) return;
+    const uint32_t lane = lane_id();
+    const bool active = st.len[aid] >= p.k && !(p.excludeAmbiguous && st.ambig[aid]);
+    uint32_t total = 0;
+    if (active) {
+        for (int m = (int)lane; m < tb.nmaps; m += 32) {
+            const uint2 r = lookup(tb.slots[m], tb.mask[m], sig[(uint64_t)m * st.n + aid]);
+            if ((int)r.y <= tb.maxValuesPerKey) total += r.y;
+        }
+    }
+    total = __reduce_add_sync(0xffffffffu, total);
+    if (lane == 0) out[aid] = total;
+}
+
+// Raw counts of the anchors [first, first + num) widened to u64, with a zero
+// after the last, ready for the exclusive scan into range offsets; also the
+// largest count of one anchor.
+__global__ void range_widen_kernel(const uint32_t* __restrict__ raw, uint64_t num,
+                                   unsigned long long* __restrict__ off, unsigned long long* __restrict__ maxima) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;  // blockDim: a multiple of 32
+    const uint32_t v = i < num ? raw[i] : 0u;
+    if (i <= num) off[i] = v;
+    const uint32_t m = __reduce_max_sync(0xffffffffu, v);
+    if (lane_id() == 0 && m > 0) atomicMax(&maxima[1], (unsigned long long)m);
+}
+
+// After the scan: the largest raw total of one batch of `batch` anchors.
+__global__ void range_batch_max_kernel(const unsigned long long* __restrict__ off, uint64_t num, uint64_t batch,
+                                       unsigned long long* __restrict__ maxima) {
+    const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t b0 = j * batch;
+    if (b0 >= num) return;
+    const uint64_t b1 = b0 + batch < num ? b0 + batch : num;
+    atomicMax(&maxima[0], off[b1] - off[b0]);
 }
 
 constexpr int kGatherThreads = 128;
@@ -179,9 +220,24 @@ __global__ void __launch_bounds__(kGatherThreads) gather_unique_kernel(StoreArg 
     __shared__ uint32_t pre[kMaxMaps + 1];
     __shared__ uint32_t nUnique;
     const int a = blockIdx.x;
-    const uint64_t aid = b.first + (uint64_t)a;
-    const uint32_t raw = rawOff[a + 1] - rawOff[a];
+    const uint64_t first = batch_first(b);
+    const uint64_t aid = first + (uint64_t)a;
     const int tid = threadIdx.x;
+    uint32_t off, raw;
+    if (b.rangeOff) {
+        // batched form: raw offsets from the range scan, buckets looked up here
+        const uint64_t r0 = first - out_first(b);
+        const unsigned long long* ro = b.rangeOff + r0;
+        off = (uint32_t)(ro[a] - ro[0]);
+        raw = (uint32_t)(ro[a + 1] - ro[a]);
+        if (tid == 0) {
+            b.rawCount[a] = off;
+            if (a == b.count - 1) b.rawCount[b.count] = (uint32_t)(ro[b.count] - ro[0]);
+        }
+    } else {
+        off = rawOff[a];
+        raw = rawOff[a + 1] - rawOff[a];
+    }
     if (raw == 0) {
         if (tid == 0) b.ncand[a] = 0;
         return;
@@ -189,7 +245,16 @@ __global__ void __launch_bounds__(kGatherThreads) gather_unique_kernel(StoreArg 
     uint32_t T = 64;
     while (T < 2 * raw) T <<= 1;
     const uint32_t mask = T - 1;
-    if (tid < tb.nmaps) rng[tid] = b.qrange[(uint64_t)a * tb.nmaps + tid];
+    if (tid < tb.nmaps) {
+        if (b.rangeOff) {
+            // the rule of query_count_kernel; raw > 0 means the anchor is active
+            uint2 r = lookup(tb.slots[tid], tb.mask[tid], b.sig[(uint64_t)tid * st.n + aid]);
+            if ((int)r.y > tb.maxValuesPerKey) r = make_uint2(0, 0);
+            rng[tid] = r;
+        } else {
+            rng[tid] = b.qrange[(uint64_t)a * tb.nmaps + tid];
+        }
+    }
     for (uint32_t i = tid; i < T; i += kGatherThreads) table[i] = 0xffffffffu;
     if (tid == 0) nUnique = 0;
     __syncthreads();
@@ -241,7 +306,7 @@ __global__ void __launch_bounds__(kGatherThreads) gather_unique_kernel(StoreArg 
     }
     __syncthreads();
     const uint32_t U = nUnique;
-    uint32_t* out = b.cand + rawOff[a];
+    uint32_t* out = b.cand + off;
     if (U <= 512) {
         // rank of each id among the unique ids = its position in ascending order
         for (uint32_t i = tid; i < U; i += kGatherThreads) {
@@ -417,6 +482,27 @@ cudaError_t launch_gather_unique(StoreArg st, TablesArg tb, Params p, BatchArg b
         if (e != cudaSuccess) return e;
     }
     gather_unique_kernel<<<b.count, kGatherThreads, smem, s>>>(st, tb, p, b, b.rawCount, T);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_raw_count(StoreArg st, TablesArg tb, Params p, const unsigned long long* sig, uint32_t* out,
+                             cudaStream_t s) {
+    if (st.n == 0) return cudaSuccess;
+    raw_count_kernel<<<(unsigned)((st.n * 32 + 255) / 256), 256, 0, s>>>(st, tb, p, sig, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_range_offsets(const uint32_t* raw, uint64_t num, uint64_t batch, unsigned long long* off,
+                                 void* tmp, unsigned long long* maxima, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(maxima, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    range_widen_kernel<<<(unsigned)((num + 1 + 255) / 256), 256, 0, s>>>(raw, num, off, maxima);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = scan_exclusive_u64(off, num + 1, tmp, s);
+    if (e != cudaSuccess) return e;
+    const uint64_t batches = (num + batch - 1) / batch;
+    range_batch_max_kernel<<<(unsigned)((batches + 255) / 256), 256, 0, s>>>(off, num, batch, maxima);
     return cudaGetLastError();
 }
 
