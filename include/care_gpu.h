@@ -134,6 +134,10 @@ typedef struct cg_stats {
     int32_t streams;
     double seconds_tune;
     uint64_t graph_replays;           /* batches run as graph replays, accumulated */
+    /* learned decision (CG_CORR_LEARNED) */
+    uint64_t learned_columns;         /* columns scored by the classifier */
+    uint64_t learned_corrections;     /* columns it set to the consensus */
+    uint64_t learned_overflow;        /* columns beyond the per-batch records (fallback decision) */
 } cg_stats;
 
 /* Fill *o with the reference defaults. */
@@ -231,6 +235,87 @@ int cg_get_candidates(cg_ctx* ctx, uint64_t anchor, uint32_t* out, uint32_t capa
  * CG_ERR_INVALID_ARGUMENT (cg_get_candidates handles it).
  */
 int cg_get_candidates_noalloc(cg_ctx* ctx, uint64_t anchor, uint32_t* out, uint32_t capacity, uint32_t* count);
+
+/* ------------------------------------------------------------------------
+ * Learned correction classifier (correction_type CG_CORR_LEARNED).  No
+ * reference counterpart: it stands where the reference's forest/logistic-
+ * regression classifier stands (include/classification.hpp:51-157 and
+ * correctAnchorClf, include/corrector.hpp:1448-1472).  For every anchor whose
+ * MSA is not high quality, each column whose consensus differs from the
+ * anchor's base is scored by a 32-64-64-1 MLP (BF16 weights, FP32
+ * accumulation, sigmoid output) over 32 features of the column; the column
+ * takes the consensus base when the output reaches threshold_anchor (0.5),
+ * otherwise the classic rule's decision (the fallback) stands.
+ *
+ * Features of a column c of an anchor of length L (in order): the four base
+ * counts / coverage (A, C, G, T); the four base weights / column weight;
+ * coverage / estimated coverage; column weight / estimated coverage; support
+ * (consensus weight / column weight); anchor-base weight / column weight;
+ * anchor-base count / coverage; consensus count / coverage; the anchor base
+ * one-hot (4); the consensus base one-hot (4); c / L; min(c, L-1-c) / L; the
+ * anchor's average support; its minimum support; its minimum coverage /
+ * estimated coverage; its maximum coverage / estimated coverage; L / 256; the
+ * anchor's number of differing columns / L; rows in the MSA / estimated
+ * coverage; the quality weight of the anchor base (1 without quality scores).
+ *
+ * A serialized classifier is a 32-byte header {char magic[8] = "CGMLP001";
+ * uint32 features = 32, hidden1 = 64, hidden2 = 64, payload bytes; uint32
+ * reserved[2]} followed by the payload: w1 BF16[64][32], w2 BF16[64][64],
+ * w3 BF16[64], b1 FP32[64], b2 FP32[64], b3 FP32, zero padding to 16 bytes.
+ * ------------------------------------------------------------------------ */
+#define CG_CLASSIFIER_FEATURES 32
+
+/* Bytes of a serialized classifier. */
+size_t cg_classifier_size(void);
+
+/* Load the classifier a CG_CORR_LEARNED context uses. */
+int cg_load_classifier(cg_ctx* ctx, const void* data, size_t size);
+
+/*
+ * The columns the learned decision scores for anchors [first, first+num),
+ * without scoring them (needs correction_type CG_CORR_LEARNED, no classifier):
+ * features[count][32], the anchor id, the position in the anchor and the
+ * consensus base of each.  *count = number of columns; at most `capacity` are
+ * written (CG_ERR_INVALID_ARGUMENT if there are more).  The order of the
+ * columns is unspecified.
+ */
+int cg_get_columns(cg_ctx* ctx, uint64_t first, uint64_t num, float* features, uint64_t* anchors,
+                   uint16_t* positions, char* consensus, uint64_t capacity, uint64_t* count);
+
+typedef struct cg_train_options {
+    int32_t device;
+    int32_t epochs;                   /* passes over the training columns (4) */
+    int32_t batch_rows;               /* columns per minibatch, a multiple of 16 (4096) */
+    float learning_rate;              /* Adam step size (2e-3) */
+    uint32_t seed;                    /* initial weights and minibatch order */
+    int32_t reserved0;
+    const void* init_model;           /* start from this serialized classifier (or NULL) */
+    size_t init_model_size;
+    int32_t reserved[8];
+} cg_train_options;
+
+void cg_default_train_options(cg_train_options* o);
+
+/*
+ * Train the classifier on the device (minibatch Adam on the mean binary
+ * cross-entropy; forward and backward on the tensor cores).  features[n][32]
+ * and labels[n] (1 = the consensus base is the true base).  Writes the
+ * serialized classifier to model_out, the loss of every step to losses (up to
+ * loss_capacity values) and the number of steps to *steps.
+ */
+int cg_train_classifier(const cg_train_options* o, const float* features, const uint8_t* labels, uint64_t n,
+                        void* model_out, size_t model_capacity, float* losses, uint64_t loss_capacity,
+                        uint64_t* steps);
+
+/* Mean loss over the n columns and its gradient with respect to every
+ * parameter (6337 values in the payload's order: w1, w2, w3, b1, b2, b3),
+ * computed by the training kernels. */
+int cg_classifier_gradients(int device, const void* model, size_t model_size, const float* features,
+                            const uint8_t* labels, uint32_t n, float* grads, float* loss);
+
+/* Output logits of the classifier for n feature rows (the inference kernel). */
+int cg_classifier_logits(int device, const void* model, size_t model_size, const float* features, uint64_t n,
+                         float* logits);
 
 #ifdef __cplusplus
 }

@@ -38,7 +38,9 @@ GPU_CU_SOURCES = [
     "k_store.cu",
     "k_tables.cu",
     "k_correct.cu",
+    "k_learned.cu",
     "care_capi.cu",
+    "care_train.cu",
 ]
 GPU_CPP_SOURCES = [
     "host/seqio.cpp",

@@ -87,7 +87,8 @@ class CgStats(ctypes.Structure):
         ("kernel_launches", ctypes.c_uint64), ("align_launches", ctypes.c_uint64), ("msa_launches", ctypes.c_uint64),
         ("seconds_filter", ctypes.c_double), ("batch_anchors", ctypes.c_int32), ("align_blocks", ctypes.c_int32),
         ("msa_warps", ctypes.c_int32), ("streams", ctypes.c_int32), ("seconds_tune", ctypes.c_double),
-        ("graph_replays", ctypes.c_uint64)]
+        ("graph_replays", ctypes.c_uint64), ("learned_columns", ctypes.c_uint64),
+        ("learned_corrections", ctypes.c_uint64), ("learned_overflow", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
@@ -96,7 +97,34 @@ class CgStats(ctypes.Structure):
 # every symbol include/care_gpu.h declares
 EXPORTED = ["cg_default_options", "cg_create", "cg_destroy", "cg_last_error", "cg_append_reads",
             "cg_build_tables", "cg_correct", "cg_get_stats", "cg_get_read_info", "cg_get_signatures",
-            "cg_get_candidates", "cg_correct_files", "cg_load_forest", "cg_get_candidates_noalloc"]
+            "cg_get_candidates", "cg_correct_files", "cg_load_forest", "cg_get_candidates_noalloc",
+            "cg_classifier_size", "cg_load_classifier", "cg_get_columns", "cg_default_train_options",
+            "cg_train_classifier", "cg_classifier_gradients", "cg_classifier_logits"]
+CLASSIFIER_FEATURES = 32
+CLASSIFIER_PARAMS = 6337  # w1 64x32, w2 64x64, w3 64, b1 64, b2 64, b3
+
+
+class TrainOptions(ctypes.Structure):
+    """cg_train_options (include/care_gpu.h)."""
+    _fields_ = [
+        ("device", ctypes.c_int32),
+        ("epochs", ctypes.c_int32),
+        ("batch_rows", ctypes.c_int32),
+        ("learning_rate", ctypes.c_float),
+        ("seed", ctypes.c_uint32),
+        ("reserved0", ctypes.c_int32),
+        ("init_model", ctypes.c_void_p),
+        ("init_model_size", ctypes.c_size_t),
+        ("reserved", ctypes.c_int32 * 8),
+    ]
+
+    @classmethod
+    def defaults(cls, **kw) -> "TrainOptions":
+        o = cls()
+        gpu_lib().cg_default_train_options(ctypes.byref(o))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
 
 
 def gpu_lib() -> ctypes.CDLL:
@@ -120,8 +148,20 @@ def gpu_lib() -> ctypes.CDLL:
         L.cg_load_forest.argtypes = [P, P, ctypes.c_size_t, ctypes.c_uint32]
         L.cg_get_candidates_noalloc.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32,
                                                 ctypes.POINTER(ctypes.c_uint32)]
+        L.cg_classifier_size.restype = ctypes.c_size_t
+        L.cg_classifier_size.argtypes = []
+        L.cg_load_classifier.argtypes = [P, P, ctypes.c_size_t]
+        L.cg_get_columns.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, P, P, P, P, ctypes.c_uint64,
+                                     ctypes.POINTER(ctypes.c_uint64)]
+        L.cg_default_train_options.argtypes = [P]
+        L.cg_train_classifier.argtypes = [P, P, P, ctypes.c_uint64, P, ctypes.c_size_t, P, ctypes.c_uint64,
+                                          ctypes.POINTER(ctypes.c_uint64)]
+        L.cg_classifier_gradients.argtypes = [ctypes.c_int, P, ctypes.c_size_t, P, P, ctypes.c_uint32, P,
+                                              ctypes.POINTER(ctypes.c_float)]
+        L.cg_classifier_logits.argtypes = [ctypes.c_int, P, ctypes.c_size_t, P, ctypes.c_uint64, P]
         for f in EXPORTED:
-            if f not in ("cg_destroy", "cg_default_options", "cg_last_error"):
+            if f not in ("cg_destroy", "cg_default_options", "cg_last_error", "cg_classifier_size",
+                         "cg_default_train_options"):
                 getattr(L, f).restype = ctypes.c_int
         L._cg_typed = True
     return L
@@ -206,6 +246,29 @@ class CareGpu:
                     "cg_get_candidates_noalloc")
         return cnt.value
 
+    def load_classifier(self, data: bytes):
+        buf = np.frombuffer(data, np.uint8)
+        self._check(self._L.cg_load_classifier(self._h, buf.ctypes.data, len(buf)), "cg_load_classifier")
+
+    def columns(self, first: int = 0, count: int | None = None):
+        """Columns the learned decision scores: (features[k][32], anchor ids, positions, consensus bases)."""
+        n, _ = self.read_info()
+        if count is None:
+            count = n - first
+        k = ctypes.c_uint64()
+        rc = self._L.cg_get_columns(self._h, first, count, None, None, None, None, 0, ctypes.byref(k))
+        if rc not in (CG_OK, 1):
+            self._check(rc, "cg_get_columns")
+        cap = k.value
+        f = np.zeros((max(cap, 1), CLASSIFIER_FEATURES), np.float32)
+        a = np.zeros(max(cap, 1), np.uint64)
+        p = np.zeros(max(cap, 1), np.uint16)
+        c = np.zeros(max(cap, 1), np.uint8)
+        self._check(self._L.cg_get_columns(self._h, first, count, f.ctypes.data, a.ctypes.data, p.ctypes.data,
+                                           c.ctypes.data, cap, ctypes.byref(k)), "cg_get_columns")
+        m = k.value
+        return f[:m], a[:m], p[:m], c[:m]
+
     def close(self):
         if getattr(self, "_h", None):
             self._L.cg_destroy(self._h)
@@ -242,3 +305,58 @@ def correct_files(options: CareOptions, inputs: list[str], output_directory: str
     if rc != CG_OK:
         raise CareError(f"cg_correct_files: {CG_ERRORS.get(rc, rc)}")
     return n.value
+
+
+def _model_buf(model: bytes):
+    return np.frombuffer(model, np.uint8)
+
+
+def train_classifier(features: np.ndarray, labels: np.ndarray, options: TrainOptions | None = None,
+                     init_model: bytes | None = None):
+    """Train the learned classifier on the device; returns (serialized model, per-step losses)."""
+    L = gpu_lib()
+    o = options or TrainOptions.defaults()
+    f = np.ascontiguousarray(features, np.float32)
+    y = np.ascontiguousarray(labels, np.uint8)
+    assert f.ndim == 2 and f.shape[1] == CLASSIFIER_FEATURES and len(y) == len(f)
+    init = None
+    if init_model is not None:
+        init = _model_buf(init_model)
+        o.init_model = init.ctypes.data
+        o.init_model_size = len(init)
+    size = L.cg_classifier_size()
+    out = np.zeros(size, np.uint8)
+    steps_max = (len(f) // max(o.batch_rows, 1)) * o.epochs
+    losses = np.zeros(max(steps_max, 1), np.float32)
+    steps = ctypes.c_uint64()
+    rc = L.cg_train_classifier(ctypes.byref(o), f.ctypes.data, y.ctypes.data, len(f), out.ctypes.data, size,
+                               losses.ctypes.data, len(losses), ctypes.byref(steps))
+    if rc != CG_OK:
+        raise CareError(f"cg_train_classifier: {CG_ERRORS.get(rc, rc)}")
+    return out.tobytes(), losses[:steps.value].copy()
+
+
+def classifier_gradients(model: bytes, features: np.ndarray, labels: np.ndarray, device: int = 0):
+    """Mean loss and its gradient (6337 values) computed by the training kernels."""
+    L = gpu_lib()
+    m = _model_buf(model)
+    f = np.ascontiguousarray(features, np.float32)
+    y = np.ascontiguousarray(labels, np.uint8)
+    g = np.zeros(CLASSIFIER_PARAMS, np.float32)
+    loss = ctypes.c_float()
+    rc = L.cg_classifier_gradients(device, m.ctypes.data, len(m), f.ctypes.data, y.ctypes.data, len(f),
+                                   g.ctypes.data, ctypes.byref(loss))
+    if rc != CG_OK:
+        raise CareError(f"cg_classifier_gradients: {CG_ERRORS.get(rc, rc)}")
+    return loss.value, g
+
+
+def classifier_logits(model: bytes, features: np.ndarray, device: int = 0) -> np.ndarray:
+    L = gpu_lib()
+    m = _model_buf(model)
+    f = np.ascontiguousarray(features, np.float32)
+    out = np.zeros(len(f), np.float32)
+    rc = L.cg_classifier_logits(device, m.ctypes.data, len(m), f.ctypes.data, len(f), out.ctypes.data)
+    if rc != CG_OK:
+        raise CareError(f"cg_classifier_logits: {CG_ERRORS.get(rc, rc)}")
+    return out

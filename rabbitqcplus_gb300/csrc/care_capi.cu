@@ -24,6 +24,7 @@
 
 #include "care_gpu.h"
 #include "care_internal.h"
+#include "care_learned.h"
 
 using namespace cg;
 
@@ -85,7 +86,7 @@ struct GraphSig {
 // One batch pipeline of the batched driver: its buffers, stream and graph.
 struct BatchSet {
     DevBuf rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, flen, nfinal, uoff, scanTmp, cursor,
-        work;
+        work, colFeat, colMeta, colCount;
     cudaStream_t stream = nullptr;
     cudaEvent_t joined = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -97,7 +98,7 @@ struct BatchSet {
         if (joined) cudaEventDestroy(joined);
         joined = nullptr;
         for (DevBuf* b : {&rawCount, &cand, &ncand, &paired, &aln, &fid, &fshift, &forient, &fweight, &flen, &nfinal,
-                          &uoff, &scanTmp, &cursor, &work})
+                          &uoff, &scanTmp, &cursor, &work, &colFeat, &colMeta, &colCount})
             b->release();
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
@@ -153,6 +154,12 @@ struct cg_ctx {
     cudaEvent_t evPro = nullptr, evStart = nullptr;
     std::vector<cudaEvent_t> batchDone;
     bool haveRawAll = false;
+
+    // learned classifier (CG_CORR_LEARNED): model and the plain driver's column records
+    DevBuf mlp, colFeat, colMeta, colCount;
+    bool haveMlp = false;
+    bool collecting = false;  // cg_get_columns: record the columns, do not score them
+    float minLogit = 0.0f;    // logit of threshold_anchor
 
     // forest classifier (CG_CORR_FOREST)
     DevBuf forestNodes, treeOffsets;
@@ -427,6 +434,31 @@ BatchArg batch_arg(cg_ctx* c, uint64_t first, int count) {
     return b;
 }
 
+// Learned decision: column records per anchor of a batch (columns past this
+// keep the fallback decision and are counted as overflow)
+constexpr uint64_t kColumnsPerAnchor = 32;
+
+int ensure_columns(cg_ctx* c, DevBuf& feat, DevBuf& meta, DevBuf& cnt, int count) {
+    const size_t cap = (size_t)count * kColumnsPerAnchor;
+    CG_CUDA(c, feat.ensure(cap * kLearnedFeatures * sizeof(__nv_bfloat16)));
+    CG_CUDA(c, meta.ensure(cap * sizeof(uint2)));
+    CG_CUDA(c, cnt.ensure(sizeof(unsigned int)));
+    return CG_OK;
+}
+
+void set_columns(BatchArg& b, const DevBuf& feat, const DevBuf& meta, const DevBuf& cnt, int count) {
+    b.colFeat = feat.as<__nv_bfloat16>();
+    b.colMeta = meta.as<uint2>();
+    b.colCount = cnt.as<unsigned int>();
+    b.colCap = (unsigned int)((uint64_t)count * kColumnsPerAnchor);
+}
+
+int infer_blocks(cg_ctx* c) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) sms = 1;
+    return std::max(sms, 1) * 4;
+}
+
 // Candidate ids of a batch (query, scan, gather/unique).  On return
 // c->hPinned[0] holds the batch's raw id total.
 int run_candidates(cg_ctx* c, uint64_t first, int count) {
@@ -468,7 +500,16 @@ int run_batch(cg_ctx* c, uint64_t first, int count, uint8_t* hFlags, char* hOut,
     CG_CUDA(c, c->nfinal.ensure((size_t)count * sizeof(uint32_t)));
     CG_CUDA(c, c->flags.ensure((size_t)count));
     CG_CUDA(c, c->out.ensure((size_t)count * c->lmax));
+    const bool learned = c->params.correctionType == CG_CORR_LEARNED;
+    if (learned) {
+        rc = ensure_columns(c, c->colFeat, c->colMeta, c->colCount, count);
+        if (rc != CG_OK) return rc;
+    }
     BatchArg b = batch_arg(c, first, count);
+    if (learned) {
+        set_columns(b, c->colFeat, c->colMeta, c->colCount, count);
+        CG_CUDA(c, cudaMemsetAsync(b.colCount, 0, sizeof(unsigned int), c->stream));
+    }
     if (c->params.paired) {
         CG_CUDA(c, launch_pair_flags(b, c->stream));
         c->stats.kernel_launches += 1;
@@ -487,6 +528,12 @@ int run_batch(cg_ctx* c, uint64_t first, int count, uint8_t* hFlags, char* hOut,
     CG_CUDA(c, launch_align_filter(st, c->params, b, c->uoff.as<uint32_t>(), c->hPinned[2], c->st1b, c->stream));
     CG_CUDA(c, cudaEventRecord(c->st2, c->stream));
     CG_CUDA(c, launch_msa_correct(st, c->params, b, (int)std::max<uint32_t>(c->hPinned[1], 1), c->stream));
+    if (learned && !c->collecting) {
+        CG_CUDA(c, launch_mlp_infer(c->mlp.as<unsigned char>(), b.colFeat, b.colMeta, b.colCount, 0, b.colCap,
+                                    c->minLogit, b.out, b.outPitch, nullptr, b.counters, infer_blocks(c),
+                                    c->stream));
+        c->stats.kernel_launches += 1;
+    }
     CG_CUDA(c, cudaEventRecord(c->st3, c->stream));
     c->stats.kernel_launches += 3;
     c->stats.align_launches += 1;
@@ -543,6 +590,7 @@ BatchArg set_arg(cg_ctx* c, BatchSet& s, int count) {
     b.cursor = s.cursor.as<unsigned long long>();
     b.rangeOff = c->rangeOff.as<unsigned long long>();
     b.work = s.work.as<unsigned int>();
+    if (c->params.correctionType == CG_CORR_LEARNED) set_columns(b, s.colFeat, s.colMeta, s.colCount, count);
     return b;
 }
 
@@ -565,6 +613,7 @@ int ensure_set(cg_ctx* c, BatchSet& s, int count, uint64_t capRaw) {
     CG_CUDA(c, s.flen.ensure(capRaw * sizeof(uint16_t)));
     CG_CUDA(c, s.cursor.ensure(2 * sizeof(unsigned long long)));
     CG_CUDA(c, s.work.ensure(2 * sizeof(unsigned int)));
+    if (c->params.correctionType == CG_CORR_LEARNED) return ensure_columns(c, s.colFeat, s.colMeta, s.colCount, count);
     return CG_OK;
 }
 
@@ -575,7 +624,9 @@ cudaError_t enqueue_batch(cg_ctx* c, BatchSet& s, int count, unsigned long long 
     const BatchArg b = set_arg(c, s, count);
     uint32_t* uoff = s.uoff.as<uint32_t>();
     int k = 0;
-    cudaError_t e = launch_gather_unique(st, c->tables, c->params, b, tableRaw, s.stream);
+    const bool learned = c->params.correctionType == CG_CORR_LEARNED;
+    cudaError_t e = learned ? cudaMemsetAsync(b.colCount, 0, sizeof(unsigned int), s.stream) : cudaSuccess;
+    if (e == cudaSuccess) e = launch_gather_unique(st, c->tables, c->params, b, tableRaw, s.stream);
     k++;
     if (e == cudaSuccess && c->params.paired) {
         e = launch_pair_flags(b, s.stream);
@@ -596,6 +647,11 @@ cudaError_t enqueue_batch(cg_ctx* c, BatchSet& s, int count, unsigned long long 
         e = launch_msa_correct(st, c->params, b, maxRows, s.stream, &sh);
         k++;
     }
+    if (e == cudaSuccess && learned) {
+        e = launch_mlp_infer(c->mlp.as<unsigned char>(), b.colFeat, b.colMeta, b.colCount, 0, b.colCap, c->minLogit,
+                             b.out, b.outPitch, nullptr, b.counters, infer_blocks(c), s.stream);
+        k++;
+    }
     if (e == cudaSuccess) {
         e = launch_batch_advance(s.cursor.as<unsigned long long>(), s.work.as<unsigned int>(), stride, s.stream);
         k++;
@@ -613,7 +669,8 @@ int capture_set(cg_ctx* c, BatchSet& s, int count, unsigned long long stride, co
     g.tableRaw = tableRaw;
     g.maxRows = maxRows;
     for (const DevBuf* d : {&s.rawCount, &s.cand, &s.ncand, &s.paired, &s.aln, &s.fid, &s.fshift, &s.forient,
-                            &s.fweight, &s.flen, &s.nfinal, &s.uoff, &s.scanTmp, &s.cursor, &s.work, &c->outRange,
+                            &s.fweight, &s.flen, &s.nfinal, &s.uoff, &s.scanTmp, &s.cursor, &s.work, &s.colFeat,
+                            &s.colMeta, &s.colCount, &c->mlp, &c->outRange,
                             &c->flagsRange, &c->rangeOff, &c->counters, &c->sig})
         g.ptrs.push_back(d->p);
     g.ptrs.push_back(reinterpret_cast<const void*>(static_cast<uintptr_t>(c->paramsVersion)));
@@ -949,7 +1006,11 @@ int cg_create(const cg_options* o, cg_ctx** out) {
     if (!(o->estimated_coverage > 0.0f)) return CG_ERR_INVALID_ARGUMENT;
     if (o->pair_mode != CG_PAIR_SE && o->pair_mode != CG_PAIR_PE) return CG_ERR_INVALID_ARGUMENT;
     if (o->correct_candidates) return CG_ERR_UNSUPPORTED;
-    if (o->correction_type != CG_CORR_CLASSIC && o->correction_type != CG_CORR_FOREST) return CG_ERR_UNSUPPORTED;
+    if (o->correction_type != CG_CORR_CLASSIC && o->correction_type != CG_CORR_FOREST &&
+        o->correction_type != CG_CORR_LEARNED)
+        return CG_ERR_UNSUPPORTED;
+    if (o->correction_type == CG_CORR_LEARNED && !(o->threshold_anchor > 0.0f && o->threshold_anchor < 1.0f))
+        return CG_ERR_INVALID_ARGUMENT;
     if (o->driver != CG_DRIVER_PLAIN && o->driver != CG_DRIVER_BATCHED) return CG_ERR_INVALID_ARGUMENT;
     if (o->batch_anchors < 0 || o->align_blocks < 0 || o->msa_warps < 0 || o->msa_warps > 8 || o->streams < 0 ||
         o->streams > kMaxSets)
@@ -957,6 +1018,8 @@ int cg_create(const cg_options* o, cg_ctx** out) {
     cg_ctx* c = new (std::nothrow) cg_ctx();
     if (!c) return CG_ERR_OUT_OF_MEMORY;
     c->o = *o;
+    if (o->correction_type == CG_CORR_LEARNED)  // p >= t  <=>  logit >= log(t / (1 - t))
+        c->minLogit = (float)std::log((double)o->threshold_anchor / (1.0 - (double)o->threshold_anchor));
     c->device = o->device;
     auto bail = [&](cudaError_t e) {
         delete c;
@@ -989,7 +1052,7 @@ void cg_destroy(cg_ctx* c) {
         b->release();
     for (BatchSet& bs : c->sets) bs.release();
     for (DevBuf* b : {&c->rawAll, &c->rangeOff, &c->rangeTmp, &c->maxima, &c->outRange, &c->flagsRange,
-                      &c->counterSave})
+                      &c->counterSave, &c->mlp, &c->colFeat, &c->colMeta, &c->colCount})
         b->release();
     for (cudaEvent_t ev : c->batchDone) cudaEventDestroy(ev);
     if (c->evPro) cudaEventDestroy(c->evPro);
@@ -1072,6 +1135,10 @@ int cg_correct(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* out_flags, char
     if (c->params.paired && ((first | num) & 1)) return fail(c, CG_ERR_INVALID_ARGUMENT, "paired mode needs even ranges");
     if (c->o.correction_type == CG_CORR_FOREST && c->numTrees == 0)
         return fail(c, CG_ERR_STATE, "forest correction requested but no forest loaded (cg_load_forest)");
+    if (c->o.correction_type == CG_CORR_LEARNED && !c->haveMlp)
+        return fail(c, CG_ERR_STATE, "learned correction requested but no classifier loaded (cg_load_classifier)");
+    if (c->o.correction_type == CG_CORR_LEARNED && c->lmax > 256)
+        return fail(c, CG_ERR_UNSUPPORTED, "learned correction supports reads up to 256 bp (longest is %d)", c->lmax);
     CG_CUDA(c, cudaSetDevice(c->device));
     if (c->o.driver == CG_DRIVER_BATCHED) return correct_batched(c, first, num, out_flags, out_seq, out_pitch);
     int B = c->o.batch_anchors > 0 ? c->o.batch_anchors : 65536;
@@ -1107,6 +1174,9 @@ int cg_get_stats(const cg_ctx* c, cg_stats* out) {
     s.msa_builds = cnt[kCounterMsaBuilds];
     s.corrected_anchors = cnt[kCounterCorrected];
     s.hq_anchors = cnt[kCounterHQ];
+    s.learned_columns = cnt[kCounterColumns];
+    s.learned_corrections = cnt[kCounterLearnedTaken];
+    s.learned_overflow = cnt[kCounterColumnOverflow];
     *out = s;
     return CG_OK;
 }
@@ -1199,6 +1269,90 @@ int cg_load_forest(cg_ctx* c, const void* data, size_t size, uint32_t max_trees)
                           cudaMemcpyHostToDevice));
     c->numTrees = (int)nt;
     if (c->built) make_params(c);
+    return CG_OK;
+}
+
+int cg_load_classifier(cg_ctx* c, const void* data, size_t size) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    std::vector<unsigned char> blob;
+    if (!cg_parse_classifier(data, size, &blob))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "not a classifier of %zu bytes with a 32-64-64-1 layout",
+                    cg_classifier_size());
+    CG_CUDA(c, cudaSetDevice(c->device));
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    CG_CUDA(c, c->mlp.ensure(kMlpBytes));
+    CG_CUDA(c, cudaMemcpy(c->mlp.p, blob.data(), kMlpBytes, cudaMemcpyHostToDevice));
+    c->haveMlp = true;
+    return CG_OK;
+}
+
+int cg_get_columns(cg_ctx* c, uint64_t first, uint64_t num, float* features, uint64_t* anchors, uint16_t* positions,
+                   char* consensus, uint64_t capacity, uint64_t* count) {
+    if (!c || !count) return CG_ERR_INVALID_ARGUMENT;
+    *count = 0;
+    if (!c->built) return fail(c, CG_ERR_STATE, "cg_build_tables has not run");
+    if (c->o.correction_type != CG_CORR_LEARNED)
+        return fail(c, CG_ERR_STATE, "columns are recorded only with correction_type CG_CORR_LEARNED");
+    if (c->lmax > 256)
+        return fail(c, CG_ERR_UNSUPPORTED, "learned correction supports reads up to 256 bp (longest is %d)", c->lmax);
+    if (first + num > c->n || first + num < first) return fail(c, CG_ERR_INVALID_ARGUMENT, "anchor range out of bounds");
+    if (capacity && (!features || !anchors || !positions || !consensus))
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "output arrays missing");
+    if (c->params.paired && ((first | num) & 1)) return fail(c, CG_ERR_INVALID_ARGUMENT, "paired mode needs even ranges");
+    CG_CUDA(c, cudaSetDevice(c->device));
+    int B = c->o.batch_anchors > 0 ? c->o.batch_anchors : 65536;
+    if (c->params.paired && (B & 1)) B++;
+    std::vector<uint8_t> hFlags(B);
+    std::vector<char> hOut((size_t)B * std::max(c->lmax, 1));
+    std::vector<uint16_t> hf;
+    std::vector<uint2> hm;
+    uint64_t total = 0;
+    c->collecting = true;
+    int rc = CG_OK;
+    for (uint64_t a = 0; a < num && rc == CG_OK; a += (uint64_t)B) {
+        const int cnt = (int)std::min<uint64_t>((uint64_t)B, num - a);
+        rc = run_batch(c, first + a, cnt, hFlags.data(), hOut.data(), (size_t)std::max(c->lmax, 1));
+        if (rc != CG_OK) break;
+        unsigned int k = 0;
+        if (cudaMemcpy(&k, c->colCount.p, sizeof(k), cudaMemcpyDeviceToHost) != cudaSuccess) {
+            rc = fail(c, CG_ERR_CUDA, "reading the column count failed");
+            break;
+        }
+        const uint64_t cap = (uint64_t)cnt * kColumnsPerAnchor;
+        if (k > cap) {
+            rc = fail(c, CG_ERR_UNSUPPORTED, "batch at anchor %llu has %u columns, more than the %llu recorded",
+                      (unsigned long long)(first + a), k, (unsigned long long)cap);
+            break;
+        }
+        if (total + k > capacity) {
+            total += k;
+            continue;  // keep counting
+        }
+        hf.resize((size_t)k * kLearnedFeatures);
+        hm.resize(k);
+        if (k && (cudaMemcpy(hf.data(), c->colFeat.p, hf.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost) !=
+                      cudaSuccess ||
+                  cudaMemcpy(hm.data(), c->colMeta.p, k * sizeof(uint2), cudaMemcpyDeviceToHost) != cudaSuccess)) {
+            rc = fail(c, CG_ERR_CUDA, "reading the columns failed");
+            break;
+        }
+        for (uint64_t i = 0; i < k; i++) {
+            for (int f = 0; f < kLearnedFeatures; f++) {
+                const uint32_t u = (uint32_t)hf[i * kLearnedFeatures + f] << 16;
+                std::memcpy(&features[(total + i) * kLearnedFeatures + f], &u, 4);
+            }
+            anchors[total + i] = first + a + hm[i].x;
+            positions[total + i] = (uint16_t)(hm[i].y & 0xffffu);
+            consensus[total + i] = (char)((hm[i].y >> 16) & 0xffu);
+        }
+        total += k;
+    }
+    c->collecting = false;
+    if (rc != CG_OK) return rc;
+    *count = total;
+    if (total > capacity)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "%llu columns, capacity %llu", (unsigned long long)total,
+                    (unsigned long long)capacity);
     return CG_OK;
 }
 

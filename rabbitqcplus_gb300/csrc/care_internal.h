@@ -16,6 +16,7 @@
 #ifndef CARE_INTERNAL_H
 #define CARE_INTERNAL_H
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -27,6 +28,7 @@ constexpr uint64_t kEmptyKey = ~0ull;
 constexpr int kSegmentReads = 65536;  // N-replacement counter restarts per parser batch
 constexpr int kMaxMaps = CG_MAX_HASHMAPS;
 constexpr int kMaxBucket = 65535;     // BucketSize is uint16 in the reference
+constexpr int kLearnedFeatures = 32;  // features of one MSA column for the learned decision
 
 struct Slot {
     unsigned long long key;
@@ -169,6 +171,15 @@ struct BatchArg {
     const unsigned long long* cursor;
     const unsigned long long* rangeOff;
     unsigned int* work;
+    // Learned decision (correctionType CG_CORR_LEARNED): the MSA kernel records
+    // every column of a non-HQ anchor whose consensus differs from the anchor's
+    // base: 32 BF16 features (colFeat) and {output row, position | consensus
+    // base << 16} (colMeta), at index atomicAdd(colCount); indexes past colCap
+    // are not stored (those columns keep the fallback decision).
+    __nv_bfloat16* colFeat;
+    uint2* colMeta;
+    unsigned int* colCount;
+    unsigned int colCap;
 };
 enum {
     kCounterRaw = 0,
@@ -179,6 +190,9 @@ enum {
     kCounterCorrected,
     kCounterHQ,
     kCounterTimeouts,
+    kCounterColumns,         // learned decision: columns recorded for the classifier
+    kCounterColumnOverflow,  // columns beyond the buffer (decided by the fallback rule)
+    kCounterLearnedTaken,    // columns the classifier corrected
     kNumCounters
 };
 

@@ -1182,6 +1182,80 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
         }
         out[c] = r;
     }
+    if (p.correctionType != CG_CORR_LEARNED || hq) return;
+    // Learned decision: record every column whose consensus differs from the
+    // anchor's base, with its features; the classifier then replaces the
+    // decision written above (the fallback) where it is confident.
+    int nd = 0;
+    for (int c = lane; c < La; c += 32) nd += col_info(w, lp, c).cons != "ACGT"[get2bit(aenc, c)];
+    nd = __reduce_add_sync(kFull, nd);
+    const float ec = p.estimatedCoverage;
+    const float invLa = __fdiv_rn(1.0f, (float)La);
+    for (int c0 = 0; c0 < La; c0 += 32) {  // warp-uniform trip count
+        const int c = c0 + lane;
+        bool rec = false;
+        ColInfo ci{};
+        uint32_t ab = 0;
+        if (c < La) {
+            ab = get2bit(aenc, c);
+            ci = col_info(w, lp, c);
+            rec = ci.cons != "ACGT"[ab];
+        }
+        const unsigned m = __ballot_sync(kFull, rec);
+        if (!m) continue;
+        unsigned slot = 0;
+        if (lane == 0) slot = atomicAdd(b.colCount, (unsigned)__popc(m));
+        slot = __shfl_sync(kFull, slot, 0) + (unsigned)__popc(m & ((1u << lane) - 1u));
+        if (!rec || slot >= b.colCap) continue;
+        const int cb = base_index(ci.cons);
+        float n4[4], w4[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            n4[q] = (float)cnt[q * lp + c];
+            w4[q] = w[q * lp + c];
+        }
+        auto pick = [](const float (&v)[4], uint32_t i) {
+            return i == 0 ? v[0] : i == 1 ? v[1] : i == 2 ? v[2] : v[3];
+        };
+        const float cov = __fadd_rn(__fadd_rn(__fadd_rn(n4[0], n4[1]), n4[2]), n4[3]);
+        const float icov = __fdiv_rn(1.0f, cov);
+        const float icw = ci.colW > 0.0f ? __fdiv_rn(1.0f, ci.colW) : 0.0f;
+        float f[kLearnedFeatures];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            f[q] = __fmul_rn(n4[q], icov);                 // base counts / coverage
+            f[4 + q] = __fmul_rn(w4[q], icw);              // weights / column weight
+            f[14 + q] = (uint32_t)q == ab ? 1.0f : 0.0f;   // anchor base
+            f[18 + q] = q == cb ? 1.0f : 0.0f;             // consensus base
+        }
+        f[8] = __fdiv_rn(cov, ec);
+        f[9] = __fdiv_rn(ci.colW, ec);
+        f[10] = sup[c];
+        f[11] = __fmul_rn(pick(w4, ab), icw);
+        f[12] = __fmul_rn(pick(n4, ab), icov);
+        f[13] = __fmul_rn(pick(n4, (uint32_t)cb), icov);
+        f[22] = __fmul_rn((float)c, invLa);
+        f[23] = __fmul_rn((float)min(c, La - 1 - c), invLa);
+        f[24] = avg;
+        f[25] = mins;
+        f[26] = __fdiv_rn((float)minc, ec);
+        f[27] = __fdiv_rn((float)maxc, ec);
+        f[28] = __fmul_rn((float)La, 1.0f / 256.0f);
+        f[29] = __fmul_rn((float)nd, invLa);
+        f[30] = __fdiv_rn((float)nActive, ec);
+        f[31] = p.useQuality ? qw[aq[c]] : 1.0f;
+        uint32_t wd[kLearnedFeatures / 2];
+#pragma unroll
+        for (int k = 0; k < kLearnedFeatures / 2; k++) {
+            const __nv_bfloat162 v = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+            wd[k] = *reinterpret_cast<const uint32_t*>(&v);
+        }
+        uint4* dst = reinterpret_cast<uint4*>(b.colFeat + (uint64_t)slot * kLearnedFeatures);
+#pragma unroll
+        for (int k = 0; k < kLearnedFeatures / 8; k++)
+            dst[k] = make_uint4(wd[4 * k], wd[4 * k + 1], wd[4 * k + 2], wd[4 * k + 3]);
+        b.colMeta[slot] = make_uint2((uint32_t)oi, (uint32_t)c | ((uint32_t)(uint8_t)ci.cons << 16));
+    }
 }
 
 // Bytes of shared memory one warp of msa_warp_kernel works in.
