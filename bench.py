@@ -4,12 +4,23 @@ Workload (default): the 10 Mbp genome with 200 diverged repeat copies, 2M x
 150 bp single-end reads at 30x, substitution rate rising 0.2% -> 2% from 5'
 to 3' (seeded synthetic data of that shape; k=20, 48 maps, coverage 30).
 
-One step = correction of every anchor of that read set.
-  value  corrected reads/s with the read store and hash tables resident in HBM
-         (device time of cg_correct, CUDA events on the library's stream)
+One step = correction of every anchor of that read set.  Three forms are
+timed, each on its own context with the same reads:
+  plain            stage kernels per batch, classic decision (bit-exact with the
+                   reference)
+  batched          captured per-batch graphs with persistent work-stealing
+                   kernels, classic decision (bit-exact with plain)
+  batched_learned  the batched driver with the learned decision (the trained
+                   classifier shipped with the package)
+and for each the base-level TP/FP/FN against the generator's truth (also for
+the forest decision, untimed).
+  value  corrected reads/s of batched_learned with the read store and hash
+         tables resident in HBM (device time of cg_correct, CUDA events on the
+         library's streams); forms[...] has the same for every form
   e2e    the same metric through the public C ABI with host buffers: append the
          reads from host memory, build the store and the tables on the device,
-         correct every anchor and copy every result back to host memory
+         load the classifier, correct every anchor and copy every result back
+         to host memory
 The read store (0.5 GB) and tables (several GB) exceed the 129 MB L2, so no
 separate flush is needed between steps.
 
@@ -34,7 +45,7 @@ sys.path.insert(0, REPO)
 
 import numpy as np  # noqa: E402
 
-from rabbitqcplus_gb300 import capi, sim  # noqa: E402
+from rabbitqcplus_gb300 import capi, learned, sim  # noqa: E402
 
 METRIC = "corrected reads/s on 1 GB300: plain vs batched+learned, at equal TP/FP vs truth"
 UNIT = "reads/s"
@@ -51,14 +62,26 @@ class ClockSampler:
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
              "clocks_event_reasons.sw_power_cap"
 
-    def __init__(self, index: int):
+    def __init__(self, index: int, paused: bool = False):
         self.index = index
         self.samples = []
         self._stop = threading.Event()
+        self._active = threading.Event()
+        if not paused:
+            self._active.set()
         self._t = None
+
+    def pause(self):
+        self._active.clear()
+
+    def resume(self):
+        self._active.set()
 
     def _run(self):
         while not self._stop.is_set():
+            if not self._active.is_set():
+                self._stop.wait(0.05)
+                continue
             try:
                 out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
                                       "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
@@ -178,44 +201,122 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    # resident correction: build once, then time K full passes
-    g = capi.CareGpu(opts)
-    g.append_reads(reads.sequences, reads.offsets)
-    g.build_tables()
-    n, lmax = g.read_info()
-    flags = np.zeros(n, np.uint8)
-    out = np.zeros((n, lmax), np.uint8)
-    for _ in range(args.warmup):
-        g.correct(0, n, flags, out)
-    st0 = g.stats()
-    barrier()
-    with ClockSampler(local) as clk:
-        t0 = time.perf_counter()
-        dev_seconds = 0.0
-        for _ in range(args.steps):
+    model = open(learned.DEFAULT_MODEL, "rb").read()
+    forest = open(os.path.join(REPO, "tests", "golden", "forest_anchor.bin"), "rb").read()
+    n_total = reads.n
+
+    def form_options(form):
+        o = capi.CareOptions.defaults(opts.estimated_coverage, kmerlength=20, pair_mode=opts.pair_mode,
+                                      device=local)
+        if form in ("batched", "batched_learned"):
+            o.driver = capi.CG_DRIVER_BATCHED
+        if form == "batched_learned":
+            o.correction_type = capi.CG_CORR_LEARNED
+        if form == "forest":
+            o.correction_type = capi.CG_CORR_FOREST
+        return o
+
+    def make_ctx(form):
+        g = capi.CareGpu(form_options(form))
+        g.append_reads(reads.sequences, reads.offsets)
+        g.build_tables()
+        if form == "batched_learned":
+            g.load_classifier(model)
+        if form == "forest":
+            g.load_forest(forest)
+        return g
+
+    flags = np.zeros(n_total, np.uint8)
+    out = None
+
+    def run_form(form, steps, warmup, clk=None):
+        """Resident correction: build once, then time `steps` full passes (device time of cg_correct)."""
+        nonlocal out
+        g = make_ctx(form)
+        n, lmax = g.read_info()
+        if out is None:
+            out = np.zeros((n, lmax), np.uint8)
+        for _ in range(warmup):
             g.correct(0, n, flags, out)
-            dev_seconds += g.stats()["seconds_correct"]
+        st0 = g.stats()
+        barrier()
+        if clk:
+            clk.resume()
+        t0 = time.perf_counter()
+        dev = 0.0
+        for _ in range(steps):
+            g.correct(0, n, flags, out)
+            dev += g.stats()["seconds_correct"]
         barrier()
         wall = time.perf_counter() - t0
-    st1 = g.stats()
-    t = torch.tensor([dev_seconds], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    dev_seconds = float(t.item())
+        if clk:
+            clk.pause()
+        st1 = g.stats()
+        final = capi.apply_corrections(reads.sequences, reads.offsets, flags, out)
+        g.close()
+        t = torch.tensor([dev], dtype=torch.float64, device="cuda")
+        if dist is not None:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev = float(t.item())
+        return {"n": n, "lmax": lmax, "dev": dev, "wall": wall, "st0": st0, "st1": st1, "score": reads.score(final),
+                "flags": flags.copy() if form in ("plain", "batched") else None,
+                "out": out.copy() if form in ("plain", "batched") else None}
+
+    hbm_peak, peak_kind = measured_peaks()
+
+    def alg_bytes(r, steps):
+        # algorithmic bytes of one pass (per anchor: its 2-bit row 40 B, 48 keys 384 B, 48 lookup slots
+        # 768 B, 4 B per raw id, 44 B per unique candidate (row + length), the output record)
+        d = {k: (r["st1"][k] - r["st0"][k]) / steps for k in ("raw_candidate_ids", "unique_candidates")}
+        pitch = (r["lmax"] + 15) // 16
+        return r["n"] * (4 * pitch + 48 * 8 + 48 * 16 + r["lmax"] + 1) + 4 * d["raw_candidate_ids"] + \
+            (4 * pitch + 4) * d["unique_candidates"]
+
+    def summary(r, steps):
+        sec = r["dev"] / steps
+        b = alg_bytes(r, steps)
+        return {"value": world * r["n"] / sec, "unit": UNIT, "ms_per_step": sec * 1e3,
+                "alg_gbs": b / sec / 1e9, "hbm_frac": b / sec / 1e9 / hbm_peak,
+                "tp": r["score"]["tp"], "fp": r["score"]["fp"], "fn": r["score"]["fn"],
+                "gpu_launches_per_step": (r["st1"]["kernel_launches"] - r["st0"]["kernel_launches"]) / steps}
+
+    clk = ClockSampler(local, paused=True)
+    with clk:
+        plain = run_form("plain", args.steps, args.warmup, clk)
+        bat = run_form("batched", args.steps, args.warmup, clk)
+        bl = run_form("batched_learned", args.steps, args.warmup, clk)
+    forest_run = run_form("forest", 1, 0)
+    st0, st1 = bl["st0"], bl["st1"]
+    n = bl["n"]
+    lmax = bl["lmax"]
+    dev_seconds = bl["dev"]
     value = world * n * args.steps / dev_seconds
     launches = st1["kernel_launches"] - st0["kernel_launches"]
-    final = capi.apply_corrections(reads.sequences, reads.offsets, flags, out)
-    score = reads.score(final)
+    same = bool(np.array_equal(plain["flags"], bat["flags"]))
+    if same:
+        idx = np.nonzero(plain["flags"] & capi.CG_RESULT_CORRECTED)[0]
+        lens = reads.lengths[idx]
+        po, bo = plain["out"][idx], bat["out"][idx]
+        mask = np.arange(lmax)[None, :] < lens[:, None]
+        same = bool(np.array_equal(np.where(mask, po, 0), np.where(mask, bo, 0)))
+    forms = {"plain": summary(plain, args.steps), "batched": summary(bat, args.steps),
+             "batched_learned": summary(bl, args.steps),
+             "forest": {"tp": forest_run["score"]["tp"], "fp": forest_run["score"]["fp"],
+                        "fn": forest_run["score"]["fn"], "driver": "plain", "timed": False},
+             "batched_bit_exact_with_plain": same,
+             "batched_shape": {k: bl["st1"][k] for k in ("batch_anchors", "align_blocks", "msa_warps", "streams",
+                                                       "seconds_tune")}}
 
-    # roofline of the dominant kernel (by device time in the timed region)
-    stages = {"align": st1["seconds_align"] - st0["seconds_align"],
-              "filter": st1["seconds_filter"] - st0["seconds_filter"],
-              "msa": st1["seconds_msa"] - st0["seconds_msa"],
-              "candidates": st1["seconds_candidates"] - st0["seconds_candidates"]}
+    # roofline of the dominant kernel, from the plain form's per-stage CUDA events (the
+    # batched form runs the same kernels inside graph replays, where they are not timed apart)
+    p0, p1 = plain["st0"], plain["st1"]
+    stages = {"align": p1["seconds_align"] - p0["seconds_align"],
+              "filter": p1["seconds_filter"] - p0["seconds_filter"],
+              "msa": p1["seconds_msa"] - p0["seconds_msa"],
+              "candidates": p1["seconds_candidates"] - p0["seconds_candidates"]}
     dom = max(stages, key=stages.get)
-    hbm_peak, peak_kind = measured_peaks()
-    per_step_cands = (st1["unique_candidates"] - st0["unique_candidates"]) / args.steps
-    per_step_msa = (st1["msa_candidates"] - st0["msa_candidates"]) / args.steps
+    per_step_cands = (p1["unique_candidates"] - p0["unique_candidates"]) / args.steps
+    per_step_msa = (p1["msa_candidates"] - p0["msa_candidates"]) / args.steps
     wp = (lmax + 31) // 32 + 1
     pitch = (lmax + 15) // 16
     if dom == "align":
@@ -223,33 +324,36 @@ def main():
         # reverse-complement hi/lo planes (4*wp words), the packed result (8 B);
         # per anchor: its forward planes (2*wp words), length and two offsets (10 B)
         bytes_step = per_step_cands * (4 + 2 + 16 * wp + 8) + n * (8 * wp + 10)
-        launches_k = (st1["align_launches"] - st0["align_launches"])
+        launches_k = (p1["align_launches"] - p0["align_launches"])
+        kname = "align_lane_kernel"
     elif dom == "msa":
         # msa_warp_kernel, per kept candidate: its record (id, shift, length, orientation,
         # weight = 13 B) and its 2-bit row; per anchor: its 2-bit row, length, the
         # corrected bases and flags written
         bytes_step = per_step_msa * (13 + 4 * pitch) + n * (4 * pitch + 2 + lmax + 1)
-        launches_k = (st1["msa_launches"] - st0["msa_launches"])
+        launches_k = (p1["msa_launches"] - p0["msa_launches"])
+        kname = "msa_warp_kernel"
     else:
-        bytes_step = (st1["raw_candidate_ids"] - st0["raw_candidate_ids"]) / args.steps * 4 + n * 48 * 24
-        launches_k = max(st1["align_launches"] - st0["align_launches"], 1)
+        bytes_step = (p1["raw_candidate_ids"] - p0["raw_candidate_ids"]) / args.steps * 4 + n * 48 * 24
+        launches_k = max(p1["align_launches"] - p0["align_launches"], 1)
+        kname = "gather_unique_kernel"
     dur = stages[dom] / max(launches_k, 1)
     bytes_launch = bytes_step * args.steps / max(launches_k, 1)
     achieved = bytes_launch / dur / 1e9
-    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
-            "avg_launch_ms": dur * 1e3, "stage_seconds_per_step": {k: v / args.steps for k, v in stages.items()}}
+    roof = {"bound": "hbm", "kernel": kname, "form": "plain", "achieved": achieved, "peak": hbm_peak,
+            "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+            "avg_launch_ms": dur * 1e3,
+            "stage_seconds_per_step": {k: v / args.steps for k, v in stages.items()},
+            "note": "compute-bound (integer pipe); the fraction is of the HBM roofline"}
 
-    # e2e through the C ABI with host buffers
+    # e2e through the C ABI with host buffers (batched + learned)
     e2e = None
     if not args.no_e2e:
         e2e_times = []
         for i in range(1 + 1):
             barrier()
             t0 = time.perf_counter()
-            g2 = capi.CareGpu(opts)
-            g2.append_reads(reads.sequences, reads.offsets)
-            g2.build_tables()
+            g2 = make_ctx("batched_learned")
             g2.correct(0, n, flags, out)
             g2.close()
             barrier()
@@ -260,9 +364,11 @@ def main():
         if dist is not None:
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         e2e = {"value": world * n / float(tt.item()), "unit": UNIT,
-               "h2d_bytes_per_step": int(reads.sequences.nbytes + reads.offsets.nbytes),
+               "h2d_bytes_per_step": int(reads.sequences.nbytes + reads.offsets.nbytes + len(model)),
                "d2h_bytes_per_step": int(flags.nbytes + out.nbytes),
-               "includes": "append from host, device read-store + table build, correction, results to host"}
+               "form": "batched_learned",
+               "includes": "append from host, device read-store + table build, classifier load, correction, "
+                           "results to host (launch shapes tuned in the warm-up)"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -272,15 +378,15 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_seconds / args.steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-                "config": config, "form": "plain", "e2e": e2e, "gpu_launches": int(launches),
-                "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
-                "wall_seconds_timed": wall, "build_seconds": st1["seconds_build"],
-                "score": score, "stats": {k: st1[k] for k in ("raw_candidate_ids", "unique_candidates",
-                                                              "aligned_candidates", "msa_candidates",
-                                                              "corrected_anchors", "hq_anchors", "table_keys",
-                                                              "table_values")}}
+                "config": config, "form": "batched_learned", "forms": forms, "e2e": e2e,
+                "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "wall_seconds_timed": bl["wall"], "build_seconds": st1["seconds_build"],
+                "score": bl["score"], "stats": {k: st1[k] for k in ("raw_candidate_ids", "unique_candidates",
+                                                                    "aligned_candidates", "msa_candidates",
+                                                                    "corrected_anchors", "hq_anchors", "table_keys",
+                                                                    "table_values", "learned_columns",
+                                                                    "learned_corrections")}}
         print(json.dumps(line), flush=True)
-    g.close()
     if dist is not None:
         dist.destroy_process_group()
 
