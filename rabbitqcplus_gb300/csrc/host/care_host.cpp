@@ -34,6 +34,7 @@ cg_options toCgOptions(const ProgramOptions& o) {
     c.correction_type = (int)o.correctionType;
     c.threshold_anchor = o.thresholdAnchor;
     c.device = o.deviceIds.empty() ? 0 : o.deviceIds[0];
+    c.driver = o.gpuBatched ? CG_DRIVER_BATCHED : CG_DRIVER_PLAIN;
     return c;
 }
 
@@ -119,6 +120,12 @@ Corrected runCorrection(const ProgramOptions& o) {
         if (!is) throw std::runtime_error("Loading classifier file failed! " + o.mlForestfileAnchor);
         std::vector<char> bytes((std::istreambuf_iterator<char>(is)), std::istreambuf_iterator<char>());
         check(ctx.c, cg_load_forest(ctx.c, bytes.data(), bytes.size(), o.maxForestTreesAnchor), "cg_load_forest");
+    }
+    if (o.correctionType == CorrectionType::Learned) {
+        std::ifstream is(o.mlClassifierFileAnchor, std::ios::binary);
+        if (!is) throw std::runtime_error("Loading classifier file failed! " + o.mlClassifierFileAnchor);
+        std::vector<char> bytes((std::istreambuf_iterator<char>(is)), std::istreambuf_iterator<char>());
+        check(ctx.c, cg_load_classifier(ctx.c, bytes.data(), bytes.size()), "cg_load_classifier");
     }
     uint64_t nr = 0;
     int32_t lmax = 0;
@@ -288,6 +295,7 @@ extern "C" int cg_correct_files(const cg_options* options, const char* const* in
     o.correctionType = (CorrectionType)options->correction_type;
     o.thresholdAnchor = options->threshold_anchor;
     o.deviceIds = {options->device};
+    o.gpuBatched = options->driver == CG_DRIVER_BATCHED;
     o.outputCorrectionQualityLabels = quality_labels != 0;
     o.gzoutput = gz_output != 0;
     o.outputdirectory = output_directory;

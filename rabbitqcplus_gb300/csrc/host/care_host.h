@@ -53,6 +53,11 @@ struct ProgramOptions {
     float pairedFilterThreshold = 0.06f;
     uint32_t maxForestTreesAnchor = 0xffffffffu;
     std::string mlForestfileAnchor = "";
+    // No reference counterpart: the GPU driver (both give identical results;
+    // the batched one replays captured per-batch graphs, see cg_options.driver)
+    // and the serialized classifier of CorrectionType::Learned.
+    bool gpuBatched = true;
+    std::string mlClassifierFileAnchor = "";
     bool showProgress = false;
     int threads = 1;
     std::vector<int> deviceIds;
