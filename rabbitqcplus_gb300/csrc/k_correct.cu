@@ -500,6 +500,90 @@ __device__ __forceinline__ void load_planes(uint32_t (&R)[2][2 * MAXW], const ui
     }
 }
 
+// The reference's sequential scan of one direction (as seq_scan), with a fast
+// rejection for shifts whose overlap has at least 64 bases: the mismatches of
+// the overlap's first two words (complete, so no masks) against the error
+// limit of the scan's longest overlap, tabMax.  The reference's limit at any
+// shift is min(maxErrTab[ov], ...) <= tabMax and the two words' mismatches
+// are part of the shift's, so a shift rejected here is rejected there too.
+// Every other shift takes the reference's step.  The direction ends where the
+// reference's does: at the first shift whose limit is <= 0, i.e. whose
+// overlap is at most max((tb - best) / 2, ovPos - 1), ovPos being the
+// smallest overlap with a positive table entry; that point moves only when
+// the best score improves.  Overlap at shift sl: min(X - sl, Y), X = La and
+// Y = Lc for the right scan (anchor shifted), the other way round for the left.
+template <int MAXW, bool LEFT>
+__device__ __forceinline__ void seq_scan_fast(const uint32_t (&S)[2][2 * MAXW], const uint32_t (&O)[2][2 * MAXW],
+                                              int La, int Lc, int n, int tb, const int16_t* __restrict__ maxErrTab,
+                                              int tabMax, int ovPos, int& bestScore, int& bestShift) {
+    const int X = LEFT ? Lc : La, Y = LEFT ? La : Lc;
+    const int slFast = Y >= 64 ? X - 64 : -1;  // overlap >= 64 up to here
+    auto stopAt = [&](int best) {
+        const int dv = max((tb - best) >> 1, ovPos - 1);  // done once the overlap is <= dv
+        return Y <= dv ? 0 : X - dv;
+    };
+    const int slStart = LEFT ? 1 : 0;
+    int stop = min(LEFT ? n + 1 : n, stopAt(bestScore));
+#pragma unroll
+    for (int W = 0; W < MAXW; W++) {
+        if (32 * W >= stop) break;
+        for (int bb = max(slStart - 32 * W, 0); bb < 32; bb++) {
+            const int sl = 32 * W + bb;
+            if (sl >= stop) break;
+            const uint32_t h0 = __funnelshift_l(S[0][W + 1], S[0][W], bb), l0 = __funnelshift_l(S[1][W + 1], S[1][W], bb);
+            const uint32_t h1 = __funnelshift_l(S[0][W + 2], S[0][W + 1], bb),
+                           l1 = __funnelshift_l(S[1][W + 2], S[1][W + 1], bb);
+            const uint32_t d0 = (h0 ^ O[0][0]) | (l0 ^ O[1][0]), d1 = (h1 ^ O[0][1]) | (l1 ^ O[1][1]);
+            if (sl <= slFast && __popc(d0) + __popc(d1) >= tabMax) continue;
+            // the reference's step
+            const int ov = min(X - sl, Y);
+            const int maxErr = min((int)maxErrTab[ov], bestScore - tb + 2 * ov);  // > 0 before `stop`
+            const int parts = (ov + 31) >> 5;
+            const uint32_t last = 0xffffffffu << ((parts << 5) - ov);
+            const uint32_t mask0 = parts > 1 ? 0xffffffffu : last;
+            const uint32_t mask1 = parts > 2 ? 0xffffffffu : (parts == 2 ? last : 0u);
+            int m = __popc(d0 & mask0) + __popc(d1 & mask1);
+            if (m < maxErr && parts > 2) {
+#pragma unroll
+                for (int i = 2; i < MAXW; i++) {
+                    if (i >= parts || m >= maxErr) break;
+                    const uint32_t mask = i == parts - 1 ? last : 0xffffffffu;
+                    const uint32_t hi = __funnelshift_l(S[0][W + i + 1], S[0][W + i], bb);
+                    const uint32_t lo = __funnelshift_l(S[1][W + i + 1], S[1][W + i], bb);
+                    m += __popc(((hi ^ O[0][i]) | (lo ^ O[1][i])) & mask);
+                }
+            }
+            if (m < maxErr) {
+                const int score = m + tb - 2 * ov;
+                if (score < bestScore) {
+                    bestScore = score;
+                    bestShift = LEFT ? -sl : sl;
+                    stop = min(stop, stopAt(bestScore));
+                }
+            }
+        }
+    }
+}
+
+template <int MAXW>
+__device__ __forceinline__ AlnRes align_seq_fast(const uint32_t (&A)[2][2 * MAXW], const uint32_t (&C)[2][2 * MAXW],
+                                                 int La, int Lc, int minov, const int16_t* maxErrTab, int ovPos) {
+    const int tb = La + Lc;
+    const int tabMax = maxErrTab[min(La, Lc)];
+    int bestScore = tb, bestShift = -Lc;
+    seq_scan_fast<MAXW, false>(A, C, La, Lc, La - minov + 1, tb, maxErrTab, tabMax, ovPos, bestScore, bestShift);
+    seq_scan_fast<MAXW, true>(C, A, La, Lc, Lc - minov, tb, maxErrTab, tabMax, ovPos, bestScore, bestShift);
+    AlnRes r;
+    r.valid = bestShift != -Lc;
+    const int cb = max(-bestShift, 0);
+    const int ce = min(Lc, La - bestShift);
+    r.overlap = ce - cb;
+    r.score = bestScore;
+    r.shift = bestShift;
+    r.nOps = bestScore - tb + 2 * r.overlap;
+    return r;
+}
+
 constexpr int kLaneThreads = 128;
 
 // One thread per (anchor, candidate): both orientations with the reference's
@@ -511,8 +595,13 @@ __global__ void __launch_bounds__(kLaneThreads) align_lane_kernel(StoreArg st, P
                                                                   const uint32_t* __restrict__ uoff, uint32_t total) {
     __shared__ int16_t maxErrTab[CG_MAX_READ_LENGTH + 2];
     __shared__ uint32_t chunk;
+    __shared__ int ovPos;  // smallest overlap whose error limit is positive
+    if (threadIdx.x == 0) ovPos = st.lmax + 1;
     for (int i = threadIdx.x; i <= st.lmax; i += blockDim.x)
         maxErrTab[i] = (int16_t)(int)__fmul_rn((float)i, p.maxErrorRate);
+    __syncthreads();
+    for (int i = threadIdx.x; i <= st.lmax; i += blockDim.x)  // the table is non-decreasing
+        if (maxErrTab[i] > 0 && (i == 0 || maxErrTab[i - 1] <= 0)) ovPos = i;
     __syncthreads();
     const uint64_t first = batch_first(b);
     // persistent form: blocks take 128-candidate chunks from a shared counter
@@ -546,9 +635,9 @@ __global__ void __launch_bounds__(kLaneThreads) align_lane_kernel(StoreArg st, P
             load_planes<MAXW>(A, st.hilo + aid * 4 * (uint64_t)wp, wp);
             const int minov = max(p.minOverlap, (int)__fmul_rn((float)La, p.minOverlapRatio));
             load_planes<MAXW>(C, st.hilo + (uint64_t)id * 4 * wp, wp);
-            const AlnRes f = align_seq<MAXW>(A, C, La, Lc, minov, maxErrTab);
+            const AlnRes f = align_seq_fast<MAXW>(A, C, La, Lc, minov, maxErrTab, ovPos);
             load_planes<MAXW>(C, st.hilo + (uint64_t)id * 4 * wp + 2 * wp, wp);
-            const AlnRes r = align_seq<MAXW>(A, C, La, Lc, minov, maxErrTab);
+            const AlnRes r = align_seq_fast<MAXW>(A, C, La, Lc, minov, maxErrTab, ovPos);
             const int ori = choose_orientation(f, r, La, p.minOverlapRatio, p.minOverlap, p.orientMaxErrorRate);
             b.aln[slot] = pack_aln(ori == 2 ? r : f, ori);
         }
