@@ -131,10 +131,11 @@ def cpu_arm(reads, opts, sample_anchors: int, threads: int, seconds_target: floa
     n = min(sample_anchors, reads.n)
     first = reads.n // 3
     t0 = time.perf_counter()
-    orc.correct(first, min(2000, n), threads=threads)
+    probe = min(2000, n, reads.n - first)
+    orc.correct(first, probe, threads=threads)
     dt = time.perf_counter() - t0
-    rate = min(2000, n) / max(dt, 1e-6)
-    n = int(min(n, max(2000, rate * seconds_target)))
+    rate = probe / max(dt, 1e-6)
+    n = int(min(n, max(2000, rate * seconds_target), reads.n - first))
     t0 = time.perf_counter()
     orc.correct(first, n, threads=threads)
     dt = time.perf_counter() - t0

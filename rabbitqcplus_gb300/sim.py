@@ -144,13 +144,30 @@ class SimReads:
         self.n = int(lib.cgsim_num_reads(self._h))
         tot = int(lib.cgsim_total_bases(self._h))
         self.offsets = np.ctypeslib.as_array(lib.cgsim_offsets(self._h), shape=(self.n + 1,)).copy()
-        self.sequences = np.ctypeslib.as_array(
-            ctypes.cast(lib.cgsim_sequences(self._h), ctypes.POINTER(ctypes.c_uint8)), shape=(tot,)).copy()
-        self.qualities = np.ctypeslib.as_array(
-            ctypes.cast(lib.cgsim_qualities(self._h), ctypes.POINTER(ctypes.c_uint8)), shape=(tot,)).copy()
-        self.truth = np.ctypeslib.as_array(
-            ctypes.cast(lib.cgsim_truth(self._h), ctypes.POINTER(ctypes.c_uint8)), shape=(tot,)).copy()
+        self._tot = tot
+        self.sequences = self._copy(lib.cgsim_sequences)
+        self._qualities = None
+        self._truth = None
         self.lengths = np.diff(self.offsets).astype(np.int32)
+
+    def _copy(self, getter) -> np.ndarray:
+        if not self._h:
+            raise ValueError("the generated read set was closed")
+        return np.ctypeslib.as_array(ctypes.cast(getter(self._h), ctypes.POINTER(ctypes.c_uint8)),
+                                     shape=(self._tot,)).copy()
+
+    # copied on first use: a 100M-read set holds 15 GB per array
+    @property
+    def qualities(self) -> np.ndarray:
+        if self._qualities is None:
+            self._qualities = self._copy(self._lib.cgsim_qualities)
+        return self._qualities
+
+    @property
+    def truth(self) -> np.ndarray:
+        if self._truth is None:
+            self._truth = self._copy(self._lib.cgsim_truth)
+        return self._truth
 
     def write_fastq(self, path1: str, path2: str | None = None) -> None:
         rc = self._lib.cgsim_write_fastq(self._h, path1.encode(), path2.encode() if path2 else None)
