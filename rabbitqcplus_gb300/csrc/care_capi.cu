@@ -86,7 +86,7 @@ struct GraphSig {
 // One batch pipeline of the batched driver: its buffers, stream and graph.
 struct BatchSet {
     DevBuf rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, flen, nfinal, uoff, scanTmp, cursor,
-        work, colFeat, colMeta, colCount;
+        work, colFeat, colMeta, colCount, order, orderScratch;
     cudaStream_t stream = nullptr;
     cudaEvent_t joined = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -98,7 +98,7 @@ struct BatchSet {
         if (joined) cudaEventDestroy(joined);
         joined = nullptr;
         for (DevBuf* b : {&rawCount, &cand, &ncand, &paired, &aln, &fid, &fshift, &forient, &fweight, &flen, &nfinal,
-                          &uoff, &scanTmp, &cursor, &work, &colFeat, &colMeta, &colCount})
+                          &uoff, &scanTmp, &cursor, &work, &colFeat, &colMeta, &colCount, &order, &orderScratch})
             b->release();
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
@@ -143,7 +143,7 @@ struct cg_ctx {
 
     // batch buffers
     DevBuf qrange, rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, flen, nfinal, flags, out, counters;
-    DevBuf scanTmp, uoff;
+    DevBuf scanTmp, uoff, msaOrder, orderScratch;
     uint32_t* hPinned = nullptr;  // 2 words: total raw, max raw
 
     // batched driver
@@ -527,6 +527,11 @@ int run_batch(cg_ctx* c, uint64_t first, int count, uint8_t* hFlags, char* hOut,
     CG_CUDA(c, cudaEventRecord(c->st1, c->stream));
     CG_CUDA(c, launch_align_filter(st, c->params, b, c->uoff.as<uint32_t>(), c->hPinned[2], c->st1b, c->stream));
     CG_CUDA(c, cudaEventRecord(c->st2, c->stream));
+    CG_CUDA(c, c->msaOrder.ensure((size_t)count * sizeof(uint32_t)));
+    CG_CUDA(c, c->orderScratch.ensure(32 * sizeof(unsigned int)));
+    CG_CUDA(c, launch_msa_order(b, c->orderScratch.as<unsigned int>(), c->msaOrder.as<uint32_t>(), c->stream));
+    c->stats.kernel_launches += 2;
+    b.order = c->msaOrder.as<uint32_t>();
     CG_CUDA(c, launch_msa_correct(st, c->params, b, (int)std::max<uint32_t>(c->hPinned[1], 1), c->stream));
     if (learned && !c->collecting) {
         CG_CUDA(c, launch_mlp_infer(c->mlp.as<unsigned char>(), b.colFeat, b.colMeta, b.colCount, 0, b.colCap,
@@ -591,6 +596,7 @@ BatchArg set_arg(cg_ctx* c, BatchSet& s, int count) {
     b.rangeOff = c->rangeOff.as<unsigned long long>();
     b.work = s.work.as<unsigned int>();
     if (c->params.correctionType == CG_CORR_LEARNED) set_columns(b, s.colFeat, s.colMeta, s.colCount, count);
+    b.order = s.order.as<uint32_t>();
     return b;
 }
 
@@ -613,6 +619,8 @@ int ensure_set(cg_ctx* c, BatchSet& s, int count, uint64_t capRaw) {
     CG_CUDA(c, s.flen.ensure(capRaw * sizeof(uint16_t)));
     CG_CUDA(c, s.cursor.ensure(2 * sizeof(unsigned long long)));
     CG_CUDA(c, s.work.ensure(2 * sizeof(unsigned int)));
+    CG_CUDA(c, s.order.ensure(n * sizeof(uint32_t)));
+    CG_CUDA(c, s.orderScratch.ensure(32 * sizeof(unsigned int)));
     if (c->params.correctionType == CG_CORR_LEARNED) return ensure_columns(c, s.colFeat, s.colMeta, s.colCount, count);
     return CG_OK;
 }
@@ -644,6 +652,10 @@ cudaError_t enqueue_batch(cg_ctx* c, BatchSet& s, int count, unsigned long long 
         k += st.wp - 1 <= 8 ? 2 : 1;
     }
     if (e == cudaSuccess) {
+        e = launch_msa_order(b, s.orderScratch.as<unsigned int>(), s.order.as<uint32_t>(), s.stream);
+        k += 2;
+    }
+    if (e == cudaSuccess) {
         e = launch_msa_correct(st, c->params, b, maxRows, s.stream, &sh);
         k++;
     }
@@ -670,7 +682,7 @@ int capture_set(cg_ctx* c, BatchSet& s, int count, unsigned long long stride, co
     g.maxRows = maxRows;
     for (const DevBuf* d : {&s.rawCount, &s.cand, &s.ncand, &s.paired, &s.aln, &s.fid, &s.fshift, &s.forient,
                             &s.fweight, &s.flen, &s.nfinal, &s.uoff, &s.scanTmp, &s.cursor, &s.work, &s.colFeat,
-                            &s.colMeta, &s.colCount, &c->mlp, &c->outRange,
+                            &s.colMeta, &s.colCount, &s.order, &s.orderScratch, &c->mlp, &c->outRange,
                             &c->flagsRange, &c->rangeOff, &c->counters, &c->sig})
         g.ptrs.push_back(d->p);
     g.ptrs.push_back(reinterpret_cast<const void*>(static_cast<uintptr_t>(c->paramsVersion)));
@@ -1048,7 +1060,8 @@ void cg_destroy(cg_ctx* c) {
     release_tables(c);
     for (DevBuf* b : {&c->enc, &c->len, &c->hilo, &c->qual, &c->ambig, &c->sig, &c->qrange, &c->rawCount, &c->cand,
                       &c->ncand, &c->paired, &c->aln, &c->fid, &c->fshift, &c->forient, &c->fweight, &c->flen, &c->nfinal,
-                      &c->flags, &c->out, &c->counters, &c->scanTmp, &c->uoff, &c->forestNodes, &c->treeOffsets})
+                      &c->flags, &c->out, &c->counters, &c->scanTmp, &c->uoff, &c->forestNodes, &c->treeOffsets,
+                      &c->msaOrder, &c->orderScratch})
         b->release();
     for (BatchSet& bs : c->sets) bs.release();
     for (DevBuf* b : {&c->rawAll, &c->rangeOff, &c->rangeTmp, &c->maxima, &c->outRange, &c->flagsRange,

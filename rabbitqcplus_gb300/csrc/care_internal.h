@@ -180,6 +180,9 @@ struct BatchArg {
     uint2* colMeta;
     unsigned int* colCount;
     unsigned int colCap;
+    // MSA order: anchors by decreasing number of kept rows (null: batch order);
+    // the heavy MSAs start first, so that none of them is left for the end
+    const uint32_t* order;
 };
 enum {
     kCounterRaw = 0,
@@ -232,6 +235,9 @@ int align_lane_occupancy(StoreArg st);
 // warp-per-anchor MSA blocks of `warps` warps that fit one SM (0: the warp
 // MSA does not apply to this store)
 int msa_warp_occupancy(StoreArg st, Params p, int warps);
+// order[count] = the batch's anchors by decreasing b.nfinal (log2 buckets);
+// scratch = 32 words, cleared by the launcher
+cudaError_t launch_msa_order(BatchArg b, unsigned int* scratch, uint32_t* order, cudaStream_t s);
 // cursor[0] += stride, work[0] = work[1] = 0 (the last node of a batch)
 cudaError_t launch_batch_advance(unsigned long long* cursor, unsigned int* work, unsigned long long stride,
                                  cudaStream_t s);

@@ -1368,17 +1368,51 @@ __global__ void __launch_bounds__(256, 4) msa_warp_kernel(StoreArg st, Params p,
     }
     const uint64_t first = batch_first(b);
     if (!b.work) {
-        const int a = blockIdx.x * warps + warp;
-        if (a < b.count) msa_warp_anchor(st, p, b, rawOff, lp, a, first, slice, qw);
+        const int i = blockIdx.x * warps + warp;
+        if (i < b.count) msa_warp_anchor(st, p, b, rawOff, lp, b.order ? (int)b.order[i] : i, first, slice, qw);
         return;
     }
     while (true) {
-        int a = 0;
-        if (lane_id() == 0) a = (int)atomicAdd(&b.work[1], 1u);
-        a = __shfl_sync(kFull, a, 0);
-        if (a >= b.count) return;
-        msa_warp_anchor(st, p, b, rawOff, lp, a, first, slice, qw);
+        int i = 0;
+        if (lane_id() == 0) i = (int)atomicAdd(&b.work[1], 1u);
+        i = __shfl_sync(kFull, i, 0);
+        if (i >= b.count) return;
+        msa_warp_anchor(st, p, b, rawOff, lp, b.order ? (int)b.order[i] : i, first, slice, qw);
         __syncwarp();
+    }
+}
+
+constexpr int kOrderBuckets = 16;
+
+// bucket 0 holds the anchors with the most kept rows (nf >= 2^14), bucket 15
+// those with none
+__device__ __forceinline__ int order_bucket(uint32_t nf) { return 15 - min(15, 32 - __clz(nf)); }
+
+__global__ void msa_order_hist_kernel(const uint32_t* __restrict__ nfinal, int count, unsigned int* hist) {
+    __shared__ unsigned int h[kOrderBuckets];
+    if (threadIdx.x < kOrderBuckets) h[threadIdx.x] = 0;
+    __syncthreads();
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < count; a += gridDim.x * blockDim.x)
+        atomicAdd(&h[order_bucket(nfinal[a])], 1u);
+    __syncthreads();
+    if (threadIdx.x < kOrderBuckets && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
+__global__ void msa_order_scatter_kernel(const uint32_t* __restrict__ nfinal, int count,
+                                         const unsigned int* __restrict__ hist, unsigned int* cursor,
+                                         uint32_t* __restrict__ order) {
+    __shared__ unsigned int start[kOrderBuckets];
+    if (threadIdx.x == 0) {
+        unsigned int acc = 0;
+        for (int i = 0; i < kOrderBuckets; i++) {
+            start[i] = acc;
+            acc += hist[i];
+        }
+    }
+    __syncthreads();
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < count; a += gridDim.x * blockDim.x) {
+        const int k = order_bucket(nfinal[a]);
+        order[start[k] + atomicAdd(&cursor[k], 1u)] = (uint32_t)a;
     }
 }
 
@@ -1496,6 +1530,18 @@ cudaError_t launch_msa_correct(StoreArg st, Params p, BatchArg b, int maxRows, c
     if (b.count == 0) return cudaSuccess;
     msa_correct_kernel<<<b.count, msa_threads(maxCols), smem, s>>>(st, p, b, b.rawCount, maxCols, bitsetWords,
                                                                     storeWeights);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_msa_order(BatchArg b, unsigned int* scratch, uint32_t* order, cudaStream_t s) {
+    if (b.count <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(scratch, 0, 2 * kOrderBuckets * sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    const unsigned blocks = (unsigned)min((b.count + 255) / 256, 304);
+    msa_order_hist_kernel<<<blocks, 256, 0, s>>>(b.nfinal, b.count, scratch);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    msa_order_scatter_kernel<<<blocks, 256, 0, s>>>(b.nfinal, b.count, scratch, scratch + kOrderBuckets, order);
     return cudaGetLastError();
 }
 
