@@ -86,7 +86,7 @@ struct GraphSig {
 // One batch pipeline of the batched driver: its buffers, stream and graph.
 struct BatchSet {
     DevBuf rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, flen, nfinal, uoff, scanTmp, cursor,
-        work, colFeat, colMeta, colCount, order, orderScratch;
+        work, colFeat, colMeta, colCount, order, orderScratch, bigScratch;
     cudaStream_t stream = nullptr;
     cudaEvent_t joined = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -98,7 +98,8 @@ struct BatchSet {
         if (joined) cudaEventDestroy(joined);
         joined = nullptr;
         for (DevBuf* b : {&rawCount, &cand, &ncand, &paired, &aln, &fid, &fshift, &forient, &fweight, &flen, &nfinal,
-                          &uoff, &scanTmp, &cursor, &work, &colFeat, &colMeta, &colCount, &order, &orderScratch})
+                          &uoff, &scanTmp, &cursor, &work, &colFeat, &colMeta, &colCount, &order, &orderScratch,
+                          &bigScratch})
             b->release();
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
@@ -143,7 +144,7 @@ struct cg_ctx {
 
     // batch buffers
     DevBuf qrange, rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, flen, nfinal, flags, out, counters;
-    DevBuf scanTmp, uoff, msaOrder, orderScratch;
+    DevBuf scanTmp, uoff, msaOrder, orderScratch, bigScratch;
     uint32_t* hPinned = nullptr;  // 2 words: total raw, max raw
 
     // batched driver
@@ -488,7 +489,10 @@ int run_candidates(cg_ctx* c, uint64_t first, int count) {
     CG_CUDA(c, c->fweight.ensure(cap * sizeof(float)));
     CG_CUDA(c, c->flen.ensure(cap * sizeof(uint16_t)));
     b = batch_arg(c, first, count);
-    CG_CUDA(c, launch_gather_unique(st, c->tables, c->params, b, (int)std::max<uint32_t>(maxRaw, 1), c->stream));
+    CG_CUDA(c, c->bigScratch.ensure((size_t)(count + 1) * sizeof(uint32_t)));
+    CG_CUDA(c, launch_gather_unique(st, c->tables, c->params, b, (int)std::max<uint32_t>(maxRaw, 1), c->stream,
+                                    c->bigScratch.as<uint32_t>()));
+    if (maxRaw > 1024) c->stats.kernel_launches += 1;
     c->stats.kernel_launches += 1;
     return CG_OK;
 }
@@ -621,6 +625,7 @@ int ensure_set(cg_ctx* c, BatchSet& s, int count, uint64_t capRaw) {
     CG_CUDA(c, s.work.ensure(2 * sizeof(unsigned int)));
     CG_CUDA(c, s.order.ensure(n * sizeof(uint32_t)));
     CG_CUDA(c, s.orderScratch.ensure(32 * sizeof(unsigned int)));
+    CG_CUDA(c, s.bigScratch.ensure((n + 1) * sizeof(uint32_t)));
     if (c->params.correctionType == CG_CORR_LEARNED) return ensure_columns(c, s.colFeat, s.colMeta, s.colCount, count);
     return CG_OK;
 }
@@ -634,8 +639,9 @@ cudaError_t enqueue_batch(cg_ctx* c, BatchSet& s, int count, unsigned long long 
     int k = 0;
     const bool learned = c->params.correctionType == CG_CORR_LEARNED;
     cudaError_t e = learned ? cudaMemsetAsync(b.colCount, 0, sizeof(unsigned int), s.stream) : cudaSuccess;
-    if (e == cudaSuccess) e = launch_gather_unique(st, c->tables, c->params, b, tableRaw, s.stream);
-    k++;
+    if (e == cudaSuccess)
+        e = launch_gather_unique(st, c->tables, c->params, b, tableRaw, s.stream, s.bigScratch.as<uint32_t>());
+    k += tableRaw > 1024 ? 2 : 1;
     if (e == cudaSuccess && c->params.paired) {
         e = launch_pair_flags(b, s.stream);
         k++;
@@ -682,7 +688,8 @@ int capture_set(cg_ctx* c, BatchSet& s, int count, unsigned long long stride, co
     g.maxRows = maxRows;
     for (const DevBuf* d : {&s.rawCount, &s.cand, &s.ncand, &s.paired, &s.aln, &s.fid, &s.fshift, &s.forient,
                             &s.fweight, &s.flen, &s.nfinal, &s.uoff, &s.scanTmp, &s.cursor, &s.work, &s.colFeat,
-                            &s.colMeta, &s.colCount, &s.order, &s.orderScratch, &c->mlp, &c->outRange,
+                            &s.colMeta, &s.colCount, &s.order, &s.orderScratch, &s.bigScratch, &c->mlp,
+                            &c->outRange,
                             &c->flagsRange, &c->rangeOff, &c->counters, &c->sig})
         g.ptrs.push_back(d->p);
     g.ptrs.push_back(reinterpret_cast<const void*>(static_cast<uintptr_t>(c->paramsVersion)));
@@ -1061,7 +1068,7 @@ void cg_destroy(cg_ctx* c) {
     for (DevBuf* b : {&c->enc, &c->len, &c->hilo, &c->qual, &c->ambig, &c->sig, &c->qrange, &c->rawCount, &c->cand,
                       &c->ncand, &c->paired, &c->aln, &c->fid, &c->fshift, &c->forient, &c->fweight, &c->flen, &c->nfinal,
                       &c->flags, &c->out, &c->counters, &c->scanTmp, &c->uoff, &c->forestNodes, &c->treeOffsets,
-                      &c->msaOrder, &c->orderScratch})
+                      &c->msaOrder, &c->orderScratch, &c->bigScratch})
         b->release();
     for (BatchSet& bs : c->sets) bs.release();
     for (DevBuf* b : {&c->rawAll, &c->rangeOff, &c->rangeTmp, &c->maxima, &c->outRange, &c->flagsRange,

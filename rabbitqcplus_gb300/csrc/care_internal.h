@@ -202,8 +202,10 @@ enum {
 cudaError_t launch_query_count(StoreArg st, TablesArg tb, Params p, BatchArg b, cudaStream_t s);
 // with b.rangeOff set the kernel looks the buckets up itself and writes the
 // batch's raw offsets into b.rawCount (no query_count pass, no scan)
+// bigScratch (optional, count + 1 words): anchors with more than 1024 raw ids
+// run in a second, large-table pass instead of sizing every block for them
 cudaError_t launch_gather_unique(StoreArg st, TablesArg tb, Params p, BatchArg b, int maxRawPerAnchor,
-                                 cudaStream_t s);
+                                 cudaStream_t s, uint32_t* bigScratch = nullptr);
 cudaError_t launch_pair_flags(BatchArg b, cudaStream_t s);
 // raw id count of every read as an anchor, out[N]
 cudaError_t launch_raw_count(StoreArg st, TablesArg tb, Params p, const unsigned long long* sig, uint32_t* out,

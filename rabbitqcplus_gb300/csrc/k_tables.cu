@@ -13,6 +13,8 @@
 // their buckets, (5) sort each bucket (at most maxValuesPerKey ids).  The
 // bucket contents -- the only thing a query observes -- equal the reference's.
 
+#include <algorithm>
+
 #include "care_device.cuh"
 #include "care_internal.h"
 
@@ -211,37 +213,32 @@ constexpr int kGatherThreads = 128;
 // ids are then put in ascending order by rank (or a bitonic sort when there
 // are many).  rawOff = exclusive scan of the raw counts; the table holds
 // tableSize >= 2 * raw slots.
-__global__ void __launch_bounds__(kGatherThreads) gather_unique_kernel(StoreArg st, TablesArg tb, Params p,
-                                                                       BatchArg b, const uint32_t* __restrict__ rawOff,
-                                                                       int tableSize) {
-    extern __shared__ uint32_t table[];        // [tableSize], then list[tableSize / 2]
-    uint32_t* list = table + tableSize;
-    __shared__ uint2 rng[kMaxMaps];
-    __shared__ uint32_t pre[kMaxMaps + 1];
-    __shared__ uint32_t nUnique;
-    const int a = blockIdx.x;
-    const uint64_t first = batch_first(b);
-    const uint64_t aid = first + (uint64_t)a;
-    const int tid = threadIdx.x;
-    uint32_t off, raw;
+// Raw id range (offset, count) of anchor a.  In the batched form it comes
+// from the range scan; the small-table pass also writes the offset into
+// b.rawCount for the later stages.
+__device__ __forceinline__ uint2 gather_range(const BatchArg& b, const uint32_t* __restrict__ rawOff, int a,
+                                              uint64_t first, bool writeOffsets) {
     if (b.rangeOff) {
-        // batched form: raw offsets from the range scan, buckets looked up here
         const uint64_t r0 = first - out_first(b);
         const unsigned long long* ro = b.rangeOff + r0;
-        off = (uint32_t)(ro[a] - ro[0]);
-        raw = (uint32_t)(ro[a + 1] - ro[a]);
-        if (tid == 0) {
+        const uint32_t off = (uint32_t)(ro[a] - ro[0]);
+        if (writeOffsets && threadIdx.x == 0) {
             b.rawCount[a] = off;
             if (a == b.count - 1) b.rawCount[b.count] = (uint32_t)(ro[b.count] - ro[0]);
         }
-    } else {
-        off = rawOff[a];
-        raw = rawOff[a + 1] - rawOff[a];
+        return make_uint2(off, (uint32_t)(ro[a + 1] - ro[a]));
     }
-    if (raw == 0) {
-        if (tid == 0) b.ncand[a] = 0;
-        return;
-    }
+    return make_uint2(rawOff[a], rawOff[a + 1] - rawOff[a]);
+}
+
+// The union of anchor a's buckets (all threads of the block), raw > 0; the
+// shared-memory table holds tableSize >= 2 * raw slots and a list of half that.
+__device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params& p, const BatchArg& b, int a,
+                           uint64_t aid, uint32_t off, uint32_t raw, uint32_t* table, int tableSize, uint2* rng,
+                           uint32_t* pre, uint32_t* nUniqueS) {
+    uint32_t* list = table + tableSize;
+    uint32_t& nUnique = *nUniqueS;
+    const int tid = threadIdx.x;
     uint32_t T = 64;
     while (T < 2 * raw) T <<= 1;
     const uint32_t mask = T - 1;
@@ -342,6 +339,51 @@ __global__ void __launch_bounds__(kGatherThreads) gather_unique_kernel(StoreArg 
         b.ncand[a] = U;
         atomicAdd(&b.counters[kCounterRaw], (unsigned long long)raw);
         atomicAdd(&b.counters[kCounterUnique], (unsigned long long)U);
+    }
+}
+
+// One block per anchor of the batch with at most smallCap raw ids (all of them
+// when bigList is null); anchors with more go to bigList for gather_big_kernel,
+// whose blocks hold tables large enough for them.  The split keeps the few
+// repeat anchors' large tables from lowering every block's occupancy.
+__global__ void __launch_bounds__(kGatherThreads) gather_unique_kernel(StoreArg st, TablesArg tb, Params p,
+                                                                       BatchArg b, const uint32_t* __restrict__ rawOff,
+                                                                       int tableSize, uint32_t smallCap,
+                                                                       uint32_t* bigList, unsigned int* bigCount) {
+    extern __shared__ uint32_t table[];  // [tableSize], then list[tableSize / 2]
+    __shared__ uint2 rng[kMaxMaps];
+    __shared__ uint32_t pre[kMaxMaps + 1];
+    __shared__ uint32_t nUnique;
+    const int a = blockIdx.x;
+    const uint64_t first = batch_first(b);
+    const uint2 r = gather_range(b, rawOff, a, first, true);
+    if (r.y == 0) {
+        if (threadIdx.x == 0) b.ncand[a] = 0;
+        return;
+    }
+    if (bigList && r.y > smallCap) {
+        if (threadIdx.x == 0) bigList[atomicAdd(bigCount, 1u)] = (uint32_t)a;
+        return;
+    }
+    gather_one(st, tb, p, b, a, first + (uint64_t)a, r.x, r.y, table, tableSize, rng, pre, &nUnique);
+}
+
+// Persistent blocks over the deferred anchors of gather_unique_kernel.
+__global__ void __launch_bounds__(kGatherThreads) gather_big_kernel(StoreArg st, TablesArg tb, Params p, BatchArg b,
+                                                                    const uint32_t* __restrict__ rawOff,
+                                                                    int tableSize, const uint32_t* bigList,
+                                                                    const unsigned int* bigCount) {
+    extern __shared__ uint32_t table[];
+    __shared__ uint2 rng[kMaxMaps];
+    __shared__ uint32_t pre[kMaxMaps + 1];
+    __shared__ uint32_t nUnique;
+    const uint64_t first = batch_first(b);
+    const unsigned int n = *bigCount;
+    for (unsigned int i = blockIdx.x; i < n; i += gridDim.x) {
+        const int a = (int)bigList[i];
+        const uint2 r = gather_range(b, rawOff, a, first, false);
+        gather_one(st, tb, p, b, a, first + (uint64_t)a, r.x, r.y, table, tableSize, rng, pre, &nUnique);
+        __syncthreads();  // the next anchor reuses the shared arrays
     }
 }
 
@@ -471,17 +513,51 @@ cudaError_t launch_query_count(StoreArg st, TablesArg tb, Params p, BatchArg b, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_gather_unique(StoreArg st, TablesArg tb, Params p, BatchArg b, int maxRawPerAnchor,
-                                 cudaStream_t s) {
+namespace {
+
+constexpr uint32_t kGatherSmallRaw = 1024;  // anchors above this go to the large-table pass
+constexpr int kGatherBigBlocksPerSm = 4;
+
+int table_slots(int maxRaw) {
     int T = 64;
-    while (T < 2 * maxRawPerAnchor) T <<= 1;
+    while (T < 2 * maxRaw) T <<= 1;
+    return T;
+}
+
+template <class K>
+cudaError_t gather_smem_attr(K kernel, size_t smem) {
+    if (smem <= 40 * 1024) return cudaSuccess;  // leaves room for the kernel's static shared memory
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+}  // namespace
+
+cudaError_t launch_gather_unique(StoreArg st, TablesArg tb, Params p, BatchArg b, int maxRawPerAnchor,
+                                 cudaStream_t s, uint32_t* bigScratch) {
+    if (b.count <= 0) return cudaSuccess;
+    const bool split = bigScratch && (uint32_t)maxRawPerAnchor > kGatherSmallRaw;
+    const int T = table_slots(split ? (int)kGatherSmallRaw : maxRawPerAnchor);
     const size_t smem = (size_t)T * sizeof(uint32_t) * 3 / 2;  // table + unique list
-    if (smem > 40 * 1024) {  // leaves room for the kernel's static shared memory
-        cudaError_t e = cudaFuncSetAttribute(gather_unique_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
+    cudaError_t e = gather_smem_attr(gather_unique_kernel, smem);
+    if (e != cudaSuccess) return e;
+    unsigned int* bigCount = split ? bigScratch : nullptr;
+    uint32_t* bigList = split ? bigScratch + 1 : nullptr;
+    if (split) {
+        e = cudaMemsetAsync(bigCount, 0, sizeof(unsigned int), s);
         if (e != cudaSuccess) return e;
     }
-    gather_unique_kernel<<<b.count, kGatherThreads, smem, s>>>(st, tb, p, b, b.rawCount, T);
+    gather_unique_kernel<<<b.count, kGatherThreads, smem, s>>>(st, tb, p, b, b.rawCount, T, kGatherSmallRaw,
+                                                                bigList, bigCount);
+    e = cudaGetLastError();
+    if (e != cudaSuccess || !split) return e;
+    const int Tb = table_slots(maxRawPerAnchor);
+    const size_t smemB = (size_t)Tb * sizeof(uint32_t) * 3 / 2;
+    e = gather_smem_attr(gather_big_kernel, smemB);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 1;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned blocks = (unsigned)std::min<int>(b.count, std::max(sms, 1) * kGatherBigBlocksPerSm);
+    gather_big_kernel<<<blocks, kGatherThreads, smemB, s>>>(st, tb, p, b, b.rawCount, Tb, bigList, bigCount);
     return cudaGetLastError();
 }
 
