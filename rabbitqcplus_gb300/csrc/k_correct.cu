@@ -1398,10 +1398,12 @@ __global__ void msa_order_hist_kernel(const uint32_t* __restrict__ nfinal, int c
     if (threadIdx.x < kOrderBuckets && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
 }
 
+// Each block reserves its slots of every bucket with one global atomic per
+// bucket per round (the per-anchor tickets come from shared memory).
 __global__ void msa_order_scatter_kernel(const uint32_t* __restrict__ nfinal, int count,
                                          const unsigned int* __restrict__ hist, unsigned int* cursor,
                                          uint32_t* __restrict__ order) {
-    __shared__ unsigned int start[kOrderBuckets];
+    __shared__ unsigned int start[kOrderBuckets], local[kOrderBuckets], base[kOrderBuckets];
     if (threadIdx.x == 0) {
         unsigned int acc = 0;
         for (int i = 0; i < kOrderBuckets; i++) {
@@ -1409,10 +1411,22 @@ __global__ void msa_order_scatter_kernel(const uint32_t* __restrict__ nfinal, in
             acc += hist[i];
         }
     }
-    __syncthreads();
-    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < count; a += gridDim.x * blockDim.x) {
-        const int k = order_bucket(nfinal[a]);
-        order[start[k] + atomicAdd(&cursor[k], 1u)] = (uint32_t)a;
+    for (int a0 = blockIdx.x * blockDim.x; a0 < count; a0 += gridDim.x * blockDim.x) {
+        if (threadIdx.x < kOrderBuckets) local[threadIdx.x] = 0;
+        __syncthreads();
+        const int a = a0 + threadIdx.x;
+        int k = 0;
+        unsigned int ticket = 0;
+        if (a < count) {
+            k = order_bucket(nfinal[a]);
+            ticket = atomicAdd(&local[k], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x < kOrderBuckets && local[threadIdx.x])
+            base[threadIdx.x] = start[threadIdx.x] + atomicAdd(&cursor[threadIdx.x], local[threadIdx.x]);
+        __syncthreads();
+        if (a < count) order[base[k] + ticket] = (uint32_t)a;
+        __syncthreads();
     }
 }
 
