@@ -125,11 +125,15 @@ struct cg_ctx {
     cudaEvent_t st0 = nullptr, st1 = nullptr, st1b = nullptr, st2 = nullptr, st3 = nullptr;  // stage boundaries
     std::string err;
 
-    // host staging of appended reads
-    std::vector<char> hChars;
-    std::vector<uint64_t> hOffs{0};
-    std::vector<char> hQual;
-    std::vector<uint64_t> callStarts;  // first read id of each append call
+    // appended reads, one device chunk per cg_append_reads call (uploaded by
+    // the call itself; encoded and released by cg_build_tables)
+    struct Chunk {
+        DevBuf chars, offs, qual;  // bases, offsets rebased to 0 (u64 [m+1]), qualities
+        uint64_t first = 0, reads = 0;
+    };
+    std::vector<Chunk> chunks;
+    uint64_t appended = 0;
+    int appendLmax = 0;
     bool haveQual = true;
 
     // device read store
@@ -274,10 +278,9 @@ void release_tables(cg_ctx* c) {
 }
 
 int build_store(cg_ctx* c) {
-    const uint64_t n = c->hOffs.size() - 1;
+    const uint64_t n = c->appended;
     c->n = n;
-    int lmax = 0;
-    for (uint64_t i = 0; i < n; i++) lmax = std::max<int>(lmax, int(c->hOffs[i + 1] - c->hOffs[i]));
+    const int lmax = c->appendLmax;
     c->lmax = std::max(lmax, 1);
     c->pitch = (c->lmax + 15) / 16;
     c->wp = (c->lmax + 31) / 32 + 1;
@@ -299,40 +302,29 @@ int build_store(cg_ctx* c) {
     if (q) CG_CUDA(c, c->qual.ensure(n * (uint64_t)c->lmax));
     CG_CUDA(c, cudaMemsetAsync(c->enc.p, 0, n * c->pitch * sizeof(uint32_t), c->stream));
     if (q) CG_CUDA(c, cudaMemsetAsync(c->qual.p, 0, n * (uint64_t)c->lmax, c->stream));
-    // upload and encode per append call (the N counter restarts per call)
-    DevBuf dChars, dOffs, dQual, dInv, tmp;
-    for (size_t ci = 0; ci < c->callStarts.size(); ci++) {
-        const uint64_t r0 = c->callStarts[ci];
-        const uint64_t r1 = ci + 1 < c->callStarts.size() ? c->callStarts[ci + 1] : n;
-        const uint64_t m = r1 - r0;
-        if (m == 0) continue;
-        const uint64_t b0 = c->hOffs[r0], b1 = c->hOffs[r1];
-        std::vector<uint64_t> offs(m + 1);
-        for (uint64_t i = 0; i <= m; i++) offs[i] = c->hOffs[r0 + i] - b0;
-        CG_CUDA(c, dChars.ensure(std::max<uint64_t>(b1 - b0, 1)));
-        CG_CUDA(c, dOffs.ensure((m + 1) * sizeof(uint64_t)));
+    // encode per append call (the N counter restarts per call)
+    DevBuf dInv, tmp;
+    for (cg_ctx::Chunk& ch : c->chunks) {
+        const uint64_t m = ch.reads;
         CG_CUDA(c, dInv.ensure((m + 1) * sizeof(uint32_t)));
         CG_CUDA(c, tmp.ensure(scan_tmp_bytes(m + 1)));
-        CG_CUDA(c, cudaMemcpyAsync(dChars.p, c->hChars.data() + b0, b1 - b0, cudaMemcpyHostToDevice, c->stream));
-        CG_CUDA(c, cudaMemcpyAsync(dOffs.p, offs.data(), (m + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice,
-                                   c->stream));
-        if (q) {
-            CG_CUDA(c, dQual.ensure(std::max<uint64_t>(b1 - b0, 1)));
-            CG_CUDA(c, cudaMemcpyAsync(dQual.p, c->hQual.data() + b0, b1 - b0, cudaMemcpyHostToDevice, c->stream));
-        }
-        CG_CUDA(c, launch_count_invalid(dChars.as<char>(), dOffs.as<uint64_t>(), m, dInv.as<uint32_t>(), c->stream));
+        CG_CUDA(c, launch_count_invalid(ch.chars.as<char>(), ch.offs.as<uint64_t>(), m, dInv.as<uint32_t>(),
+                                        c->stream));
         CG_CUDA(c, scan_exclusive_u32(dInv.as<uint32_t>(), m, tmp.p, c->stream));
-        CG_CUDA(c, launch_encode(dChars.as<char>(), dOffs.as<uint64_t>(), q ? dQual.as<char>() : nullptr, m, r0,
-                                 dInv.as<uint32_t>(), nullptr, c->enc.as<uint32_t>(), c->len.as<uint16_t>(),
+        CG_CUDA(c, launch_encode(ch.chars.as<char>(), ch.offs.as<uint64_t>(), q ? ch.qual.as<char>() : nullptr, m,
+                                 ch.first, dInv.as<uint32_t>(), nullptr, c->enc.as<uint32_t>(), c->len.as<uint16_t>(),
                                  c->qual.as<uint8_t>(), c->ambig.as<uint8_t>(), c->pitch, c->lmax, c->stream));
-        // the staging buffers are freed below only after the stream drained
+        // the chunks and staging buffers are freed below only after the stream drained
     }
     CG_CUDA(c, cudaStreamSynchronize(c->stream));
-    dChars.release();
-    dOffs.release();
-    dQual.release();
     dInv.release();
     tmp.release();
+    for (cg_ctx::Chunk& ch : c->chunks) {
+        ch.chars.release();
+        ch.offs.release();
+        ch.qual.release();
+    }
+    c->chunks.clear();
     StoreArg st = store_arg(c);
     CG_CUDA(c, launch_hilo(st, c->hilo.as<uint32_t>(), c->stream));
     return CG_OK;
@@ -1070,6 +1062,11 @@ void cg_destroy(cg_ctx* c) {
                       &c->flags, &c->out, &c->counters, &c->scanTmp, &c->uoff, &c->forestNodes, &c->treeOffsets,
                       &c->msaOrder, &c->orderScratch, &c->bigScratch})
         b->release();
+    for (cg_ctx::Chunk& ch : c->chunks) {
+        ch.chars.release();
+        ch.offs.release();
+        ch.qual.release();
+    }
     for (BatchSet& bs : c->sets) bs.release();
     for (DevBuf* b : {&c->rawAll, &c->rangeOff, &c->rangeTmp, &c->maxima, &c->outRange, &c->flagsRange,
                       &c->counterSave, &c->mlp, &c->colFeat, &c->colMeta, &c->colCount})
@@ -1101,21 +1098,37 @@ int cg_append_reads(cg_ctx* c, const char* sequences, const uint64_t* offsets, c
         if (offsets[i + 1] - offsets[i] > CG_MAX_READ_LENGTH)
             return fail(c, CG_ERR_UNSUPPORTED, "read %llu longer than %d", (unsigned long long)i, CG_MAX_READ_LENGTH);
     }
-    if ((c->hOffs.size() - 1) + num_reads > 0xffffffffull)
-        return fail(c, CG_ERR_UNSUPPORTED, "more than 2^32-1 reads");
-    const uint64_t base = c->hChars.size();
+    if (c->appended + num_reads > 0xffffffffull) return fail(c, CG_ERR_UNSUPPORTED, "more than 2^32-1 reads");
+    CG_CUDA(c, cudaSetDevice(c->device));
     const uint64_t bytes = offsets[num_reads] - offsets[0];
-    c->callStarts.push_back(c->hOffs.size() - 1);
-    c->hChars.insert(c->hChars.end(), sequences + offsets[0], sequences + offsets[0] + bytes);
-    if (c->o.use_quality_scores) c->hQual.insert(c->hQual.end(), qualities + offsets[0], qualities + offsets[0] + bytes);
-    for (uint64_t i = 1; i <= num_reads; i++) c->hOffs.push_back(base + offsets[i] - offsets[0]);
+    std::vector<uint64_t> offs(num_reads + 1);
+    int lmax = 0;
+    for (uint64_t i = 0; i <= num_reads; i++) offs[i] = offsets[i] - offsets[0];
+    for (uint64_t i = 0; i < num_reads; i++) lmax = std::max<int>(lmax, int(offs[i + 1] - offs[i]));
+    c->chunks.emplace_back();
+    cg_ctx::Chunk& ch = c->chunks.back();
+    ch.first = c->appended;
+    ch.reads = num_reads;
+    // straight from the caller's memory to the device: no host staging copy
+    CG_CUDA(c, ch.chars.ensure(std::max<uint64_t>(bytes, 1)));
+    CG_CUDA(c, ch.offs.ensure((num_reads + 1) * sizeof(uint64_t)));
+    CG_CUDA(c, cudaMemcpyAsync(ch.chars.p, sequences + offsets[0], bytes, cudaMemcpyHostToDevice, c->stream));
+    CG_CUDA(c, cudaMemcpyAsync(ch.offs.p, offs.data(), (num_reads + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                               c->stream));
+    if (c->o.use_quality_scores) {
+        CG_CUDA(c, ch.qual.ensure(std::max<uint64_t>(bytes, 1)));
+        CG_CUDA(c, cudaMemcpyAsync(ch.qual.p, qualities + offsets[0], bytes, cudaMemcpyHostToDevice, c->stream));
+    }
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));  // `offs` and the caller's buffers may go away
+    c->appended += num_reads;
+    c->appendLmax = std::max(c->appendLmax, lmax);
     return CG_OK;
 }
 
 int cg_build_tables(cg_ctx* c) {
     if (!c) return CG_ERR_INVALID_ARGUMENT;
-    if (c->hOffs.size() < 2) return fail(c, CG_ERR_STATE, "no reads appended");
-    if (c->o.pair_mode == CG_PAIR_PE && ((c->hOffs.size() - 1) & 1))
+    if (c->appended == 0) return fail(c, CG_ERR_STATE, "no reads appended");
+    if (c->o.pair_mode == CG_PAIR_PE && (c->appended & 1))
         return fail(c, CG_ERR_INVALID_ARGUMENT, "paired mode needs an even number of reads");
     CG_CUDA(c, cudaSetDevice(c->device));
     CG_CUDA(c, cudaEventRecord(c->ev0, c->stream));
@@ -1139,9 +1152,6 @@ int cg_build_tables(cg_ctx* c) {
     c->stats.num_maps = c->nmaps;
     c->stats.max_read_length = c->lmax;
     c->built = true;
-    // the host copy of the reads is no longer needed
-    std::vector<char>().swap(c->hChars);
-    std::vector<char>().swap(c->hQual);
     return CG_OK;
 }
 
@@ -1203,7 +1213,7 @@ int cg_get_stats(const cg_ctx* c, cg_stats* out) {
 
 int cg_get_read_info(const cg_ctx* c, uint64_t* num_reads, int32_t* max_length) {
     if (!c) return CG_ERR_INVALID_ARGUMENT;
-    if (num_reads) *num_reads = c->built ? c->n : c->hOffs.size() - 1;
+    if (num_reads) *num_reads = c->built ? c->n : c->appended;
     if (max_length) *max_length = c->lmax;
     return CG_OK;
 }
