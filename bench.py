@@ -48,6 +48,7 @@ import numpy as np  # noqa: E402
 from rabbitqcplus_gb300 import capi, learned, sim  # noqa: E402
 
 METRIC = "corrected reads/s on 1 GB300: plain vs batched+learned, at equal TP/FP vs truth"
+ALIGN_DRAM_BYTES_PER_CANDIDATE = 83.30e6 / 3.777e6
 UNIT = "reads/s"
 
 
@@ -341,11 +342,20 @@ def main():
     dur = stages[dom] / max(launches_k, 1)
     bytes_launch = bytes_step * args.steps / max(launches_k, 1)
     achieved = bytes_launch / dur / 1e9
+    traffic = None
+    if dom == "align":
+        # DRAM bytes (read + write) of align_lane_kernel per candidate, from an ncu capture of one
+        # 65536-anchor launch of this workload at 2 Mbp: 83.3 MB for 3.777M candidates; scaled here
+        # by the candidates of an average launch (the traffic grows with the candidates processed)
+        traffic = ALIGN_DRAM_BYTES_PER_CANDIDATE * per_step_cands * args.steps / max(launches_k, 1)
     roof = {"bound": "hbm", "kernel": kname, "form": "plain", "achieved": achieved, "peak": hbm_peak,
-            "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+            "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic, "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": bytes_launch,
             "avg_launch_ms": dur * 1e3,
             "stage_seconds_per_step": {k: v / args.steps for k, v in stages.items()},
-            "note": "compute-bound (integer pipe); the fraction is of the HBM roofline"}
+            "note": "integer-pipe bound (ALU pipe 71% active in ncu); the fraction is of the HBM roofline, and "
+                    "traffic (measured DRAM bytes) is below the algorithmic bytes because candidate planes "
+                    "shared between anchors hit in L2"}
 
     # e2e through the C ABI with host buffers (batched + learned)
     e2e = None
