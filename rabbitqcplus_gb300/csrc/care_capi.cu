@@ -446,10 +446,11 @@ void set_columns(BatchArg& b, const DevBuf& feat, const DevBuf& meta, const DevB
     b.colCap = (unsigned int)((uint64_t)count * kColumnsPerAnchor);
 }
 
+// classifier blocks: two per SM (each holds 128 of an SM's 512 tensor-memory columns)
 int infer_blocks(cg_ctx* c) {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) sms = 1;
-    return std::max(sms, 1) * 4;
+    return std::max(sms, 1) * 2;
 }
 
 // Candidate ids of a batch (query, scan, gather/unique).  On return

@@ -294,17 +294,25 @@ int cg_classifier_logits(int device, const void* model_data, size_t model_size, 
     Stream st;
     TRY(cudaStreamCreateWithFlags(&st.s, cudaStreamNonBlocking));
     cudaStream_t s = st.s;
-    Dev f32, bf, model, out;
+    Dev f32, bf, model, out, counters;
     int rc = upload_features(features, n, f32, bf, s);
     if (rc != CG_OK) return rc;
     TRY(model.alloc(kMlpBytes));
     TRY(cudaMemcpyAsync(model.p, blob.data(), kMlpBytes, cudaMemcpyHostToDevice, s));
     TRY(out.alloc(n * sizeof(float)));
-    const int blocks = (int)std::min<uint64_t>((n + 63) / 64, 4096);
+    TRY(counters.alloc(kNumCounters * sizeof(unsigned long long)));
+    TRY(cudaMemsetAsync(counters.p, 0, kNumCounters * sizeof(unsigned long long), s));
+    int sms = 1;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) sms = 1;
+    const int blocks = (int)std::min<uint64_t>((n + 127) / 128, 2ull * (uint64_t)std::max(sms, 1));
     TRY(launch_mlp_infer(model.as<unsigned char>(), bf.as<__nv_bfloat16>(), nullptr, nullptr, (unsigned)n,
-                         (unsigned)n, 0.0f, nullptr, 0, out.as<float>(), nullptr, blocks, s));
+                         (unsigned)n, 0.0f, nullptr, 0, out.as<float>(), counters.as<unsigned long long>(), blocks,
+                         s));
+    unsigned long long hc[kNumCounters];
+    TRY(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
     TRY(cudaMemcpyAsync(logits, out.p, n * sizeof(float), cudaMemcpyDeviceToHost, s));
     TRY(cudaStreamSynchronize(s));
+    if (hc[kCounterTimeouts]) return CG_ERR_TIMEOUT;
     return CG_OK;
 }
 

@@ -139,61 +139,248 @@ __device__ __forceinline__ void mlp_forward(const SmemMlp& s, XF x, float (&h1)[
     logit[1] = __fadd_rn(z1, s.b3);
 }
 
-constexpr int kInferWarps = 4;
+// ---------------------------------------------------------------- inference (tcgen05)
+//
+// 128 columns (rows of the product, the MMA's M) per tile.  Operands sit in
+// shared memory in the canonical K-major layout without swizzle (8-row x
+// 16-byte core matrices; the K/8 core matrices of an 8-row group contiguous);
+// one thread issues tcgen05.mma (kind::f16, BF16 A and B, FP32 accumulators
+// in tensor memory), tcgen05.commit arrives on an mbarrier, and every thread
+// reads its row of the accumulators back with tcgen05.ld (thread = TMEM lane).
+// Layer 1 accumulates in TMEM columns 0-63, layer 2 in 64-127; the epilogue of
+// layer 1 (bias, ReLU, BF16) writes layer 2's A operand back to shared memory.
 
-// Inference over a column buffer: warps take 16 columns at a time.  With
+constexpr int kTcRows = 128;
+constexpr uint32_t kTmemCols = 128;
+constexpr uint32_t kWaitSpins = 1u << 20;  // mbarrier polls before a wait is declared failed
+
+// byte offset of element (row, k) of a K-major tile with kdim columns
+__device__ __forceinline__ uint32_t core_offset(int row, int k, int kdim) {
+    return (uint32_t)((((row >> 3) * (kdim >> 3) + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1));
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* ptr) { return (uint32_t)__cvta_generic_to_shared(ptr); }
+
+// shared-memory matrix descriptor: start address, leading byte offset (next
+// core matrix along K), stride byte offset (next 8-row group), version 1, no
+// swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3fffu) | ((uint64_t)((lbo >> 4) & 0x3fffu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, M x N
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// bounded wait for the completion of mbarrier phase `parity`
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    for (uint32_t i = 0; i < kWaitSpins; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// 32 consecutive FP32 accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+                 : "=r"(r[0]),"=r"(r[1]),"=r"(r[2]),"=r"(r[3]),"=r"(r[4]),"=r"(r[5]),"=r"(r[6]),"=r"(r[7]),"=r"(r[8]),"=r"(r[9]),"=r"(r[10]),"=r"(r[11]),"=r"(r[12]),"=r"(r[13]),"=r"(r[14]),"=r"(r[15]),"=r"(r[16]),"=r"(r[17]),"=r"(r[18]),"=r"(r[19]),"=r"(r[20]),"=r"(r[21]),"=r"(r[22]),"=r"(r[23]),"=r"(r[24]),"=r"(r[25]),"=r"(r[26]),"=r"(r[27]),"=r"(r[28]),"=r"(r[29]),"=r"(r[30]),"=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// Inference over a column buffer, persistent over 128-column tiles.  With
 // `logits` set the outputs are written there; otherwise every column whose
 // logit reaches `minLogit` (the logit of the confidence threshold) gets the
 // consensus base in its output row, and the others keep the fallback decision
-// the MSA kernel already wrote.
-__global__ void __launch_bounds__(kInferWarps * 32) mlp_infer_kernel(const unsigned char* __restrict__ model,
-                                                                     const __nv_bfloat16* __restrict__ feat,
-                                                                     const uint2* __restrict__ meta,
-                                                                     const unsigned int* __restrict__ countPtr,
-                                                                     unsigned int count, unsigned int cap,
-                                                                     float minLogit, char* out, int outPitch,
-                                                                     float* logits,
-                                                                     unsigned long long* counters) {
-    __shared__ SmemMlp s;
-    stage_weights(s, model);
+// the MSA kernel already wrote.  A wait that does not end counts in
+// counters[kCounterTimeouts] and ends the block (after a second bounded wait
+// for its MMAs and the release of its tensor memory).
+__global__ void __launch_bounds__(kTcRows) mlp_infer_kernel(const unsigned char* __restrict__ model,
+                                                            const __nv_bfloat16* __restrict__ feat,
+                                                            const uint2* __restrict__ meta,
+                                                            const unsigned int* __restrict__ countPtr,
+                                                            unsigned int count, unsigned int cap, float minLogit,
+                                                            char* out, int outPitch, float* logits,
+                                                            unsigned long long* counters) {
+    __shared__ __align__(1024) unsigned char a1[kTcRows * kMlpFeatures * 2];
+    __shared__ __align__(1024) unsigned char a2[kTcRows * kMlpHidden * 2];
+    __shared__ __align__(1024) unsigned char b1[kMlpHidden * kMlpFeatures * 2];
+    __shared__ __align__(1024) unsigned char b2[kMlpHidden * kMlpHidden * 2];
+    __shared__ float bias1[kMlpHidden], bias2[kMlpHidden], wout[kMlpHidden];
+    __shared__ float bias3;
+    __shared__ __align__(8) unsigned long long mbar;
+    __shared__ uint32_t tmemBase;
+    const int tid = (int)threadIdx.x, warp = tid >> 5;
+    // weights into the canonical layout (B operands: N x K, K-major = the stored rows)
+    const __nv_bfloat16* w1 = reinterpret_cast<const __nv_bfloat16*>(model + kMlpOffW1);
+    const __nv_bfloat16* w2 = reinterpret_cast<const __nv_bfloat16*>(model + kMlpOffW2);
+    const __nv_bfloat16* w3 = reinterpret_cast<const __nv_bfloat16*>(model + kMlpOffW3);
+    for (int i = tid; i < kMlpHidden * kMlpFeatures; i += kTcRows)
+        *reinterpret_cast<__nv_bfloat16*>(b1 + core_offset(i / kMlpFeatures, i % kMlpFeatures, kMlpFeatures)) = w1[i];
+    for (int i = tid; i < kMlpHidden * kMlpHidden; i += kTcRows)
+        *reinterpret_cast<__nv_bfloat16*>(b2 + core_offset(i / kMlpHidden, i % kMlpHidden, kMlpHidden)) = w2[i];
+    const float* bsrc = reinterpret_cast<const float*>(model + kMlpOffB1);
+    if (tid < kMlpHidden) {
+        bias1[tid] = bsrc[tid];
+        bias2[tid] = bsrc[kMlpHidden + tid];
+        wout[tid] = __bfloat162float(w3[tid]);
+    }
+    if (tid == 0) {
+        bias3 = bsrc[2 * kMlpHidden];
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmemBase)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
     __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = tmemBase;
+    const uint32_t lane0 = tbase + ((uint32_t)(warp * 32) << 16);  // this warp's 32 TMEM lanes
+    const uint32_t mb = smem_u32(&mbar);
+    constexpr uint32_t idesc = instr_desc(kTcRows, kMlpHidden);
     unsigned int n = countPtr ? *countPtr : count;
-    if (countPtr && blockIdx.x == 0 && threadIdx.x == 0 && counters) {
+    if (countPtr && blockIdx.x == 0 && tid == 0 && counters) {
         atomicAdd(&counters[kCounterColumns], (unsigned long long)n);
         if (n > cap) atomicAdd(&counters[kCounterColumnOverflow], (unsigned long long)(n - cap));
     }
     if (n > cap) n = cap;
-    const int lane = (int)lane_id();
-    const int g = lane >> 2, t = lane & 3;
-    const unsigned warp = blockIdx.x * kInferWarps + (threadIdx.x >> 5);
-    const unsigned nwarps = gridDim.x * kInferWarps;
-    const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f);
+    uint32_t phase = 0;
     unsigned int taken = 0;
-    for (unsigned r0 = warp * 16; r0 < n; r0 += nwarps * 16) {
-        auto x = [&](int r, int f) -> __nv_bfloat16 {
-            const unsigned row = r0 + (unsigned)r;
-            return row < n ? feat[(uint64_t)row * kMlpFeatures + f] : zero;
-        };
-        float h1[8][4], h2[8][4], z[2];
-        mlp_forward(s, x, h1, h2, z);
-        if (t == 0) {
+    bool failed = false;
+    for (unsigned int t0 = blockIdx.x * kTcRows; t0 < n; t0 += gridDim.x * kTcRows) {
+        const unsigned int row = t0 + (unsigned int)tid;
+        uint4 f[4];
 #pragma unroll
-            for (int half = 0; half < 2; half++) {
-                const unsigned row = r0 + (unsigned)(g + 8 * half);
-                if (row >= n) continue;
-                if (logits) {
-                    logits[row] = z[half];
-                } else if (z[half] >= minLogit) {
-                    const uint2 m = meta[row];
-                    out[(uint64_t)m.x * outPitch + (m.y & 0xffffu)] = (char)((m.y >> 16) & 0xffu);
-                    taken++;
+        for (int j = 0; j < 4; j++) f[j] = make_uint4(0, 0, 0, 0);
+        if (row < n) {
+            const uint4* src = reinterpret_cast<const uint4*>(feat + (uint64_t)row * kMlpFeatures);
+#pragma unroll
+            for (int j = 0; j < 4; j++) f[j] = src[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) *reinterpret_cast<uint4*>(a1 + core_offset(tid, 8 * j, kMlpFeatures)) = f[j];
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // visible to the tensor core
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+#pragma unroll
+            for (int k = 0; k < kMlpFeatures / 16; k++)
+                tc_mma(tbase, smem_desc(smem_u32(a1) + 256u * k, 128, 512), smem_desc(smem_u32(b1) + 256u * k, 128, 512),
+                       idesc, k > 0);
+            tc_commit(mb);
+        }
+        bool ok = mbar_wait(mb, phase);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        tc_fence_after();
+        // layer 1 epilogue: this thread's row -> bias, ReLU, BF16 -> layer 2's A operand
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            float v[32];
+            tc_ld32(lane0 + 32u * half, v);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                uint32_t w[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int c = 32 * half + 8 * j + 2 * q;
+                    w[q] = pack_bf16(fmaxf(__fadd_rn(v[8 * j + 2 * q], bias1[c]), 0.0f),
+                                     fmaxf(__fadd_rn(v[8 * j + 2 * q + 1], bias1[c + 1]), 0.0f));
                 }
+                *reinterpret_cast<uint4*>(a2 + core_offset(tid, 32 * half + 8 * j, kMlpHidden)) =
+                    make_uint4(w[0], w[1], w[2], w[3]);
             }
         }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+#pragma unroll
+            for (int k = 0; k < kMlpHidden / 16; k++)
+                tc_mma(tbase + kMlpHidden, smem_desc(smem_u32(a2) + 256u * k, 128, 1024),
+                       smem_desc(smem_u32(b2) + 256u * k, 128, 1024), idesc, k > 0);
+            tc_commit(mb);
+        }
+        ok = mbar_wait(mb, phase);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        tc_fence_after();
+        float z = 0.0f;
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            float v[32];
+            tc_ld32(lane0 + (uint32_t)kMlpHidden + 32u * half, v);
+#pragma unroll
+            for (int i = 0; i < 32; i++) {
+                const int c = 32 * half + i;
+                const float h = __bfloat162float(__float2bfloat16_rn(fmaxf(__fadd_rn(v[i], bias2[c]), 0.0f)));
+                z = __fadd_rn(z, __fmul_rn(h, wout[c]));
+            }
+        }
+        z = __fadd_rn(z, bias3);
+        if (row < n) {
+            if (logits) {
+                logits[row] = z;
+            } else if (z >= minLogit) {
+                const uint2 m = meta[row];
+                out[(uint64_t)m.x * outPitch + (m.y & 0xffffu)] = (char)((m.y >> 16) & 0xffu);
+                taken++;
+            }
+        }
+        tc_fence_before();  // the next tile's MMAs overwrite the accumulators read here
     }
+    if (failed) {
+        if (tid == 0 && counters) atomicAdd(&counters[kCounterTimeouts], 1ull);
+        mbar_wait(mb, phase ^ 1u);  // the MMAs in flight, bounded again
+    }
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(kTmemCols) : "memory");
     if (counters && !logits) {
         taken = __reduce_add_sync(kFull, taken);
-        if (lane == 0 && taken) atomicAdd(&counters[kCounterLearnedTaken], (unsigned long long)taken);
+        if ((tid & 31) == 0 && taken) atomicAdd(&counters[kCounterLearnedTaken], (unsigned long long)taken);
     }
 }
 
@@ -462,8 +649,8 @@ cudaError_t launch_mlp_infer(const unsigned char* model, const __nv_bfloat16* fe
                              char* out, int outPitch, float* logits, unsigned long long* counters, int blocks,
                              cudaStream_t s) {
     if (blocks <= 0) blocks = 1;
-    mlp_infer_kernel<<<blocks, kInferWarps * 32, 0, s>>>(model, feat, meta, countPtr, count, cap, minLogit, out,
-                                                         outPitch, logits, counters);
+    mlp_infer_kernel<<<blocks, kTcRows, 0, s>>>(model, feat, meta, countPtr, count, cap, minLogit, out, outPitch,
+                                                 logits, counters);
     return cudaGetLastError();
 }
 
