@@ -22,6 +22,7 @@
 #include <string>
 #include <vector>
 
+#include "care_capi_internal.h"
 #include "care_gpu.h"
 #include "care_internal.h"
 #include "care_learned.h"
@@ -144,6 +145,9 @@ struct cg_ctx {
     std::vector<MapTable> maps;
     TablesArg tables{};
     Params params{};
+    // where cg_correct's results go: host memory, or device memory for the
+    // device file path (cg::correct_into_device)
+    cudaMemcpyKind outKind = cudaMemcpyDeviceToHost;
     uint64_t paramsVersion = 0;
 
     // batch buffers
@@ -540,9 +544,9 @@ int run_batch(cg_ctx* c, uint64_t first, int count, uint8_t* hFlags, char* hOut,
     c->stats.kernel_launches += 3;
     c->stats.align_launches += 1;
     c->stats.msa_launches += 1;
-    CG_CUDA(c, cudaMemcpyAsync(hFlags, b.flags, (size_t)count, cudaMemcpyDeviceToHost, c->stream));
+    CG_CUDA(c, cudaMemcpyAsync(hFlags, b.flags, (size_t)count, c->outKind, c->stream));
     CG_CUDA(c, cudaMemcpy2DAsync(hOut, outPitch, b.out, (size_t)c->lmax, std::min<size_t>(outPitch, c->lmax),
-                                 (size_t)count, cudaMemcpyDeviceToHost, c->stream));
+                                 (size_t)count, c->outKind, c->stream));
     CG_CUDA(c, cudaEventSynchronize(c->st3));
     float t01 = 0, t11 = 0, t12 = 0, t23 = 0;
     cudaEventElapsedTime(&t01, c->st0, c->st1);
@@ -971,13 +975,15 @@ int correct_batched(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* out_flags,
     // results of each batch to the host as soon as the batch is done
     for (uint64_t j = 0; j < nb; j++) {
         CG_CUDA(c, cudaStreamWaitEvent(c->copyStream, c->batchDone[j], 0));
-        CG_CUDA(c, cudaMemcpyAsync(out_flags + j * B, c->flagsRange.as<uint8_t>() + j * B, B, cudaMemcpyDeviceToHost,
+        CG_CUDA(c, cudaMemcpyAsync(out_flags + j * B, c->flagsRange.as<uint8_t>() + j * B, B, c->outKind,
                                    c->copyStream));
         CG_CUDA(c, cudaMemcpy2DAsync(out_seq + j * B * out_pitch, out_pitch, c->outRange.as<char>() + j * B * c->lmax,
-                                     (size_t)c->lmax, (size_t)c->lmax, B, cudaMemcpyDeviceToHost, c->copyStream));
+                                     (size_t)c->lmax, (size_t)c->lmax, B, c->outKind, c->copyStream));
     }
-    rc = join_sets(c, pl.streams, c->stream);
-    if (rc != CG_OK) return rc;
+    if (nb > 0) {  // the pipelines exist only once a full batch ran
+        rc = join_sets(c, pl.streams, c->stream);
+        if (rc != CG_OK) return rc;
+    }
     CG_CUDA(c, cudaEventRecord(c->evPro, c->copyStream));
     CG_CUDA(c, cudaStreamWaitEvent(c->stream, c->evPro, 0));
     CG_CUDA(c, cudaEventRecord(c->ev1, c->stream));
@@ -1495,3 +1501,43 @@ extern "C" int cg_get_candidates_noalloc(cg_ctx* c, uint64_t anchor, uint32_t* o
     }
     return CG_OK;
 }
+
+// ---------------------------------------------------------------- device file path hooks
+namespace cg {
+
+int append_device_chunk(cg_ctx* c, void* dChars, uint64_t* dOffs, void* dQual, uint64_t n, int lmax) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    if (c->built) return fail(c, CG_ERR_STATE, "reads cannot be appended after cg_build_tables");
+    if (n == 0) return fail(c, CG_ERR_INVALID_ARGUMENT, "empty read batch");
+    if (c->o.use_quality_scores && !dQual)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "quality scores requested but not given");
+    if (lmax > CG_MAX_READ_LENGTH) return fail(c, CG_ERR_UNSUPPORTED, "reads longer than %d", CG_MAX_READ_LENGTH);
+    if (c->appended + n > 0xffffffffull) return fail(c, CG_ERR_UNSUPPORTED, "more than 2^32-1 reads");
+    c->chunks.emplace_back();
+    cg_ctx::Chunk& ch = c->chunks.back();
+    ch.first = c->appended;
+    ch.reads = n;
+    ch.chars.p = dChars;  // the chunk owns the buffers from here on (freed after the build)
+    ch.chars.bytes = 1;
+    ch.offs.p = dOffs;
+    ch.offs.bytes = (n + 1) * sizeof(uint64_t);
+    if (c->o.use_quality_scores) {
+        ch.qual.p = dQual;
+        ch.qual.bytes = 1;
+    } else if (dQual) {
+        cudaFree(dQual);
+    }
+    c->appended += n;
+    c->appendLmax = std::max(c->appendLmax, lmax);
+    return CG_OK;
+}
+
+int correct_into_device(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* dFlags, char* dSeq, size_t pitch) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    c->outKind = cudaMemcpyDeviceToDevice;
+    const int rc = cg_correct(c, first, num, dFlags, dSeq, pitch);
+    c->outKind = cudaMemcpyDeviceToHost;
+    return rc;
+}
+
+}  // namespace cg

@@ -91,6 +91,15 @@ def test_batched_sub_range_with_remainder_and_repeated_calls():
     assert st["graph_replays"] == 4
 
 
+def test_batched_range_smaller_than_one_batch():
+    # fewer anchors than a batch: everything runs as the remainder
+    r = small_reads(seed=47, n=6_000)
+    (plain,), _ = run(capi.CareOptions.defaults(30.0), r)
+    (bat,), st = run(batched(capi.CareOptions.defaults(30.0), 0), r)
+    same(plain, bat, r.lengths)
+    assert st["graph_replays"] == 0
+
+
 def test_batched_paired_end():
     cfg = sim.SimConfig(seed=45, genome_length=50_000, num_reads=10_000, paired=True, insert_mean=300,
                         insert_sd=30, sub_rate_5p=0.01, sub_rate_3p=0.01)
