@@ -92,7 +92,12 @@ typedef struct cg_options {
     int32_t align_blocks;             /* batched: persistent alignment blocks (128 threads); 0 = tuned */
     int32_t msa_warps;                /* batched: anchors in flight per MSA block, 1..8; 0 = tuned */
     int32_t streams;                  /* batched: batches in flight, 1 or 2; 0 = tuned */
-    int32_t reserved[4];
+    /* cg_correct_files only (no reference counterpart): 0 = FASTQ inputs are
+     * parsed and the output records written on the device (inputs that are not
+     * plain 4-line FASTQ still take the host path), 1 = always parse and write
+     * on the host; both give the same files */
+    int32_t host_file_io;
+    int32_t reserved[3];
 } cg_options;
 
 #define CG_DRIVER_PLAIN 0

@@ -41,6 +41,7 @@ GPU_CU_SOURCES = [
     "k_learned.cu",
     "care_capi.cu",
     "care_train.cu",
+    "care_files.cu",
 ]
 GPU_CPP_SOURCES = [
     "host/seqio.cpp",

@@ -47,7 +47,8 @@ class CareOptions(ctypes.Structure):
         ("align_blocks", ctypes.c_int32),
         ("msa_warps", ctypes.c_int32),
         ("streams", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 4),
+        ("host_file_io", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 3),
     ]
 
     @classmethod

@@ -2,6 +2,7 @@
 #include "care_host.h"
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <fstream>
 #include <iterator>
@@ -10,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "care_files.h"
 #include "seqio.h"
 
 namespace care_gb300 {
@@ -174,6 +176,56 @@ Corrected runCorrection(const ProgramOptions& o) {
     return r;
 }
 
+std::vector<char> loadFile(const std::string& path, const char* what) {
+    std::ifstream is(path, std::ios::binary);
+    if (!is) throw std::runtime_error(std::string("Loading classifier file failed! ") + path);
+    (void)what;
+    return std::vector<char>((std::istreambuf_iterator<char>(is)), std::istreambuf_iterator<char>());
+}
+
+// STEP1-3 with the FASTQ parsing and the output records on the device
+// (care_files.h).  false: the inputs are not all plain 4-line FASTQ (or the
+// path is switched off) and nothing was done.
+bool correctOnDevice(const ProgramOptions& o, cg::FastqRun* run) {
+    if (!o.deviceFileIO || o.inputfiles.empty() || o.outputfilenames.empty()) return false;
+    if (o.correctionType == CorrectionType::Print) return false;
+    for (const auto& f : o.inputfiles) {
+        const FileFormat fmt = detectFormat(f);
+        if (fmt != FileFormat::FASTQ && fmt != FileFormat::FASTQGZ) return false;
+    }
+    const bool paired = o.pairType == SequencePairType::PairedEnd && o.inputfiles.size() == 2;
+    std::vector<std::vector<char>> data;
+    for (const auto& f : o.inputfiles) data.push_back(readWholeFile(f));
+    std::vector<const std::vector<char>*> inputs;
+    for (const auto& d : data) inputs.push_back(&d);
+    std::vector<char> forest, classifier;
+    if (o.correctionType == CorrectionType::Forest) forest = loadFile(o.mlForestfileAnchor, "forest");
+    if (o.correctionType == CorrectionType::Learned) classifier = loadFile(o.mlClassifierFileAnchor, "classifier");
+    const cg_options co = toCgOptions(o);  // FASTQ carries qualities
+    std::string err;
+    const int rc = cg::correct_fastq_on_device(co, inputs, paired, o.outputCorrectionQualityLabels,
+                                               (int)o.outputfilenames.size(),
+                                               o.correctionType == CorrectionType::Forest ? &forest : nullptr,
+                                               o.maxForestTreesAnchor,
+                                               o.correctionType == CorrectionType::Learned ? &classifier : nullptr,
+                                               run, &err);
+    if (rc == CG_ERR_UNSUPPORTED) return false;
+    if (rc != CG_OK) throw std::runtime_error("device file path failed (" + std::to_string(rc) + "): " + err);
+    return true;
+}
+
+FileFormat outputFormat(const ProgramOptions& o) {
+    FileFormat fmt = detectFormat(o.inputfiles[0]);
+    if (o.gzoutput) {
+        if (fmt == FileFormat::FASTQ) fmt = FileFormat::FASTQGZ;
+        if (fmt == FileFormat::FASTA) fmt = FileFormat::FASTAGZ;
+    } else {
+        if (fmt == FileFormat::FASTQGZ) fmt = FileFormat::FASTQ;
+        if (fmt == FileFormat::FASTAGZ) fmt = FileFormat::FASTA;
+    }
+    return fmt;
+}
+
 std::string labelled(const std::string& header, uint8_t status, bool labels) {
     if (!labels) return header;
     // src/correctionresultoutput.cpp:403-414
@@ -183,17 +235,25 @@ std::string labelled(const std::string& header, uint8_t status, bool labels) {
 }  // namespace
 
 RunReport performCorrection(const ProgramOptions& o) {
-    Corrected r = runCorrection(o);
-    std::vector<FileFormat> formats;
-    for (const auto& f : o.inputfiles) formats.push_back(detectFormat(f));
-    FileFormat fmt = formats[0];
-    if (o.gzoutput) {
-        if (fmt == FileFormat::FASTQ) fmt = FileFormat::FASTQGZ;
-        if (fmt == FileFormat::FASTA) fmt = FileFormat::FASTAGZ;
-    } else {
-        if (fmt == FileFormat::FASTQGZ) fmt = FileFormat::FASTQ;
-        if (fmt == FileFormat::FASTAGZ) fmt = FileFormat::FASTA;
+    {
+        cg::FastqRun dr;
+        if (correctOnDevice(o, &dr)) {
+            const FileFormat fmt = outputFormat(o);
+            for (size_t f = 0; f < o.outputfilenames.size(); f++) {
+                SequenceWriter w(o.outputdirectory + "/" + o.outputfilenames[f], fmt);
+                w.writeRaw(dr.outputs[f].data(), dr.outputs[f].size());
+            }
+            RunReport rep;
+            rep.reads = dr.reads;
+            rep.records = dr.records;
+            rep.stats = dr.stats;
+            rep.deviceFileIO = true;
+            return rep;
+        }
     }
+    if (o.inputfiles.empty()) throw std::runtime_error("no input files");
+    Corrected r = runCorrection(o);
+    const FileFormat fmt = outputFormat(o);
     if (o.outputfilenames.empty()) throw std::runtime_error("no output file names");
     std::vector<std::unique_ptr<SequenceWriter>> writers;
     for (const auto& name : o.outputfilenames)
@@ -217,6 +277,49 @@ RunReport performCorrection(const ProgramOptions& o) {
 
 RunReport performCorrectionToSink(const ProgramOptions& o, const std::function<void(int)>& onStart,
                                   const ChunkSink& sink) {
+    {
+        cg::FastqRun dr;
+        ProgramOptions od = o;
+        const int nfiles = (o.pairType == SequencePairType::PairedEnd && o.inputfiles.size() == 2) ? 2 : 1;
+        od.outputfilenames.assign(nfiles, "queue");  // one record stream per queue
+        if (correctOnDevice(od, &dr)) {
+            RunReport rep;
+            rep.reads = dr.reads;
+            rep.records = dr.records;
+            rep.stats = dr.stats;
+            rep.deviceFileIO = true;
+            onStart((int)dr.records);  // src/correctionresultoutput.cpp:465-466
+            if (dr.records == 0) return rep;
+            // whole records into chunks of under 1 MiB, the host writer's cut points
+            const size_t cap = 1u << 20;
+            std::vector<size_t> at(nfiles, 0);
+            bool ok = true, more = true;
+            while (ok && more) {
+                more = false;
+                for (int f = 0; f < nfiles && ok; f++) {  // the files' chunks alternate
+                    const std::vector<char>& b = dr.outputs[f];
+                    size_t end = at[f];
+                    while (end < b.size()) {
+                        size_t rec = end;
+                        for (int line = 0; line < 4; line++) {
+                            const void* nl = std::memchr(b.data() + rec, '\n', b.size() - rec);
+                            rec = (const char*)nl - b.data() + 1;
+                        }
+                        if (rec - end >= cap) throw std::runtime_error("record larger than a 1 MiB chunk");
+                        if (rec - at[f] >= cap) break;
+                        end = rec;
+                    }
+                    if (end == at[f]) continue;
+                    char* chunk = new char[cap];
+                    std::memcpy(chunk, b.data() + at[f], end - at[f]);
+                    ok = sink(f, chunk, (int)(end - at[f]));
+                    at[f] = end;
+                    more |= at[f] < b.size();
+                }
+            }
+            return rep;
+        }
+    }
     Corrected r = runCorrection(o);
     RunReport rep;
     rep.reads = r.reads.size();
@@ -296,6 +399,7 @@ extern "C" int cg_correct_files(const cg_options* options, const char* const* in
     o.thresholdAnchor = options->threshold_anchor;
     o.deviceIds = {options->device};
     o.gpuBatched = options->driver == CG_DRIVER_BATCHED;
+    o.deviceFileIO = options->host_file_io == 0;
     o.outputCorrectionQualityLabels = quality_labels != 0;
     o.gzoutput = gz_output != 0;
     o.outputdirectory = output_directory;
@@ -305,7 +409,8 @@ extern "C" int cg_correct_files(const cg_options* options, const char* const* in
         RunReport rep = performCorrection(o);
         if (num_records) *num_records = rep.records;
         return CG_OK;
-    } catch (const std::exception&) {
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "cg_correct_files: %s\n", e.what());  // the C ABI has no context to hold it
         return CG_ERR_IO;
     }
 }

@@ -58,6 +58,9 @@ struct ProgramOptions {
     // and the serialized classifier of CorrectionType::Learned.
     bool gpuBatched = true;
     std::string mlClassifierFileAnchor = "";
+    // FASTQ inputs parsed and output records written on the device (inputs
+    // that are not plain 4-line FASTQ take the host reader and writer anyway)
+    bool deviceFileIO = true;
     bool showProgress = false;
     int threads = 1;
     std::vector<int> deviceIds;
@@ -79,6 +82,7 @@ struct RunReport {
     uint64_t reads = 0;
     uint64_t records = 0;  // correction records (changNum)
     cg_stats stats{};
+    bool deviceFileIO = false;  // the files were parsed and written on the device
 };
 
 // STEP1-3 into files outputdirectory/outputfilenames[i].  Throws on error.

@@ -1,5 +1,6 @@
 #include "seqio.h"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <stdexcept>
@@ -211,6 +212,59 @@ void SequenceWriter::write(const std::string& header, const char* seq, size_t le
         b.push_back('\n');
     }
     if (b.size() > (1u << 22)) impl->flush();
+}
+
+void SequenceWriter::writeRaw(const char* data, size_t len) {
+    impl->flush();
+    const size_t step = 1u << 30;  // gzwrite takes an unsigned count
+    for (size_t done = 0; done < len; done += step) {
+        const size_t k = len - done < step ? len - done : step;
+#ifdef CG_HAVE_ZLIB
+        if (impl->gz) {
+            if (gzwrite(impl->gz, data + done, (unsigned)k) != (int)k) throw std::runtime_error("gzip write failed");
+            continue;
+        }
+#endif
+        if (std::fwrite(data + done, 1, k, impl->f) != k) throw std::runtime_error("write failed");
+    }
+}
+
+std::vector<char> readWholeFile(const std::string& path) {
+    std::vector<char> out;
+#ifdef CG_HAVE_ZLIB
+    gzFile gz = gzopen(path.c_str(), "rb");
+    if (!gz) throw std::runtime_error("cannot open " + path);
+    gzbuffer(gz, 1 << 20);
+    size_t used = 0;
+    out.resize(1 << 24);
+    while (true) {
+        if (used == out.size()) out.resize(out.size() * 2);
+        const size_t want = std::min<size_t>(out.size() - used, 1u << 30);
+        const int got = gzread(gz, out.data() + used, (unsigned)want);
+        if (got < 0) {
+            gzclose(gz);
+            throw std::runtime_error("cannot read " + path);
+        }
+        if (got == 0) break;
+        used += (size_t)got;
+    }
+    gzclose(gz);
+    out.resize(used);
+#else
+    if (endsWith(path, ".gz")) throw std::runtime_error("gzip input needs zlib: " + path);
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) throw std::runtime_error("cannot open " + path);
+    std::fseek(f, 0, SEEK_END);
+    const long size = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    out.resize(size > 0 ? (size_t)size : 0);
+    if (!out.empty() && std::fread(out.data(), 1, out.size(), f) != out.size()) {
+        std::fclose(f);
+        throw std::runtime_error("cannot read " + path);
+    }
+    std::fclose(f);
+#endif
+    return out;
 }
 
 void readSingleFile(const std::string& path, ReadSet& out, uint8_t fileId) {

@@ -54,11 +54,16 @@ public:
     SequenceWriter(const std::string& path, FileFormat format);
     ~SequenceWriter();
     void write(const std::string& header, const char* seq, size_t len, const std::string& qual);
+    // bytes of already formatted records
+    void writeRaw(const char* data, size_t len);
 
 private:
     struct Impl;
     std::unique_ptr<Impl> impl;
 };
+
+// The whole (decompressed) content of a plain or gzip file.
+std::vector<char> readWholeFile(const std::string& path);
 
 // Reads all files of one input group: a single-end file, an interleaved
 // paired file, or two paired files read alternately.
