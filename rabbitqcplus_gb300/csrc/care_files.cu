@@ -23,6 +23,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -477,7 +478,9 @@ int correct_fastq_on_device(const cg_options& options, const std::vector<const s
     DCHECK(cudaGetLastError());
     unsigned long long records = 0;
     DCHECK(cudaMemcpyAsync(&records, recCount.p, sizeof(records), cudaMemcpyDeviceToHost, s));
-    run->outputs.assign((size_t)numOutputs, std::vector<char>());
+    run->outputs.clear();
+    run->outputs.resize((size_t)numOutputs);
+    run->outputSizes.assign((size_t)numOutputs, 0);
     DMem pos, tmp;
     DCHECK(pos.alloc((n + 1) * sizeof(unsigned long long)));
     DCHECK(tmp.alloc(scan_tmp_bytes(n + 1)));
@@ -497,8 +500,9 @@ int correct_fastq_on_device(const cg_options& options, const std::vector<const s
                                                            status.as<uint8_t>(), seqOut.as<char>(), pitch,
                                                            qualityLabels ? 1 : 0, outDev.as<char>());
         DCHECK(cudaGetLastError());
-        run->outputs[f].resize(total);
-        DCHECK(cudaMemcpyAsync(run->outputs[f].data(), outDev.p, total, cudaMemcpyDeviceToHost, s));
+        run->outputs[f].reset(new char[total]);  // left uninitialised: the copy fills it
+        run->outputSizes[f] = total;
+        DCHECK(cudaMemcpyAsync(run->outputs[f].get(), outDev.p, total, cudaMemcpyDeviceToHost, s));
         DCHECK(cudaStreamSynchronize(s));
     }
     DCHECK(cudaStreamSynchronize(s));

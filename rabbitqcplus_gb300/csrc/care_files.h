@@ -14,6 +14,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -25,7 +26,9 @@ struct FastqRun {
     uint64_t reads = 0;
     uint64_t records = 0;                    // correction records (changNum)
     cg_stats stats{};
-    std::vector<std::vector<char>> outputs;  // bytes of every output file
+    // bytes of every output file
+    std::vector<std::unique_ptr<char[]>> outputs;
+    std::vector<size_t> outputSizes;
 };
 
 // Corrects the reads of `inputs` (the bytes of whole FASTQ files) and returns

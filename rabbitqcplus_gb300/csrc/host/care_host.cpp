@@ -241,7 +241,7 @@ RunReport performCorrection(const ProgramOptions& o) {
             const FileFormat fmt = outputFormat(o);
             for (size_t f = 0; f < o.outputfilenames.size(); f++) {
                 SequenceWriter w(o.outputdirectory + "/" + o.outputfilenames[f], fmt);
-                w.writeRaw(dr.outputs[f].data(), dr.outputs[f].size());
+                w.writeRaw(dr.outputs[f].get(), dr.outputSizes[f]);
             }
             RunReport rep;
             rep.reads = dr.reads;
@@ -297,13 +297,14 @@ RunReport performCorrectionToSink(const ProgramOptions& o, const std::function<v
             while (ok && more) {
                 more = false;
                 for (int f = 0; f < nfiles && ok; f++) {  // the files' chunks alternate
-                    const std::vector<char>& b = dr.outputs[f];
+                    const char* b = dr.outputs[f].get();
+                    const size_t bsize = dr.outputSizes[f];
                     size_t end = at[f];
-                    while (end < b.size()) {
+                    while (end < bsize) {
                         size_t rec = end;
                         for (int line = 0; line < 4; line++) {
-                            const void* nl = std::memchr(b.data() + rec, '\n', b.size() - rec);
-                            rec = (const char*)nl - b.data() + 1;
+                            const void* nl = std::memchr(b + rec, '\n', bsize - rec);
+                            rec = (const char*)nl - b + 1;
                         }
                         if (rec - end >= cap) throw std::runtime_error("record larger than a 1 MiB chunk");
                         if (rec - at[f] >= cap) break;
@@ -311,10 +312,10 @@ RunReport performCorrectionToSink(const ProgramOptions& o, const std::function<v
                     }
                     if (end == at[f]) continue;
                     char* chunk = new char[cap];
-                    std::memcpy(chunk, b.data() + at[f], end - at[f]);
+                    std::memcpy(chunk, b + at[f], end - at[f]);
                     ok = sink(f, chunk, (int)(end - at[f]));
                     at[f] = end;
-                    more |= at[f] < b.size();
+                    more |= at[f] < bsize;
                 }
             }
             return rep;

@@ -231,6 +231,24 @@ void SequenceWriter::writeRaw(const char* data, size_t len) {
 
 std::vector<char> readWholeFile(const std::string& path) {
     std::vector<char> out;
+    bool gzipped = false;
+    {
+        FILE* f = std::fopen(path.c_str(), "rb");
+        if (!f) throw std::runtime_error("cannot open " + path);
+        unsigned char magic[2] = {0, 0};
+        gzipped = std::fread(magic, 1, 2, f) == 2 && magic[0] == 0x1f && magic[1] == 0x8b;
+        if (!gzipped) {  // plain: one read of the whole file
+            std::fseek(f, 0, SEEK_END);
+            const long size = std::ftell(f);
+            std::fseek(f, 0, SEEK_SET);
+            out.resize(size > 0 ? (size_t)size : 0);
+            const bool ok = out.empty() || std::fread(out.data(), 1, out.size(), f) == out.size();
+            std::fclose(f);
+            if (!ok) throw std::runtime_error("cannot read " + path);
+            return out;
+        }
+        std::fclose(f);
+    }
 #ifdef CG_HAVE_ZLIB
     gzFile gz = gzopen(path.c_str(), "rb");
     if (!gz) throw std::runtime_error("cannot open " + path);
@@ -251,18 +269,8 @@ std::vector<char> readWholeFile(const std::string& path) {
     gzclose(gz);
     out.resize(used);
 #else
-    if (endsWith(path, ".gz")) throw std::runtime_error("gzip input needs zlib: " + path);
-    FILE* f = std::fopen(path.c_str(), "rb");
-    if (!f) throw std::runtime_error("cannot open " + path);
-    std::fseek(f, 0, SEEK_END);
-    const long size = std::ftell(f);
-    std::fseek(f, 0, SEEK_SET);
-    out.resize(size > 0 ? (size_t)size : 0);
-    if (!out.empty() && std::fread(out.data(), 1, out.size(), f) != out.size()) {
-        std::fclose(f);
-        throw std::runtime_error("cannot read " + path);
-    }
-    std::fclose(f);
+    (void)gzipped;
+    throw std::runtime_error("gzip input needs zlib: " + path);
 #endif
     return out;
 }
