@@ -501,23 +501,27 @@ __device__ __forceinline__ void load_planes(uint32_t (&R)[2][2 * MAXW], const ui
 }
 
 // The reference's sequential scan of one direction (as seq_scan), with a fast
-// rejection for shifts whose overlap has at least 64 bases: the mismatches of
-// the overlap's first two words (complete, so no masks) against the error
-// limit of the scan's longest overlap, tabMax.  The reference's limit at any
-// shift is min(maxErrTab[ov], ...) <= tabMax and the two words' mismatches
-// are part of the shift's, so a shift rejected here is rejected there too.
-// Every other shift takes the reference's step.  The direction ends where the
-// reference's does: at the first shift whose limit is <= 0, i.e. whose
-// overlap is at most max((tb - best) / 2, ovPos - 1), ovPos being the
-// smallest overlap with a positive table entry; that point moves only when
-// the best score improves.  Overlap at shift sl: min(X - sl, Y), X = La and
-// Y = Lc for the right scan (anchor shifted), the other way round for the left.
+// rejection for shifts whose overlap has at least 32 bases: with at least 64
+// bases, the mismatches of the overlap's first two words (complete, so no
+// masks) against the error limit of the scan's longest overlap, tabMax; with
+// 32 to 63 bases, those of the first word against the limit at overlap
+// min(63, La, Lc), tab63.  The reference's limit at any shift is
+// min(maxErrTab[ov], ...) and the table is non-decreasing, so it is at most
+// the bound used, and the words' mismatches are part of the shift's: a shift
+// rejected here is rejected there too.  Every other shift takes the
+// reference's step.  The direction ends where the reference's does: at the
+// first shift whose limit is <= 0, i.e. whose overlap is at most
+// max((tb - best) / 2, ovPos - 1), ovPos being the smallest overlap with a
+// positive table entry; that point moves only when the best score improves.
+// Overlap at shift sl: min(X - sl, Y), X = La and Y = Lc for the right scan
+// (anchor shifted), the other way round for the left.
 template <int MAXW, bool LEFT>
 __device__ __forceinline__ void seq_scan_fast(const uint32_t (&S)[2][2 * MAXW], const uint32_t (&O)[2][2 * MAXW],
                                               int La, int Lc, int n, int tb, const int16_t* __restrict__ maxErrTab,
-                                              int tabMax, int ovPos, int& bestScore, int& bestShift) {
+                                              int tabMax, int tab63, int ovPos, int& bestScore, int& bestShift) {
     const int X = LEFT ? Lc : La, Y = LEFT ? La : Lc;
-    const int slFast = Y >= 64 ? X - 64 : -1;  // overlap >= 64 up to here
+    const int slFast = Y >= 64 ? X - 64 : -1;   // overlap >= 64 up to here
+    const int slFast1 = Y >= 32 ? X - 32 : -1;  // overlap >= 32 up to here
     auto stopAt = [&](int best) {
         const int dv = max((tb - best) >> 1, ovPos - 1);  // done once the overlap is <= dv
         return Y <= dv ? 0 : X - dv;
@@ -534,7 +538,11 @@ __device__ __forceinline__ void seq_scan_fast(const uint32_t (&S)[2][2 * MAXW], 
             const uint32_t h1 = __funnelshift_l(S[0][W + 2], S[0][W + 1], bb),
                            l1 = __funnelshift_l(S[1][W + 2], S[1][W + 1], bb);
             const uint32_t d0 = (h0 ^ O[0][0]) | (l0 ^ O[1][0]), d1 = (h1 ^ O[0][1]) | (l1 ^ O[1][1]);
-            if (sl <= slFast && __popc(d0) + __popc(d1) >= tabMax) continue;
+            if (sl <= slFast) {
+                if (__popc(d0) + __popc(d1) >= tabMax) continue;
+            } else if (sl <= slFast1 && __popc(d0) >= tab63) {
+                continue;
+            }
             // the reference's step
             const int ov = min(X - sl, Y);
             const int maxErr = min((int)maxErrTab[ov], bestScore - tb + 2 * ov);  // > 0 before `stop`
@@ -570,9 +578,11 @@ __device__ __forceinline__ AlnRes align_seq_fast(const uint32_t (&A)[2][2 * MAXW
                                                  int La, int Lc, int minov, const int16_t* maxErrTab, int ovPos) {
     const int tb = La + Lc;
     const int tabMax = maxErrTab[min(La, Lc)];
+    const int tab63 = maxErrTab[min(63, min(La, Lc))];
     int bestScore = tb, bestShift = -Lc;
-    seq_scan_fast<MAXW, false>(A, C, La, Lc, La - minov + 1, tb, maxErrTab, tabMax, ovPos, bestScore, bestShift);
-    seq_scan_fast<MAXW, true>(C, A, La, Lc, Lc - minov, tb, maxErrTab, tabMax, ovPos, bestScore, bestShift);
+    seq_scan_fast<MAXW, false>(A, C, La, Lc, La - minov + 1, tb, maxErrTab, tabMax, tab63, ovPos, bestScore,
+                               bestShift);
+    seq_scan_fast<MAXW, true>(C, A, La, Lc, Lc - minov, tb, maxErrTab, tabMax, tab63, ovPos, bestScore, bestShift);
     AlnRes r;
     r.valid = bestShift != -Lc;
     const int cb = max(-bestShift, 0);
