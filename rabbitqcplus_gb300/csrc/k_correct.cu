@@ -416,95 +416,28 @@ __global__ void __launch_bounds__(kAlignWarps * 32, REGS ? (MAXW <= 5 ? 6 : 4) :
 
 // ---------------------------------------------------------------- lane per candidate
 
-// One direction of the reference's sequential shift scan for one lane.
-// S: words of the shifted sequence, O: words of the other one (hi, lo planes,
-// zero past the read).  Right scan (LEFT false): shift sl = 0..n-1 moves the
-// anchor; left scan: sl = 1..n moves the candidate.  max_errors and the break
-// follow src/cpu_alignment.cpp:324-397 / 408-481 exactly; the first two words
-// are evaluated without branches, later ones only while under max_errors.
-template <int MAXW, bool LEFT>
-__device__ __forceinline__ void seq_scan(const uint32_t (&S)[2][2 * MAXW], const uint32_t (&O)[2][2 * MAXW],
-                                         int La, int Lc, int n, int tb, const int16_t* __restrict__ maxErrTab,
-                                         int& bestScore, int& bestShift) {
-    bool done = false;
-#pragma unroll
-    for (int W = 0; W < MAXW; W++) {
-        if (done) break;
-        for (int bb = 0; bb < 32; bb++) {
-            const int sl = 32 * W + bb;
-            if (LEFT && sl == 0) continue;
-            if (LEFT ? sl > n : sl >= n) {
-                done = true;
-                break;
-            }
-            const int ov = LEFT ? min(La, Lc - sl) : min(La - sl, Lc);
-            const int maxErr = min((int)maxErrTab[ov], bestScore - tb + 2 * ov);
-            if (maxErr <= 0) {
-                done = true;
-                break;
-            }
-            const int parts = (ov + 31) >> 5;
-            const int rem = (parts << 5) - ov;
-            const uint32_t last = 0xffffffffu << rem;
-            const uint32_t mask0 = parts > 1 ? 0xffffffffu : last;
-            const uint32_t mask1 = parts > 2 ? 0xffffffffu : (parts == 2 ? last : 0u);
-            const uint32_t h0 = __funnelshift_l(S[0][W + 1], S[0][W], bb), l0 = __funnelshift_l(S[1][W + 1], S[1][W], bb);
-            const uint32_t h1 = __funnelshift_l(S[0][W + 2], S[0][W + 1], bb),
-                           l1 = __funnelshift_l(S[1][W + 2], S[1][W + 1], bb);
-            int m = __popc(((h0 ^ O[0][0]) | (l0 ^ O[1][0])) & mask0) + __popc(((h1 ^ O[0][1]) | (l1 ^ O[1][1])) & mask1);
-            if (m < maxErr && parts > 2) {
-#pragma unroll
-                for (int i = 2; i < MAXW; i++) {
-                    if (i >= parts || m >= maxErr) break;
-                    const uint32_t mask = i == parts - 1 ? last : 0xffffffffu;
-                    const uint32_t hi = __funnelshift_l(S[0][W + i + 1], S[0][W + i], bb);
-                    const uint32_t lo = __funnelshift_l(S[1][W + i + 1], S[1][W + i], bb);
-                    m += __popc(((hi ^ O[0][i]) | (lo ^ O[1][i])) & mask);
-                }
-            }
-            if (m < maxErr) {
-                const int score = m + tb - 2 * ov;
-                if (score < bestScore) {
-                    bestScore = score;
-                    bestShift = LEFT ? -sl : sl;
-                }
-            }
-        }
-    }
-}
-
+// Both reads' planes for the lane kernel: words 0..MAXW (a read of at most
+// 32 * MAXW bases and the zero word after it).  Every word a shift reads lies
+// at index <= MAXW.
 template <int MAXW>
-__device__ __forceinline__ AlnRes align_seq(const uint32_t (&A)[2][2 * MAXW], const uint32_t (&C)[2][2 * MAXW],
-                                            int La, int Lc, int minov, const int16_t* maxErrTab) {
-    const int tb = La + Lc;
-    int bestScore = tb, bestShift = -Lc;
-    seq_scan<MAXW, false>(A, C, La, Lc, La - minov + 1, tb, maxErrTab, bestScore, bestShift);
-    seq_scan<MAXW, true>(C, A, La, Lc, Lc - minov, tb, maxErrTab, bestScore, bestShift);
-    AlnRes r;
-    r.valid = bestShift != -Lc;
-    const int cb = max(-bestShift, 0);
-    const int ce = min(Lc, La - bestShift);
-    r.overlap = ce - cb;
-    r.score = bestScore;
-    r.shift = bestShift;
-    r.nOps = bestScore - tb + 2 * r.overlap;
-    return r;
-}
-
-template <int MAXW>
-__device__ __forceinline__ void load_planes(uint32_t (&R)[2][2 * MAXW], const uint32_t* __restrict__ hilo, int wp) {
+__device__ __forceinline__ void load_planes(uint32_t (&R)[2][MAXW + 1], const uint32_t* __restrict__ hilo, int wp) {
 #pragma unroll
-    for (int i = 0; i < 2 * MAXW; i++) {
+    for (int i = 0; i <= MAXW; i++) {
         R[0][i] = i < wp ? hilo[i] : 0u;
         R[1][i] = i < wp ? hilo[wp + i] : 0u;
     }
 }
 
-// The reference's sequential scan of one direction (as seq_scan), with a fast
-// rejection for shifts whose overlap has at least 32 bases: with at least 64
-// bases, the mismatches of the overlap's first two words (complete, so no
-// masks) against the error limit of the scan's longest overlap, tabMax; with
-// 32 to 63 bases, those of the first word against the limit at overlap
+// One direction of the reference's sequential shift scan for one lane
+// (src/cpu_alignment.cpp:324-397 right, 408-481 left; the same max_errors,
+// score and break).  S: words of the shifted sequence, O: words of the other
+// one (hi, lo planes, zero past the read).  Right scan (LEFT false): shift
+// sl = 0..n-1 moves the anchor; left scan: sl = 1..n moves the candidate.
+//
+// A fast rejection for shifts whose overlap has at least 32 bases: with at
+// least 64 bases, the mismatches of the overlap's first two words (complete,
+// so no masks) against the error limit of the scan's longest overlap, tabMax;
+// with 32 to 63 bases, those of the first word against the limit at overlap
 // min(63, La, Lc), tab63.  The reference's limit at any shift is
 // min(maxErrTab[ov], ...) and the table is non-decreasing, so it is at most
 // the bound used, and the words' mismatches are part of the shift's: a shift
@@ -515,10 +448,20 @@ __device__ __forceinline__ void load_planes(uint32_t (&R)[2][2 * MAXW], const ui
 // positive table entry; that point moves only when the best score improves.
 // Overlap at shift sl: min(X - sl, Y), X = La and Y = Lc for the right scan
 // (anchor shifted), the other way round for the left.
+//
+// Shifts go by word groups W (sl = 32 W + bb); after each group the shifted
+// read's words move down by one, so that word W + i is always S[.][i] and one
+// copy of the loop body serves every group (S is consumed).  The lanes of
+// `lanes` (one candidate each) walk the shifts in step: every loop bound is
+// the same for all of them (warp minimum or maximum of the lanes' own
+// bounds), so the common loops carry one test per shift and no per-lane
+// exits.  A lane past its own end only sees shifts that its step rejects
+// (beyond the end the limit is <= 0, and the step checks the end).
 template <int MAXW, bool LEFT>
-__device__ __forceinline__ void seq_scan_fast(const uint32_t (&S)[2][2 * MAXW], const uint32_t (&O)[2][2 * MAXW],
-                                              int La, int Lc, int n, int tb, const int16_t* __restrict__ maxErrTab,
-                                              int tabMax, int tab63, int ovPos, int& bestScore, int& bestShift) {
+__device__ __forceinline__ void seq_scan_fast(uint32_t (&S)[2][MAXW + 1], const uint32_t (&O)[2][MAXW + 1], int La,
+                                              int Lc, int n, int tb, const int16_t* __restrict__ maxErrTab,
+                                              int tabMax, int tab63, int ovPos, unsigned lanes, int& bestScore,
+                                              int& bestShift) {
     const int X = LEFT ? Lc : La, Y = LEFT ? La : Lc;
     const int slFast = Y >= 64 ? X - 64 : -1;   // overlap >= 64 up to here
     const int slFast1 = Y >= 32 ? X - 32 : -1;  // overlap >= 32 up to here
@@ -526,39 +469,36 @@ __device__ __forceinline__ void seq_scan_fast(const uint32_t (&S)[2][2 * MAXW], 
         const int dv = max((tb - best) >> 1, ovPos - 1);  // done once the overlap is <= dv
         return Y <= dv ? 0 : X - dv;
     };
-    const int slStart = LEFT ? 1 : 0;
     int stop = min(LEFT ? n + 1 : n, stopAt(bestScore));
-#pragma unroll
-    for (int W = 0; W < MAXW; W++) {
-        if (32 * W >= stop) break;
-        for (int bb = max(slStart - 32 * W, 0); bb < 32; bb++) {
-            const int sl = 32 * W + bb;
-            if (sl >= stop) break;
-            const uint32_t h0 = __funnelshift_l(S[0][W + 1], S[0][W], bb), l0 = __funnelshift_l(S[1][W + 1], S[1][W], bb);
-            const uint32_t h1 = __funnelshift_l(S[0][W + 2], S[0][W + 1], bb),
-                           l1 = __funnelshift_l(S[1][W + 2], S[1][W + 1], bb);
-            const uint32_t d0 = (h0 ^ O[0][0]) | (l0 ^ O[1][0]), d1 = (h1 ^ O[0][1]) | (l1 ^ O[1][1]);
-            if (sl <= slFast) {
-                if (__popc(d0) + __popc(d1) >= tabMax) continue;
-            } else if (sl <= slFast1 && __popc(d0) >= tab63) {
-                continue;
-            }
-            // the reference's step
+    const int fastAll = __reduce_min_sync(lanes, slFast);    // every lane in the two-word tier up to here
+    const int fastAny = __reduce_max_sync(lanes, slFast);    // no lane in it past here
+    const int fast1All = __reduce_min_sync(lanes, slFast1);  // every lane in a word tier up to here
+    auto diff = [&](int bb, int i) {
+        return (__funnelshift_l(S[0][i + 1], S[0][i], bb) ^ O[0][i]) |
+               (__funnelshift_l(S[1][i + 1], S[1][i], bb) ^ O[1][i]);
+    };
+    int bb = LEFT ? 1 : 0;
+#pragma unroll 1
+    for (int base = 0; base < 32 * MAXW; base += 32, bb = 0) {
+        const int wStop = __reduce_max_sync(lanes, stop);
+        if (base >= wStop) break;
+        const int ge = min(32, wStop - base);
+        // the reference's step at shift base + bb
+        auto step = [&](int bb) {
+            const int sl = base + bb;
+            if (sl >= stop) return;
             const int ov = min(X - sl, Y);
             const int maxErr = min((int)maxErrTab[ov], bestScore - tb + 2 * ov);  // > 0 before `stop`
             const int parts = (ov + 31) >> 5;
             const uint32_t last = 0xffffffffu << ((parts << 5) - ov);
             const uint32_t mask0 = parts > 1 ? 0xffffffffu : last;
             const uint32_t mask1 = parts > 2 ? 0xffffffffu : (parts == 2 ? last : 0u);
-            int m = __popc(d0 & mask0) + __popc(d1 & mask1);
+            int m = __popc(diff(bb, 0) & mask0) + __popc(diff(bb, 1) & mask1);
             if (m < maxErr && parts > 2) {
 #pragma unroll
                 for (int i = 2; i < MAXW; i++) {
                     if (i >= parts || m >= maxErr) break;
-                    const uint32_t mask = i == parts - 1 ? last : 0xffffffffu;
-                    const uint32_t hi = __funnelshift_l(S[0][W + i + 1], S[0][W + i], bb);
-                    const uint32_t lo = __funnelshift_l(S[1][W + i + 1], S[1][W + i], bb);
-                    m += __popc(((hi ^ O[0][i]) | (lo ^ O[1][i])) & mask);
+                    m += __popc(diff(bb, i) & (i == parts - 1 ? last : 0xffffffffu));
                 }
             }
             if (m < maxErr) {
@@ -569,20 +509,53 @@ __device__ __forceinline__ void seq_scan_fast(const uint32_t (&S)[2][2 * MAXW], 
                     stop = min(stop, stopAt(bestScore));
                 }
             }
+        };
+        // shifts where the lanes' tiers differ: each lane tests its own
+        auto mixed = [&](int e) {
+            for (; bb < e; bb++) {
+                const int sl = base + bb;
+                const int m1 = __popc(diff(bb, 0));
+                if (sl <= slFast) {
+                    if (m1 + __popc(diff(bb, 1)) >= tabMax) continue;
+                } else if (sl <= slFast1 && m1 >= tab63) {
+                    continue;
+                }
+                step(bb);
+            }
+        };
+        for (const int e = min(ge, fastAll + 1 - base); bb < e; bb++)  // all lanes: two words
+            if (__popc(diff(bb, 0)) + __popc(diff(bb, 1)) < tabMax) step(bb);
+        mixed(min(ge, max(bb, fastAny + 1 - base)));
+        for (const int e = min(ge, fast1All + 1 - base); bb < e; bb++)  // all lanes: one word
+            if (__popc(diff(bb, 0)) < tab63) step(bb);
+        mixed(ge);
+#pragma unroll
+        for (int k = 0; k < MAXW; k++) {
+            S[0][k] = S[0][k + 1];
+            S[1][k] = S[1][k + 1];
         }
+        S[0][MAXW] = S[1][MAXW] = 0u;
     }
 }
 
+// Both directions for one orientation of the candidate (planes at cPlanes);
+// A and C are working copies that the scans consume.
 template <int MAXW>
-__device__ __forceinline__ AlnRes align_seq_fast(const uint32_t (&A)[2][2 * MAXW], const uint32_t (&C)[2][2 * MAXW],
-                                                 int La, int Lc, int minov, const int16_t* maxErrTab, int ovPos) {
+__device__ __forceinline__ AlnRes align_seq_fast(const uint32_t* __restrict__ aPlanes,
+                                                 const uint32_t* __restrict__ cPlanes, int wp, uint32_t (&A)[2][MAXW + 1],
+                                                 uint32_t (&C)[2][MAXW + 1], int La, int Lc, int minov,
+                                                 const int16_t* maxErrTab, int ovPos, unsigned lanes) {
     const int tb = La + Lc;
     const int tabMax = maxErrTab[min(La, Lc)];
     const int tab63 = maxErrTab[min(63, min(La, Lc))];
     int bestScore = tb, bestShift = -Lc;
-    seq_scan_fast<MAXW, false>(A, C, La, Lc, La - minov + 1, tb, maxErrTab, tabMax, tab63, ovPos, bestScore,
+    load_planes<MAXW>(A, aPlanes, wp);
+    load_planes<MAXW>(C, cPlanes, wp);
+    seq_scan_fast<MAXW, false>(A, C, La, Lc, La - minov + 1, tb, maxErrTab, tabMax, tab63, ovPos, lanes, bestScore,
                                bestShift);
-    seq_scan_fast<MAXW, true>(C, A, La, Lc, Lc - minov, tb, maxErrTab, tabMax, tab63, ovPos, bestScore, bestShift);
+    load_planes<MAXW>(A, aPlanes, wp);
+    seq_scan_fast<MAXW, true>(C, A, La, Lc, Lc - minov, tb, maxErrTab, tabMax, tab63, ovPos, lanes, bestScore,
+                              bestShift);
     AlnRes r;
     r.valid = bestShift != -Lc;
     const int cb = max(-bestShift, 0);
@@ -627,6 +600,7 @@ __global__ void __launch_bounds__(kLaneThreads, MAXW <= 5 ? 8 : 1) align_lane_ke
         }
         if (t0 >= total) return;
         const uint32_t t = t0 + threadIdx.x;
+        const unsigned lanes = __ballot_sync(kFull, t < total);  // the warp's lanes with a candidate
         if (t < total) {
             int lo = 0, hi = b.count;  // last anchor with uoff[a] <= t
             while (hi - lo > 1) {
@@ -641,13 +615,17 @@ __global__ void __launch_bounds__(kLaneThreads, MAXW <= 5 ? 8 : 1) align_lane_ke
             const uint32_t id = b.cand[slot];
             const int La = st.len[aid], Lc = st.len[id];
             const int wp = st.wp;
-            uint32_t A[2][2 * MAXW], C[2][2 * MAXW];
-            load_planes<MAXW>(A, st.hilo + aid * 4 * (uint64_t)wp, wp);
+            uint32_t A[2][MAXW + 1], C[2][MAXW + 1];
             const int minov = max(p.minOverlap, (int)__fmul_rn((float)La, p.minOverlapRatio));
-            load_planes<MAXW>(C, st.hilo + (uint64_t)id * 4 * wp, wp);
-            const AlnRes f = align_seq_fast<MAXW>(A, C, La, Lc, minov, maxErrTab, ovPos);
-            load_planes<MAXW>(C, st.hilo + (uint64_t)id * 4 * wp + 2 * wp, wp);
-            const AlnRes r = align_seq_fast<MAXW>(A, C, La, Lc, minov, maxErrTab, ovPos);
+            AlnRes f, r;
+#pragma unroll 1
+            for (int o = 0; o < 2; o++) {  // forward, then reverse complement
+                const AlnRes x = align_seq_fast<MAXW>(st.hilo + aid * 4 * (uint64_t)wp,
+                                                      st.hilo + (uint64_t)id * 4 * wp + 2 * wp * o, wp, A, C, La,
+                                                      Lc, minov, maxErrTab, ovPos, lanes);
+                if (o == 0) f = x;
+                else r = x;
+            }
             const int ori = choose_orientation(f, r, La, p.minOverlapRatio, p.minOverlap, p.orientMaxErrorRate);
             b.aln[slot] = pack_aln(ori == 2 ? r : f, ori);
         }
