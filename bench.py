@@ -394,7 +394,7 @@ def main():
                 "wall_seconds_timed": bl["wall"], "build_seconds": st1["seconds_build"],
                 "score": bl["score"], "stats": {k: st1[k] for k in ("raw_candidate_ids", "unique_candidates",
                                                                     "aligned_candidates", "msa_candidates",
-                                                                    "corrected_anchors", "hq_anchors", "table_keys",
+                                                                    "msa_builds", "corrected_anchors", "hq_anchors", "table_keys",
                                                                     "table_values", "learned_columns",
                                                                     "learned_corrections")}}
         print(json.dumps(line), flush=True)

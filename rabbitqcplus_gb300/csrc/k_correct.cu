@@ -1042,8 +1042,10 @@ __device__ __forceinline__ int base_index(char c) { return c == 'A' ? 0 : c == '
 // position the four counts and four weights; rows are added one at a time
 // (anchor, then the kept candidates in list order) with the lanes over the
 // row's positions, so every column receives its additions in the reference's
-// order.  Candidate metadata of 32 rows is held one row per lane and the rows'
-// 2-bit words are staged in shared memory per chunk.
+// order.  Lane l owns the columns c with c % 32 == l in every pass (rows,
+// consensus, properties, decision), so consecutive rows need no warp sync.
+// The 2-bit words and the metadata of 32 rows are staged in shared memory per
+// chunk.
 //
 // `sm` is the warp's own slice of shared memory (msa_warp_slice_bytes), `qw`
 // the block's quality weights.
@@ -1055,6 +1057,7 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
     uint32_t* cnt = reinterpret_cast<uint32_t*>(w + 4 * lp);     // [4][lp]
     float* sup = reinterpret_cast<float*>(cnt + 4 * lp);         // [lp]
     uint32_t* stage = reinterpret_cast<uint32_t*>(sup + lp);     // [32][pitch]
+    int4* meta = reinterpret_cast<int4*>(stage + 32 * st.pitch);  // [32]: shift, len | orient << 16, weight, id
     const uint64_t aid = first + (uint64_t)a;
     const uint64_t oi = (first - out_first(b)) + (uint64_t)a;   // output row
     const uint32_t nf = b.nfinal[a];
@@ -1106,19 +1109,20 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
                 const uint32_t rid = __shfl_sync(kFull, mid, r);
                 if (idx < rows * pitch) stage[idx] = st.enc[(uint64_t)rid * pitch + (idx - r * pitch)];
             }
+            meta[lane] = make_int4(mshift, mlen | (int)(mo << 16), __float_as_int(mw), (int)mid);
             __syncwarp();
             for (int r = 0; r < rows; r++) {
-                const uint32_t o = __shfl_sync(kFull, mo, r);
+                const int4 md = meta[r];
+                const uint32_t o = (uint32_t)md.y >> 16;
                 if (o & kRm) continue;
-                const int shift = __shfl_sync(kFull, mshift, r);
-                const int len = __shfl_sync(kFull, mlen, r);
-                const float weight = __shfl_sync(kFull, mw, r);
+                const int shift = md.x, len = md.y & 0xffff;
+                const float weight = __int_as_float(md.z);
                 const bool rc = o == 2;
                 const uint32_t* e = stage + r * pitch;
                 const uint8_t* q = nullptr;
-                if (p.useQuality) q = st.qual + (uint64_t)__shfl_sync(kFull, mid, r) * st.lmax;
+                if (p.useQuality) q = st.qual + (uint64_t)(uint32_t)md.w * st.lmax;
                 const int c0 = max(shift, 0), c1 = min(La, shift + len);  // overlap with the anchor
-                for (int c = c0 + lane; c < c1; c += 32) {
+                for (int c = c0 + ((lane - c0) & 31); c < c1; c += 32) {  // this lane's columns
                     const int pos = c - shift;
                     const int sp = rc ? len - 1 - pos : pos;
                     uint32_t bb = get2bit(e, sp);
@@ -1127,8 +1131,8 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
                     w[bb * lp + c] = __fadd_rn(w[bb * lp + c], wt);
                     cnt[bb * lp + c]++;
                 }
-                __syncwarp();
             }
+            __syncwarp();  // the next chunk overwrites the staged rows
         }
         builds++;
         if (iter == 5 || nActive == 0) break;
@@ -1337,7 +1341,7 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
 
 // Bytes of shared memory one warp of msa_warp_kernel works in.
 __host__ __device__ inline size_t msa_warp_slice_bytes(int lp, int pitch) {
-    return (size_t)lp * (9 * sizeof(float)) + (size_t)32 * pitch * sizeof(uint32_t);
+    return (size_t)lp * (9 * sizeof(float)) + (size_t)32 * pitch * sizeof(uint32_t) + 32 * sizeof(int4);
 }
 
 // `warps` warps per block, each on its own anchors.  Plain form: anchor
