@@ -1019,9 +1019,11 @@ struct ColInfo {
     float consW, colW;
 };
 
-__device__ __forceinline__ ColInfo col_info(const float* w, int cp, int c) {
+// wc[q * cp + c]: weight bits (x) and count (y) of base q in column c
+__device__ __forceinline__ ColInfo col_info(const uint2* wc, int cp, int c) {
     ColInfo r;
-    const float wA = w[c], wC = w[cp + c], wG = w[2 * cp + c], wT = w[3 * cp + c];
+    const float wA = __uint_as_float(wc[c].x), wC = __uint_as_float(wc[cp + c].x),
+                wG = __uint_as_float(wc[2 * cp + c].x), wT = __uint_as_float(wc[3 * cp + c].x);
     r.cons = 'A';
     r.consW = wA;
     if (wC > r.consW) { r.cons = 'C'; r.consW = wC; }
@@ -1039,7 +1041,8 @@ __device__ __forceinline__ int base_index(char c) { return c == 'A' ? 0 : c == '
 // properties and both decisions -- lies in the anchor's columns, so only the
 // part of each row that overlaps the anchor is accumulated, in anchor
 // coordinates (column = anchor position).  Shared memory holds per anchor
-// position the four counts and four weights; rows are added one at a time
+// position and base the weight and the count side by side (one 8-byte
+// access per addition); rows are added one at a time
 // (anchor, then the kept candidates in list order) with the lanes over the
 // row's positions, so every column receives its additions in the reference's
 // order.  Lane l owns the columns c with c % 32 == l in every pass (rows,
@@ -1053,9 +1056,8 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
                                              const uint32_t* __restrict__ rawOff, int lp, int a, uint64_t first,
                                              unsigned char* sm, const float* qw) {
     const int lane = (int)lane_id();
-    float* w = reinterpret_cast<float*>(sm);                     // [4][lp]
-    uint32_t* cnt = reinterpret_cast<uint32_t*>(w + 4 * lp);     // [4][lp]
-    float* sup = reinterpret_cast<float*>(cnt + 4 * lp);         // [lp]
+    uint2* wc = reinterpret_cast<uint2*>(sm);                    // [4][lp]: weight bits, count
+    float* sup = reinterpret_cast<float*>(wc + 4 * lp);          // [lp]
     uint32_t* stage = reinterpret_cast<uint32_t*>(sup + lp);     // [32][pitch]
     int4* meta = reinterpret_cast<int4*>(stage + 32 * st.pitch);  // [32]: shift, len | orient << 16, weight, id
     const uint64_t aid = first + (uint64_t)a;
@@ -1072,7 +1074,9 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
     const uint32_t* aenc = st.enc + aid * (uint64_t)pitch;
     const uint8_t* aq = p.useQuality ? st.qual + aid * (uint64_t)st.lmax : nullptr;
     constexpr uint8_t kRm = 0x80;
-    auto covAt = [&](int c) { return (int)(cnt[c] + cnt[lp + c] + cnt[2 * lp + c] + cnt[3 * lp + c]); };
+    auto wAt = [&](int q, int c) { return __uint_as_float(wc[q * lp + c].x); };
+    auto cntAt = [&](int q, int c) { return wc[q * lp + c].y; };
+    auto covAt = [&](int c) { return (int)(cntAt(0, c) + cntAt(1, c) + cntAt(2, c) + cntAt(3, c)); };
 
     int nActive = (int)nf, builds = 0;
     for (int iter = 0;; iter++) {
@@ -1085,8 +1089,8 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
             const float wt = p.useQuality ? __fmul_rn(1.0f, qw[aq[pos]]) : 1.0f;
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                w[q * lp + pos] = (uint32_t)q == bb ? __fadd_rn(0.0f, wt) : 0.0f;
-                cnt[q * lp + pos] = (uint32_t)q == bb ? 1u : 0u;
+                wc[q * lp + pos] = (uint32_t)q == bb ? make_uint2(__float_as_uint(__fadd_rn(0.0f, wt)), 1u)
+                                                     : make_uint2(__float_as_uint(0.0f), 0u);
             }
         }
         __syncwarp();
@@ -1122,14 +1126,19 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
                 const uint8_t* q = nullptr;
                 if (p.useQuality) q = st.qual + (uint64_t)(uint32_t)md.w * st.lmax;
                 const int c0 = max(shift, 0), c1 = min(La, shift + len);  // overlap with the anchor
-                for (int c = c0 + ((lane - c0) & 31); c < c1; c += 32) {  // this lane's columns
-                    const int pos = c - shift;
-                    const int sp = rc ? len - 1 - pos : pos;
-                    uint32_t bb = get2bit(e, sp);
-                    if (rc) bb = 3u - bb;
+                int c = c0 + ((lane - c0) & 31);                           // this lane's first column
+                // the row position moves by 32 per column step of the lane, so
+                // its word moves by 2 and its bit offset stays
+                int sp = rc ? len - 1 - (c - shift) : c - shift;
+                const int dsp = rc ? -32 : 32, dwi = rc ? -2 : 2;
+                const uint32_t sh = 30u - 2u * (uint32_t)(sp & 15), flip = rc ? 3u : 0u;
+                for (int wi = sp >> 4; c < c1; c += 32, wi += dwi, sp += dsp) {
+                    const uint32_t bb = ((e[wi] >> sh) & 3u) ^ flip;
                     const float wt = p.useQuality ? __fmul_rn(weight, qw[q[sp]]) : weight;
-                    w[bb * lp + c] = __fadd_rn(w[bb * lp + c], wt);
-                    cnt[bb * lp + c]++;
+                    uint2 v = wc[bb * lp + c];
+                    v.x = __float_as_uint(__fadd_rn(__uint_as_float(v.x), wt));
+                    v.y++;
+                    wc[bb * lp + c] = v;
                 }
             }
             __syncwarp();  // the next chunk overwrites the staged rows
@@ -1140,11 +1149,11 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
         bool mism = false;
         int firstSig = 0x7fffffff;
         for (int c = lane; c < La; c += 32) {
-            const ColInfo ci = col_info(w, lp, c);
+            const ColInfo ci = col_info(wc, lp, c);
             mism |= ci.cons != "ACGT"[get2bit(aenc, c)];
             const int cidx = base_index(ci.cons);
             bool sig = false;
-            for (int i = 0; i < 4; i++) sig |= (i != cidx && p.significantCount <= (int)cnt[i * lp + c]);
+            for (int i = 0; i < 4; i++) sig |= (i != cidx && p.significantCount <= (int)cntAt(i, c));
             if (sig && c < firstSig) firstSig = c;
         }
         if (!__any_sync(kFull, mism)) break;
@@ -1152,11 +1161,11 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
         if (col == 0x7fffffff) break;
         int found;
         {
-            const ColInfo ci = col_info(w, lp, col);
+            const ColInfo ci = col_info(wc, lp, col);
             const int cidx = base_index(ci.cons);
             found = -1;
             for (int i = 0; i < 4; i++)
-                if (i != cidx && p.significantCount <= (int)cnt[i * lp + col]) found = i;
+                if (i != cidx && p.significantCount <= (int)cntAt(i, col)) found = i;
         }
         const uint32_t orig = get2bit(aenc, col);
         const bool keepMatching = orig == (uint32_t)found;
@@ -1191,7 +1200,7 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
     float mins = 3.402823466e+38f;
     int minc = 0x7fffffff, maxc = -1;
     for (int c = lane; c < La; c += 32) {
-        const ColInfo ci = col_info(w, lp, c);
+        const ColInfo ci = col_info(wc, lp, c);
         const float s = __fdiv_rn(ci.consW, ci.colW);
         sup[c] = s;
         mins = fminf(mins, s);
@@ -1234,8 +1243,8 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
     for (int c = lane; c < La; c += 32) {
         const uint32_t ab = get2bit(aenc, c);
         const char orig = "ACGT"[ab];
-        const ColInfo ci = col_info(w, lp, c);
-        const int origCov = (int)cnt[ab * lp + c];
+        const ColInfo ci = col_info(wc, lp, c);
+        const int origCov = (int)cntAt(ab, c);
         char r;
         if (forest) {
             // correctAnchorClf (include/corrector.hpp:1448-1472), features of
@@ -1243,9 +1252,9 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
             r = ci.cons;
             if (!hq && r != orig) {
                 const int ci_ = base_index(ci.cons);
-                const float wCons = w[ci_ * lp + c];
-                const float nCons = (float)cnt[ci_ * lp + c];
-                const float wOrig = w[ab * lp + c];
+                const float wCons = wAt(ci_, c);
+                const float nCons = (float)cntAt(ci_, c);
+                const float wOrig = wAt(ab, c);
                 const float cv = (float)covAt(c);
                 const float oc = (float)origCov;
                 const float ec = p.estimatedCoverage;
@@ -1268,7 +1277,7 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
     // anchor's base, with its features; the classifier then replaces the
     // decision written above (the fallback) where it is confident.
     int nd = 0;
-    for (int c = lane; c < La; c += 32) nd += col_info(w, lp, c).cons != "ACGT"[get2bit(aenc, c)];
+    for (int c = lane; c < La; c += 32) nd += col_info(wc, lp, c).cons != "ACGT"[get2bit(aenc, c)];
     nd = __reduce_add_sync(kFull, nd);
     const float ec = p.estimatedCoverage;
     const float invLa = __fdiv_rn(1.0f, (float)La);
@@ -1279,7 +1288,7 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
         uint32_t ab = 0;
         if (c < La) {
             ab = get2bit(aenc, c);
-            ci = col_info(w, lp, c);
+            ci = col_info(wc, lp, c);
             rec = ci.cons != "ACGT"[ab];
         }
         const unsigned m = __ballot_sync(kFull, rec);
@@ -1292,8 +1301,8 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
         float n4[4], w4[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            n4[q] = (float)cnt[q * lp + c];
-            w4[q] = w[q * lp + c];
+            n4[q] = (float)cntAt(q, c);
+            w4[q] = wAt(q, c);
         }
         auto pick = [](const float (&v)[4], uint32_t i) {
             return i == 0 ? v[0] : i == 1 ? v[1] : i == 2 ? v[2] : v[3];
