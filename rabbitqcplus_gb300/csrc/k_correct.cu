@@ -1078,22 +1078,10 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
     auto cntAt = [&](int q, int c) { return wc[q * lp + c].y; };
     auto covAt = [&](int c) { return (int)(cntAt(0, c) + cntAt(1, c) + cntAt(2, c) + cntAt(3, c)); };
 
-    int nActive = (int)nf, builds = 0;
-    for (int iter = 0;; iter++) {
-        int act = 0;
-        for (uint32_t j = lane; j < nf; j += 32) act += !(b.forient[base + j] & kRm);
-        nActive = __reduce_add_sync(kFull, act);
-        // anchor row (weight 1 times the quality weight) initialises the columns
-        for (int pos = lane; pos < La; pos += 32) {
-            const uint32_t bb = get2bit(aenc, pos);
-            const float wt = p.useQuality ? __fmul_rn(1.0f, qw[aq[pos]]) : 1.0f;
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                wc[q * lp + pos] = (uint32_t)q == bb ? make_uint2(__float_as_uint(__fadd_rn(0.0f, wt)), 1u)
-                                                     : make_uint2(__float_as_uint(0.0f), 0u);
-            }
-        }
-        __syncwarp();
+    // Rows are added (sign +1: every row still in the MSA, after the anchor
+    // row) or taken out again (sign -1: the rows just removed, marked kNew).
+    constexpr uint8_t kNew = 0x40;
+    auto rowsPass = [&](bool add) {
         for (uint32_t j0 = 0; j0 < nf; j0 += 32) {
             const uint32_t jr = j0 + lane;
             const int rows = (int)min(32u, nf - j0);
@@ -1107,21 +1095,25 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
                 mid = b.fid[base + jr];
                 mw = b.fweight[base + jr];
             }
+            const bool sel = jr < nf && (add ? !(mo & kRm) : (mo & kNew) != 0);
+            const unsigned selRows = __ballot_sync(kFull, sel);
+            if (!selRows) continue;
+            if (!add && sel) b.forient[base + jr] = (uint8_t)(mo & ~kNew);
             for (int i0 = 0; i0 < rows * pitch; i0 += 32) {  // warp-uniform trip count
                 const int idx = i0 + lane;
                 const int r = min(idx / pitch, rows - 1);
                 const uint32_t rid = __shfl_sync(kFull, mid, r);
-                if (idx < rows * pitch) stage[idx] = st.enc[(uint64_t)rid * pitch + (idx - r * pitch)];
+                if (idx < rows * pitch && ((selRows >> r) & 1u))
+                    stage[idx] = st.enc[(uint64_t)rid * pitch + (idx - r * pitch)];
             }
-            meta[lane] = make_int4(mshift, mlen | (int)(mo << 16), __float_as_int(mw), (int)mid);
+            meta[lane] = make_int4(mshift, mlen | (int)((mo & 3u) << 16), __float_as_int(mw), (int)mid);
             __syncwarp();
             for (int r = 0; r < rows; r++) {
+                if (!((selRows >> r) & 1u)) continue;
                 const int4 md = meta[r];
-                const uint32_t o = (uint32_t)md.y >> 16;
-                if (o & kRm) continue;
+                const bool rc = ((uint32_t)md.y >> 16) == 2;
                 const int shift = md.x, len = md.y & 0xffff;
                 const float weight = __int_as_float(md.z);
-                const bool rc = o == 2;
                 const uint32_t* e = stage + r * pitch;
                 const uint8_t* q = nullptr;
                 if (p.useQuality) q = st.qual + (uint64_t)(uint32_t)md.w * st.lmax;
@@ -1136,15 +1128,76 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
                     const uint32_t bb = ((e[wi] >> sh) & 3u) ^ flip;
                     const float wt = p.useQuality ? __fmul_rn(weight, qw[q[sp]]) : weight;
                     uint2 v = wc[bb * lp + c];
-                    v.x = __float_as_uint(__fadd_rn(__uint_as_float(v.x), wt));
-                    v.y++;
+                    if (add) {
+                        v.x = __float_as_uint(__fadd_rn(__uint_as_float(v.x), wt));
+                        v.y++;
+                    } else {
+                        v.x = __float_as_uint(__fsub_rn(__uint_as_float(v.x), wt));
+                        v.y--;
+                    }
                     wc[bb * lp + c] = v;
                 }
             }
             __syncwarp();  // the next chunk overwrites the staged rows
         }
+    };
+    // The MSA of the rows still in it, built as the reference builds it: the
+    // anchor row (weight 1 times the quality weight), then the rows in order.
+    auto build = [&]() {
+        for (int pos = lane; pos < La; pos += 32) {
+            const uint32_t bb = get2bit(aenc, pos);
+            const float wt = p.useQuality ? __fmul_rn(1.0f, qw[aq[pos]]) : 1.0f;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                wc[q * lp + pos] = (uint32_t)q == bb ? make_uint2(__float_as_uint(__fadd_rn(0.0f, wt)), 1u)
+                                                     : make_uint2(__float_as_uint(0.0f), 0u);
+            }
+        }
+        __syncwarp();
+        rowsPass(true);
+    };
+
+    // Region refinement (src/msa.cpp:532-734 and the loop around it in
+    // include/corrector.hpp): up to five rounds, each removing the rows that
+    // differ from the anchor at one significant column and rebuilding.  A
+    // round here subtracts the removed rows instead of rebuilding: counts are
+    // then exact, weights within E_c = (3 nf + 4) 2^-24 S_c of the rebuilt
+    // ones (S_c = column c's total weight in the first build; every partial
+    // sum and difference stays below it).  A round only reads the consensus
+    // (the largest weight) and the counts, so it sees what the rebuilt MSA
+    // shows wherever the two largest weights of every column differ by more
+    // than 2 E_c; otherwise the MSA is rebuilt first.  The MSA that the
+    // decision reads is always a full build.
+    int nActive = 0, builds = 0;
+    for (uint32_t j = lane; j < nf; j += 32) nActive += !(b.forient[base + j] & kRm);
+    nActive = __reduce_add_sync(kFull, nActive);
+    bool exact = true;
+    build();
+    for (int c = lane; c < La; c += 32) {  // S_c, kept in `sup` until the properties
+        const ColInfo ci = col_info(wc, lp, c);
+        sup[c] = ci.colW;
+    }
+    const float tol = __fmul_rn(2.5f * 5.9604645e-8f, (float)(3 * nf + 4));  // 2 E_c / S_c with slack
+    for (int iter = 0;; iter++) {
         builds++;
         if (iter == 5 || nActive == 0) break;
+        if (!exact) {
+            bool close = false;
+            for (int c = lane; c < La; c += 32) {
+                float t1 = 0.0f, t2 = 0.0f;  // the two largest weights
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float v = wAt(q, c);
+                    t2 = fmaxf(t2, fminf(t1, v));
+                    t1 = fmaxf(t1, v);
+                }
+                close |= !(__fsub_rn(t1, t2) > __fmul_rn(tol, sup[c]));
+            }
+            if (__any_sync(kFull, close)) {
+                build();
+                exact = true;
+            }
+        }
         // findCandidatesOfDifferentRegion (src/msa.cpp:532-734), in anchor coordinates
         bool mism = false;
         int firstSig = 0x7fffffff;
@@ -1190,12 +1243,18 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
         // a veto (or nothing to remove) leaves the MSA as it is; the
         // reference then rebuilds the same MSA and reaches the same decision
         if (__any_sync(kFull, veto) || !__any_sync(kFull, any)) break;
+        int act = 0;
         for (uint32_t j = lane; j < nf; j += 32) {
             const uint8_t o = b.forient[base + j];
-            if (!(o & kRm) && differs(j)) b.forient[base + j] = o | kRm;
+            if (!(o & kRm) && differs(j)) b.forient[base + j] = o | kRm | kNew;
+            else act += !(o & kRm);
         }
+        nActive = __reduce_add_sync(kFull, act);
         __syncwarp();
+        rowsPass(false);
+        exact = false;
     }
+    if (!exact) build();
     // getMSAProperties (src/msa.cpp:304-376) and the decision
     float mins = 3.402823466e+38f;
     int minc = 0x7fffffff, maxc = -1;
