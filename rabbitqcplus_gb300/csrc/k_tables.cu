@@ -209,10 +209,11 @@ constexpr int kGatherThreads = 128;
 
 // One block per anchor: the union of the anchor's buckets, ascending, without
 // the anchor itself (and without ambiguous reads if requested).  The raw ids
-// go into a shared-memory hash set (duplicates vanish on insert); the unique
-// ids are then put in ascending order by rank (or a bitonic sort when there
-// are many).  rawOff = exclusive scan of the raw counts; the table holds
-// tableSize >= 2 * raw slots.
+// go into a shared-memory hash set (duplicates vanish on insert, the first
+// copy of an id joins the unique list); the unique ids are then put in
+// ascending order by rank (or a bitonic sort when there are many).  rawOff =
+// exclusive scan of the raw counts; the table holds tableSize >= 2 * raw
+// slots.
 // Raw id range (offset, count) of anchor a.  In the batched form it comes
 // from the range scan; the small-table pass also writes the offset into
 // b.rawCount for the later stages.
@@ -233,14 +234,17 @@ __device__ __forceinline__ uint2 gather_range(const BatchArg& b, const uint32_t*
 
 // The union of anchor a's buckets (all threads of the block), raw > 0; the
 // shared-memory table holds tableSize >= 2 * raw slots and a list of half that.
+// Groups of 16 threads take the maps in turn (a bucket's first 16 ids with one
+// load per thread, all maps' loads issued before the inserts); an id joins the
+// unique list when its first copy enters the hash set.
 __device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params& p, const BatchArg& b, int a,
                            uint64_t aid, uint32_t off, uint32_t raw, uint32_t* table, int tableSize, uint2* rng,
-                           uint32_t* pre, uint32_t* nUniqueS) {
+                           uint32_t* nUniqueS) {
     uint32_t* list = table + tableSize;
     uint32_t& nUnique = *nUniqueS;
     const int tid = threadIdx.x;
     uint32_t T = 64;
-    while (T < 2 * raw) T <<= 1;
+    while (T < raw + raw / 2) T <<= 1;  // at most two thirds full
     const uint32_t mask = T - 1;
     if (tid < tb.nmaps) {
         if (b.rangeOff) {
@@ -255,51 +259,34 @@ __device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params
     for (uint32_t i = tid; i < T; i += kGatherThreads) table[i] = 0xffffffffu;
     if (tid == 0) nUnique = 0;
     __syncthreads();
-    if (tid == 0) {
-        uint32_t acc = 0;
-        for (int m = 0; m < tb.nmaps; m++) {
-            pre[m] = acc;
-            acc += rng[m].y;
-        }
-        pre[tb.nmaps] = acc;
-    }
-    __syncthreads();
-    // every thread loads its raw ids first (independent loads), then inserts them
-    constexpr int kPer = 8;
-    for (uint32_t i0 = 0; i0 < raw; i0 += kGatherThreads * kPer) {
-        uint32_t vals[kPer];
-#pragma unroll
-        for (int k = 0; k < kPer; k++) {
-            const uint32_t i = i0 + (uint32_t)k * kGatherThreads + tid;
-            vals[k] = 0xffffffffu;
-            if (i < raw) {
-                int lo = 0, hi = tb.nmaps;  // last map with pre[m] <= i
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (pre[mid] <= i) lo = mid;
-                    else hi = mid;
-                }
-                vals[k] = tb.values[lo][rng[lo].x + (i - pre[lo])];
+    auto insert = [&](uint32_t v) {
+        uint32_t h = (v * 0x9E3779B1u) & mask;
+        for (uint32_t probe = 0; probe < T; probe++) {
+            const uint32_t old = atomicCAS(&table[h], 0xffffffffu, v);
+            if (old == 0xffffffffu) {  // the first copy of v
+                if ((uint64_t)v != aid && !(p.excludeAmbiguous && st.ambig[v])) list[atomicAdd(&nUnique, 1u)] = v;
+                return;
             }
+            if (old == v) return;
+            h = (h + 1) & mask;
         }
+    };
+    constexpr int kGroup = 16, kGroups = kGatherThreads / kGroup, kMapsPer = (kMaxMaps + kGroups - 1) / kGroups;
+    const int g = tid / kGroup, gl = tid % kGroup;
+    uint32_t vals[kMapsPer];
 #pragma unroll
-        for (int k = 0; k < kPer; k++) {
-            const uint32_t v = vals[k];
-            if (v == 0xffffffffu) continue;
-            uint32_t h = (v * 0x9E3779B1u) & mask;
-            for (uint32_t probe = 0; probe < T; probe++) {
-                const uint32_t old = atomicCAS(&table[h], 0xffffffffu, v);
-                if (old == 0xffffffffu || old == v) break;
-                h = (h + 1) & mask;
-            }
-        }
+    for (int k = 0; k < kMapsPer; k++) {
+        const int m = g + k * kGroups;
+        vals[k] = 0xffffffffu;
+        if (m < tb.nmaps && (uint32_t)gl < rng[m].y) vals[k] = tb.values[m][rng[m].x + gl];
     }
-    __syncthreads();
-    for (uint32_t i = tid; i < T; i += kGatherThreads) {
-        const uint32_t v = table[i];
-        if (v == 0xffffffffu || (uint64_t)v == aid) continue;
-        if (p.excludeAmbiguous && st.ambig[v]) continue;
-        list[atomicAdd(&nUnique, 1u)] = v;
+#pragma unroll
+    for (int k = 0; k < kMapsPer; k++)
+        if (vals[k] != 0xffffffffu) insert(vals[k]);
+    for (int k = 0; k < kMapsPer; k++) {  // ids past a bucket's first 16
+        const int m = g + k * kGroups;
+        if (m >= tb.nmaps) break;
+        for (uint32_t i = kGroup + gl; i < rng[m].y; i += kGroup) insert(tb.values[m][rng[m].x + i]);
     }
     __syncthreads();
     const uint32_t U = nUnique;
@@ -352,7 +339,6 @@ __global__ void __launch_bounds__(kGatherThreads) gather_unique_kernel(StoreArg 
                                                                        uint32_t* bigList, unsigned int* bigCount) {
     extern __shared__ uint32_t table[];  // [tableSize], then list[tableSize / 2]
     __shared__ uint2 rng[kMaxMaps];
-    __shared__ uint32_t pre[kMaxMaps + 1];
     __shared__ uint32_t nUnique;
     const int a = blockIdx.x;
     const uint64_t first = batch_first(b);
@@ -365,7 +351,7 @@ __global__ void __launch_bounds__(kGatherThreads) gather_unique_kernel(StoreArg 
         if (threadIdx.x == 0) bigList[atomicAdd(bigCount, 1u)] = (uint32_t)a;
         return;
     }
-    gather_one(st, tb, p, b, a, first + (uint64_t)a, r.x, r.y, table, tableSize, rng, pre, &nUnique);
+    gather_one(st, tb, p, b, a, first + (uint64_t)a, r.x, r.y, table, tableSize, rng, &nUnique);
 }
 
 // Persistent blocks over the deferred anchors of gather_unique_kernel.
@@ -375,14 +361,13 @@ __global__ void __launch_bounds__(kGatherThreads) gather_big_kernel(StoreArg st,
                                                                     const unsigned int* bigCount) {
     extern __shared__ uint32_t table[];
     __shared__ uint2 rng[kMaxMaps];
-    __shared__ uint32_t pre[kMaxMaps + 1];
     __shared__ uint32_t nUnique;
     const uint64_t first = batch_first(b);
     const unsigned int n = *bigCount;
     for (unsigned int i = blockIdx.x; i < n; i += gridDim.x) {
         const int a = (int)bigList[i];
         const uint2 r = gather_range(b, rawOff, a, first, false);
-        gather_one(st, tb, p, b, a, first + (uint64_t)a, r.x, r.y, table, tableSize, rng, pre, &nUnique);
+        gather_one(st, tb, p, b, a, first + (uint64_t)a, r.x, r.y, table, tableSize, rng, &nUnique);
         __syncthreads();  // the next anchor reuses the shared arrays
     }
 }
