@@ -48,7 +48,9 @@ import numpy as np  # noqa: E402
 from rabbitqcplus_gb300 import capi, learned, sim  # noqa: E402
 
 METRIC = "corrected reads/s on 1 GB300: plain vs batched+learned, at equal TP/FP vs truth"
-ALIGN_DRAM_BYTES_PER_CANDIDATE = 83.30e6 / 3.777e6
+# DRAM bytes (read + write) of align_lane_kernel per candidate, measured by ncu on one
+# 65536-anchor launch of this workload at 2 Mbp: 91.59 MB for 3.777M candidates
+ALIGN_DRAM_BYTES_PER_CANDIDATE = 91.59e6 / 3.777e6
 UNIT = "reads/s"
 
 
@@ -353,7 +355,7 @@ def main():
             "algorithmic_bytes_per_launch": bytes_launch,
             "avg_launch_ms": dur * 1e3,
             "stage_seconds_per_step": {k: v / args.steps for k, v in stages.items()},
-            "note": "integer-pipe bound (ALU pipe 71% active in ncu); the fraction is of the HBM roofline, and "
+            "note": "integer-pipe bound (ALU pipe 75% active in ncu); the fraction is of the HBM roofline, and "
                     "traffic (measured DRAM bytes) is below the algorithmic bytes because candidate planes "
                     "shared between anchors hit in L2"}
 
