@@ -1013,17 +1013,29 @@ __global__ void __launch_bounds__(1024) msa_correct_kernel(StoreArg st, Params p
 
 // ---------------------------------------------------------------- MSA, warp per anchor
 
-// Column statistics derived from a column's weights (src/msa.cpp:135-157).
+// A column's weights and counts and the statistics derived from them
+// (src/msa.cpp:135-157).
 struct ColInfo {
+    float w[4];
+    uint32_t n[4];
     char cons;
     float consW, colW;
+    __device__ float wOf(uint32_t i) const { return i == 0 ? w[0] : i == 1 ? w[1] : i == 2 ? w[2] : w[3]; }
+    __device__ uint32_t nOf(uint32_t i) const { return i == 0 ? n[0] : i == 1 ? n[1] : i == 2 ? n[2] : n[3]; }
+    __device__ int cov() const { return (int)(n[0] + n[1] + n[2] + n[3]); }
 };
 
-// wc[q * cp + c]: weight bits (x) and count (y) of base q in column c
+// wc[q * cp + c]: weight bits (x) and count (y) of base q in column c, read
+// as one 8-byte entry per base
 __device__ __forceinline__ ColInfo col_info(const uint2* wc, int cp, int c) {
     ColInfo r;
-    const float wA = __uint_as_float(wc[c].x), wC = __uint_as_float(wc[cp + c].x),
-                wG = __uint_as_float(wc[2 * cp + c].x), wT = __uint_as_float(wc[3 * cp + c].x);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const uint2 v = wc[q * cp + c];
+        r.w[q] = __uint_as_float(v.x);
+        r.n[q] = v.y;
+    }
+    const float wA = r.w[0], wC = r.w[1], wG = r.w[2], wT = r.w[3];
     r.cons = 'A';
     r.consW = wA;
     if (wC > r.consW) { r.cons = 'C'; r.consW = wC; }
@@ -1074,9 +1086,6 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
     const uint32_t* aenc = st.enc + aid * (uint64_t)pitch;
     const uint8_t* aq = p.useQuality ? st.qual + aid * (uint64_t)st.lmax : nullptr;
     constexpr uint8_t kRm = 0x80;
-    auto wAt = [&](int q, int c) { return __uint_as_float(wc[q * lp + c].x); };
-    auto cntAt = [&](int q, int c) { return wc[q * lp + c].y; };
-    auto covAt = [&](int c) { return (int)(cntAt(0, c) + cntAt(1, c) + cntAt(2, c) + cntAt(3, c)); };
 
     // Rows are added (sign +1: every row still in the MSA, after the anchor
     // row) or taken out again (sign -1: the rows just removed, marked kNew).
@@ -1185,9 +1194,10 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
             bool close = false;
             for (int c = lane; c < La; c += 32) {
                 float t1 = 0.0f, t2 = 0.0f;  // the two largest weights
+                const ColInfo ci = col_info(wc, lp, c);
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    const float v = wAt(q, c);
+                    const float v = ci.w[q];
                     t2 = fmaxf(t2, fminf(t1, v));
                     t1 = fmaxf(t1, v);
                 }
@@ -1206,7 +1216,8 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
             mism |= ci.cons != "ACGT"[get2bit(aenc, c)];
             const int cidx = base_index(ci.cons);
             bool sig = false;
-            for (int i = 0; i < 4; i++) sig |= (i != cidx && p.significantCount <= (int)cntAt(i, c));
+#pragma unroll
+            for (int i = 0; i < 4; i++) sig |= (i != cidx && p.significantCount <= (int)ci.n[i]);
             if (sig && c < firstSig) firstSig = c;
         }
         if (!__any_sync(kFull, mism)) break;
@@ -1217,8 +1228,9 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
             const ColInfo ci = col_info(wc, lp, col);
             const int cidx = base_index(ci.cons);
             found = -1;
+#pragma unroll
             for (int i = 0; i < 4; i++)
-                if (i != cidx && p.significantCount <= (int)cntAt(i, col)) found = i;
+                if (i != cidx && p.significantCount <= (int)ci.n[i]) found = i;
         }
         const uint32_t orig = get2bit(aenc, col);
         const bool keepMatching = orig == (uint32_t)found;
@@ -1263,7 +1275,7 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
         const float s = __fdiv_rn(ci.consW, ci.colW);
         sup[c] = s;
         mins = fminf(mins, s);
-        const int cv = covAt(c);
+        const int cv = ci.cov();
         minc = min(minc, cv);
         maxc = max(maxc, cv);
     }
@@ -1303,7 +1315,7 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
         const uint32_t ab = get2bit(aenc, c);
         const char orig = "ACGT"[ab];
         const ColInfo ci = col_info(wc, lp, c);
-        const int origCov = (int)cntAt(ab, c);
+        const int origCov = (int)ci.nOf(ab);
         char r;
         if (forest) {
             // correctAnchorClf (include/corrector.hpp:1448-1472), features of
@@ -1311,10 +1323,10 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
             r = ci.cons;
             if (!hq && r != orig) {
                 const int ci_ = base_index(ci.cons);
-                const float wCons = wAt(ci_, c);
-                const float nCons = (float)cntAt(ci_, c);
-                const float wOrig = wAt(ab, c);
-                const float cv = (float)covAt(c);
+                const float wCons = ci.wOf((uint32_t)ci_);
+                const float nCons = (float)ci.nOf((uint32_t)ci_);
+                const float wOrig = ci.wOf(ab);
+                const float cv = (float)ci.cov();
                 const float oc = (float)origCov;
                 const float ec = p.estimatedCoverage;
                 const float f[13] = {__fdiv_rn(oc, cv),      __fdiv_rn(wOrig, ci.colW), __fdiv_rn(wOrig, oc),
@@ -1360,8 +1372,8 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
         float n4[4], w4[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            n4[q] = (float)cntAt(q, c);
-            w4[q] = wAt(q, c);
+            n4[q] = (float)ci.n[q];
+            w4[q] = ci.w[q];
         }
         auto pick = [](const float (&v)[4], uint32_t i) {
             return i == 0 ? v[0] : i == 1 ? v[1] : i == 2 ? v[2] : v[3];
