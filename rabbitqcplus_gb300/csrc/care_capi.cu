@@ -142,7 +142,8 @@ struct cg_ctx {
     uint64_t n = 0;
     int lmax = 0, pitch = 0, wp = 0, k = 20, nmaps = 48, maxValuesPerKey = 75;
     DevBuf enc, len, hilo, qual, ambig, sig;
-    std::vector<MapTable> maps;
+    std::vector<MapTable> maps;    // views into slotSlab and valueSlab
+    DevBuf slotSlab, valueSlab;
     TablesArg tables{};
     Params params{};
     // where cg_correct's results go: host memory, or device memory for the
@@ -274,11 +275,9 @@ StoreArg store_arg(const cg_ctx* c) {
 }
 
 void release_tables(cg_ctx* c) {
-    for (auto& m : c->maps) {
-        if (m.slots) cudaFree(m.slots);
-        if (m.values) cudaFree(m.values);
-    }
     c->maps.clear();
+    c->slotSlab.release();
+    c->valueSlab.release();
 }
 
 int build_store(cg_ctx* c) {
@@ -342,38 +341,70 @@ int build_tables(cg_ctx* c) {
     const uint64_t cap = pow2_at_least(std::max<uint64_t>(2 * n, 1024));
     if (cap > 0x80000000ull) return fail(c, CG_ERR_UNSUPPORTED, "too many reads for one table (%llu)",
                                          (unsigned long long)n);
-    DevBuf tmp, cursor, packed, scanTmp;
+    // Two passes over the maps.  The first counts every map's keys and values
+    // (the totals stay on the device); one copy and one synchronisation then
+    // size a slab of slots and a slab of values for all maps.  The second
+    // counts again (the counting table is shared by the maps) and places and
+    // fills each map's slots and values.
+    DevBuf tmp, cursor, packed, scanTmp, totals;
     CG_CUDA(c, tmp.ensure(cap * sizeof(Slot)));
     CG_CUDA(c, cursor.ensure(cap * sizeof(uint32_t)));
     CG_CUDA(c, packed.ensure((cap + 1) * sizeof(unsigned long long)));
     CG_CUDA(c, scanTmp.ensure(scan_tmp_bytes(cap + 1)));
-    unsigned long long* hTot = nullptr;
-    CG_CUDA(c, cudaMallocHost(&hTot, sizeof(unsigned long long)));
+    CG_CUDA(c, totals.ensure((size_t)c->nmaps * sizeof(unsigned long long)));
     release_tables(c);
     c->maps.resize(c->nmaps);
     c->stats.table_keys = 0;
     c->stats.table_values = 0;
-    int rc = CG_OK;
-    for (int h = 0; h < c->nmaps && rc == CG_OK; h++) {
+    auto countMap = [&](int h) {
         const unsigned long long* keys = c->sig.as<unsigned long long>() + (uint64_t)h * n;
         cudaError_t e = launch_table_init(tmp.as<Slot>(), cap, c->stream);
         if (e == cudaSuccess) e = launch_table_count(keys, n, tmp.as<Slot>(), (uint32_t)(cap - 1), c->stream);
         if (e == cudaSuccess) e = launch_table_mark(tmp.as<Slot>(), cap, c->maxValuesPerKey,
                                                     packed.as<unsigned long long>(), c->stream);
         if (e == cudaSuccess) e = scan_exclusive_u64(packed.as<unsigned long long>(), cap + 1, scanTmp.p, c->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(hTot, packed.as<unsigned long long>() + cap,
-                                                  sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-        if (e != cudaSuccess) {
-            rc = fail(c, CG_ERR_CUDA, "table %d count: %s", h, cudaGetErrorString(e));
-            break;
-        }
+        return e;
+    };
+    for (int h = 0; h < c->nmaps; h++) {
+        cudaError_t e = countMap(h);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(totals.as<unsigned long long>() + h, packed.as<unsigned long long>() + cap,
+                                sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c->stream);
+        if (e != cudaSuccess) return fail(c, CG_ERR_CUDA, "table %d count: %s", h, cudaGetErrorString(e));
+    }
+    std::vector<unsigned long long> tot(c->nmaps);
+    CG_CUDA(c, cudaMemcpyAsync(tot.data(), totals.p, tot.size() * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, c->stream));
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    uint64_t slotTotal = 0, valueTotal = 0;
+    std::vector<uint64_t> slotOff(c->nmaps), valueOff(c->nmaps);
+    for (int h = 0; h < c->nmaps; h++) {
         MapTable& mt = c->maps[h];
-        mt.keys = *hTot >> 32;
-        mt.nvalues = *hTot & 0xffffffffull;
+        mt.keys = tot[h] >> 32;
+        mt.nvalues = tot[h] & 0xffffffffull;
         mt.cap = pow2_at_least(std::max<uint64_t>(2 * mt.keys, 64));
-        e = cudaMalloc(&mt.slots, mt.cap * sizeof(Slot));
-        if (e == cudaSuccess) e = cudaMalloc(&mt.values, std::max<uint64_t>(mt.nvalues, 1) * sizeof(uint32_t));
+        slotOff[h] = slotTotal;
+        valueOff[h] = valueTotal;
+        slotTotal += mt.cap;
+        valueTotal += (std::max<uint64_t>(mt.nvalues, 1) + 3) / 4 * 4;  // 16-byte aligned per map
+    }
+    {
+        cudaError_t e = c->slotSlab.ensure(slotTotal * sizeof(Slot));
+        if (e == cudaSuccess) e = c->valueSlab.ensure(valueTotal * sizeof(uint32_t));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            release_tables(c);
+            return fail(c, e == cudaErrorMemoryAllocation ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA, "tables: %s",
+                        cudaGetErrorString(e));
+        }
+    }
+    int rc = CG_OK;
+    for (int h = 0; h < c->nmaps && rc == CG_OK; h++) {
+        const unsigned long long* keys = c->sig.as<unsigned long long>() + (uint64_t)h * n;
+        MapTable& mt = c->maps[h];
+        mt.slots = c->slotSlab.as<Slot>() + slotOff[h];
+        mt.values = c->valueSlab.as<uint32_t>() + valueOff[h];
+        cudaError_t e = countMap(h);
         if (e == cudaSuccess) e = launch_table_init(mt.slots, mt.cap, c->stream);
         if (e == cudaSuccess) e = launch_table_place(tmp.as<Slot>(), cap, packed.as<unsigned long long>(),
                                                      c->maxValuesPerKey, mt.slots, (uint32_t)(mt.cap - 1),
@@ -383,8 +414,7 @@ int build_tables(cg_ctx* c) {
                                                     cursor.as<uint32_t>(), mt.values, c->stream);
         if (e == cudaSuccess) e = launch_table_sort(mt.slots, mt.cap, mt.values, c->stream);
         if (e != cudaSuccess) {
-            rc = fail(c, e == cudaErrorMemoryAllocation ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA, "table %d build: %s",
-                      h, cudaGetErrorString(e));
+            rc = fail(c, CG_ERR_CUDA, "table %d build: %s", h, cudaGetErrorString(e));
             break;
         }
         c->stats.table_keys += mt.keys;
@@ -394,11 +424,11 @@ int build_tables(cg_ctx* c) {
         c->tables.mask[h] = (uint32_t)(mt.cap - 1);
     }
     cudaError_t e = cudaStreamSynchronize(c->stream);
-    cudaFreeHost(hTot);
     tmp.release();
     cursor.release();
     packed.release();
     scanTmp.release();
+    totals.release();
     if (rc != CG_OK) return rc;
     CG_CUDA(c, e);
     c->tables.nmaps = c->nmaps;
