@@ -142,8 +142,8 @@ struct cg_ctx {
     uint64_t n = 0;
     int lmax = 0, pitch = 0, wp = 0, k = 20, nmaps = 48, maxValuesPerKey = 75;
     DevBuf enc, len, hilo, qual, ambig, sig;
-    std::vector<MapTable> maps;    // views into slotSlab and valueSlab
-    DevBuf slotSlab, valueSlab;
+    std::vector<MapTable> maps;    // views into tableSlabs
+    std::vector<DevBuf> tableSlabs;
     TablesArg tables{};
     Params params{};
     // where cg_correct's results go: host memory, or device memory for the
@@ -276,8 +276,8 @@ StoreArg store_arg(const cg_ctx* c) {
 
 void release_tables(cg_ctx* c) {
     c->maps.clear();
-    c->slotSlab.release();
-    c->valueSlab.release();
+    for (DevBuf& d : c->tableSlabs) d.release();
+    c->tableSlabs.clear();
 }
 
 int build_store(cg_ctx* c) {
@@ -341,94 +341,127 @@ int build_tables(cg_ctx* c) {
     const uint64_t cap = pow2_at_least(std::max<uint64_t>(2 * n, 1024));
     if (cap > 0x80000000ull) return fail(c, CG_ERR_UNSUPPORTED, "too many reads for one table (%llu)",
                                          (unsigned long long)n);
-    // Two passes over the maps.  The first counts every map's keys and values
-    // (the totals stay on the device); one copy and one synchronisation then
-    // size a slab of slots and a slab of values for all maps.  The second
-    // counts again (the counting table is shared by the maps) and places and
-    // fills each map's slots and values.
-    DevBuf tmp, cursor, packed, scanTmp, totals;
-    CG_CUDA(c, tmp.ensure(cap * sizeof(Slot)));
-    CG_CUDA(c, cursor.ensure(cap * sizeof(uint32_t)));
-    CG_CUDA(c, packed.ensure((cap + 1) * sizeof(unsigned long long)));
-    CG_CUDA(c, scanTmp.ensure(scan_tmp_bytes(cap + 1)));
-    CG_CUDA(c, totals.ensure((size_t)c->nmaps * sizeof(unsigned long long)));
+    // The maps are built in waves of up to kTableStreams maps, one stream and
+    // one set of counting buffers per map of a wave (as many as a quarter of
+    // the free memory holds).  A wave counts its maps' keys and values, one
+    // synchronisation sizes one slab for the wave's slots and values, then the
+    // wave places and fills its maps; the next wave's counting follows on the
+    // same streams.
+    constexpr int kTableStreams = 8;
+    const size_t perStream = cap * (sizeof(Slot) + sizeof(uint32_t)) + (cap + 1) * sizeof(unsigned long long) +
+                             scan_tmp_bytes(cap + 1);
+    size_t freeB = 0, totalB = 0;
+    CG_CUDA(c, cudaMemGetInfo(&freeB, &totalB));
+    const int S = (int)std::max<size_t>(1, std::min<size_t>({(size_t)kTableStreams, (size_t)c->nmaps,
+                                                            freeB / 4 / std::max<size_t>(perStream, 1)}));
+    struct Lane {
+        cudaStream_t stream = nullptr;
+        cudaEvent_t done = nullptr;
+        DevBuf tmp, cursor, packed, scanTmp;
+    };
+    std::vector<Lane> lanes(S);
+    unsigned long long* hTot = nullptr;
     release_tables(c);
     c->maps.resize(c->nmaps);
     c->stats.table_keys = 0;
     c->stats.table_values = 0;
-    auto countMap = [&](int h) {
-        const unsigned long long* keys = c->sig.as<unsigned long long>() + (uint64_t)h * n;
-        cudaError_t e = launch_table_init(tmp.as<Slot>(), cap, c->stream);
-        if (e == cudaSuccess) e = launch_table_count(keys, n, tmp.as<Slot>(), (uint32_t)(cap - 1), c->stream);
-        if (e == cudaSuccess) e = launch_table_mark(tmp.as<Slot>(), cap, c->maxValuesPerKey,
-                                                    packed.as<unsigned long long>(), c->stream);
-        if (e == cudaSuccess) e = scan_exclusive_u64(packed.as<unsigned long long>(), cap + 1, scanTmp.p, c->stream);
-        return e;
-    };
-    for (int h = 0; h < c->nmaps; h++) {
-        cudaError_t e = countMap(h);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(totals.as<unsigned long long>() + h, packed.as<unsigned long long>() + cap,
-                                sizeof(unsigned long long), cudaMemcpyDeviceToDevice, c->stream);
-        if (e != cudaSuccess) return fail(c, CG_ERR_CUDA, "table %d count: %s", h, cudaGetErrorString(e));
-    }
-    std::vector<unsigned long long> tot(c->nmaps);
-    CG_CUDA(c, cudaMemcpyAsync(tot.data(), totals.p, tot.size() * sizeof(unsigned long long),
-                               cudaMemcpyDeviceToHost, c->stream));
-    CG_CUDA(c, cudaStreamSynchronize(c->stream));
-    uint64_t slotTotal = 0, valueTotal = 0;
-    std::vector<uint64_t> slotOff(c->nmaps), valueOff(c->nmaps);
-    for (int h = 0; h < c->nmaps; h++) {
-        MapTable& mt = c->maps[h];
-        mt.keys = tot[h] >> 32;
-        mt.nvalues = tot[h] & 0xffffffffull;
-        mt.cap = pow2_at_least(std::max<uint64_t>(2 * mt.keys, 64));
-        slotOff[h] = slotTotal;
-        valueOff[h] = valueTotal;
-        slotTotal += mt.cap;
-        valueTotal += (std::max<uint64_t>(mt.nvalues, 1) + 3) / 4 * 4;  // 16-byte aligned per map
-    }
-    {
-        cudaError_t e = c->slotSlab.ensure(slotTotal * sizeof(Slot));
-        if (e == cudaSuccess) e = c->valueSlab.ensure(valueTotal * sizeof(uint32_t));
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            release_tables(c);
-            return fail(c, e == cudaErrorMemoryAllocation ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA, "tables: %s",
-                        cudaGetErrorString(e));
-        }
-    }
+    cudaEvent_t sigDone = nullptr;
     int rc = CG_OK;
-    for (int h = 0; h < c->nmaps && rc == CG_OK; h++) {
-        const unsigned long long* keys = c->sig.as<unsigned long long>() + (uint64_t)h * n;
-        MapTable& mt = c->maps[h];
-        mt.slots = c->slotSlab.as<Slot>() + slotOff[h];
-        mt.values = c->valueSlab.as<uint32_t>() + valueOff[h];
-        cudaError_t e = countMap(h);
-        if (e == cudaSuccess) e = launch_table_init(mt.slots, mt.cap, c->stream);
-        if (e == cudaSuccess) e = launch_table_place(tmp.as<Slot>(), cap, packed.as<unsigned long long>(),
-                                                     c->maxValuesPerKey, mt.slots, (uint32_t)(mt.cap - 1),
-                                                     nullptr, c->stream);
-        if (e == cudaSuccess) e = cudaMemsetAsync(cursor.p, 0, cap * sizeof(uint32_t), c->stream);
-        if (e == cudaSuccess) e = launch_table_fill(keys, n, tmp.as<Slot>(), (uint32_t)(cap - 1),
-                                                    cursor.as<uint32_t>(), mt.values, c->stream);
-        if (e == cudaSuccess) e = launch_table_sort(mt.slots, mt.cap, mt.values, c->stream);
-        if (e != cudaSuccess) {
-            rc = fail(c, CG_ERR_CUDA, "table %d build: %s", h, cudaGetErrorString(e));
-            break;
+    auto cuda = [&](cudaError_t e, const char* what) {
+        if (e != cudaSuccess && rc == CG_OK)
+            rc = fail(c, e == cudaErrorMemoryAllocation ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA, "tables (%s): %s",
+                      what, cudaGetErrorString(e));
+        return rc == CG_OK;
+    };
+    if (cuda(cudaMallocHost(&hTot, (size_t)c->nmaps * sizeof(unsigned long long)), "host totals") &&
+        cuda(cudaEventCreateWithFlags(&sigDone, cudaEventDisableTiming), "event") &&
+        cuda(cudaEventRecord(sigDone, c->stream), "event")) {
+        for (Lane& l : lanes) {
+            if (!cuda(cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking), "stream") ||
+                !cuda(cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming), "event") ||
+                !cuda(cudaStreamWaitEvent(l.stream, sigDone, 0), "wait") ||
+                !cuda(l.tmp.ensure(cap * sizeof(Slot)), "counting table") ||
+                !cuda(l.cursor.ensure(cap * sizeof(uint32_t)), "cursors") ||
+                !cuda(l.packed.ensure((cap + 1) * sizeof(unsigned long long)), "counts") ||
+                !cuda(l.scanTmp.ensure(scan_tmp_bytes(cap + 1)), "scan"))
+                break;
         }
-        c->stats.table_keys += mt.keys;
-        c->stats.table_values += mt.nvalues;
-        c->tables.slots[h] = mt.slots;
-        c->tables.values[h] = mt.values;
-        c->tables.mask[h] = (uint32_t)(mt.cap - 1);
+    }
+    for (int w0 = 0; w0 < c->nmaps && rc == CG_OK; w0 += S) {
+        const int w1 = std::min(c->nmaps, w0 + S);
+        for (int h = w0; h < w1 && rc == CG_OK; h++) {
+            Lane& l = lanes[h - w0];
+            const unsigned long long* keys = c->sig.as<unsigned long long>() + (uint64_t)h * n;
+            cudaError_t e = launch_table_init(l.tmp.as<Slot>(), cap, l.stream);
+            if (e == cudaSuccess) e = launch_table_count(keys, n, l.tmp.as<Slot>(), (uint32_t)(cap - 1), l.stream);
+            if (e == cudaSuccess) e = launch_table_mark(l.tmp.as<Slot>(), cap, c->maxValuesPerKey,
+                                                        l.packed.as<unsigned long long>(), l.stream);
+            if (e == cudaSuccess) e = scan_exclusive_u64(l.packed.as<unsigned long long>(), cap + 1, l.scanTmp.p,
+                                                         l.stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(hTot + h, l.packed.as<unsigned long long>() + cap,
+                                                      sizeof(unsigned long long), cudaMemcpyDeviceToHost, l.stream);
+            cuda(e, "count");
+        }
+        for (int h = w0; h < w1 && rc == CG_OK; h++) cuda(cudaStreamSynchronize(lanes[h - w0].stream), "count");
+        if (rc != CG_OK) break;
+        uint64_t slotTotal = 0, valueTotal = 0;
+        std::vector<uint64_t> valueOff(w1 - w0);
+        for (int h = w0; h < w1; h++) {
+            MapTable& mt = c->maps[h];
+            mt.keys = hTot[h] >> 32;
+            mt.nvalues = hTot[h] & 0xffffffffull;
+            mt.cap = pow2_at_least(std::max<uint64_t>(2 * mt.keys, 64));
+            slotTotal += mt.cap;
+        }
+        for (int h = w0; h < w1; h++) {
+            valueOff[h - w0] = valueTotal;
+            valueTotal += (std::max<uint64_t>(c->maps[h].nvalues, 1) + 3) / 4 * 4;  // 16-byte aligned per map
+        }
+        c->tableSlabs.emplace_back();
+        DevBuf& slab = c->tableSlabs.back();
+        if (!cuda(slab.ensure(slotTotal * sizeof(Slot) + valueTotal * sizeof(uint32_t)), "slab")) break;
+        Slot* slotBase = slab.as<Slot>();
+        uint32_t* valueBase = reinterpret_cast<uint32_t*>(slotBase + slotTotal);
+        for (int h = w0; h < w1 && rc == CG_OK; h++) {
+            Lane& l = lanes[h - w0];
+            const unsigned long long* keys = c->sig.as<unsigned long long>() + (uint64_t)h * n;
+            MapTable& mt = c->maps[h];
+            mt.slots = slotBase;
+            slotBase += mt.cap;
+            mt.values = valueBase + valueOff[h - w0];
+            cudaError_t e = launch_table_init(mt.slots, mt.cap, l.stream);
+            if (e == cudaSuccess) e = launch_table_place(l.tmp.as<Slot>(), cap, l.packed.as<unsigned long long>(),
+                                                         c->maxValuesPerKey, mt.slots, (uint32_t)(mt.cap - 1),
+                                                         nullptr, l.stream);
+            if (e == cudaSuccess) e = cudaMemsetAsync(l.cursor.p, 0, cap * sizeof(uint32_t), l.stream);
+            if (e == cudaSuccess) e = launch_table_fill(keys, n, l.tmp.as<Slot>(), (uint32_t)(cap - 1),
+                                                        l.cursor.as<uint32_t>(), mt.values, l.stream);
+            if (e == cudaSuccess) e = launch_table_sort(mt.slots, mt.cap, mt.values, l.stream);
+            if (!cuda(e, "build")) break;
+            c->stats.table_keys += mt.keys;
+            c->stats.table_values += mt.nvalues;
+            c->tables.slots[h] = mt.slots;
+            c->tables.values[h] = mt.values;
+            c->tables.mask[h] = (uint32_t)(mt.cap - 1);
+        }
+    }
+    // the context's stream continues after every wave's last work
+    for (Lane& l : lanes) {
+        if (l.stream && l.done && cudaEventRecord(l.done, l.stream) == cudaSuccess)
+            cuda(cudaStreamWaitEvent(c->stream, l.done, 0), "join");
     }
     cudaError_t e = cudaStreamSynchronize(c->stream);
-    tmp.release();
-    cursor.release();
-    packed.release();
-    scanTmp.release();
-    totals.release();
+    for (Lane& l : lanes) {
+        if (l.stream) cudaStreamSynchronize(l.stream);
+        l.tmp.release();
+        l.cursor.release();
+        l.packed.release();
+        l.scanTmp.release();
+        if (l.done) cudaEventDestroy(l.done);
+        if (l.stream) cudaStreamDestroy(l.stream);
+    }
+    if (sigDone) cudaEventDestroy(sigDone);
+    if (hTot) cudaFreeHost(hTot);
     if (rc != CG_OK) return rc;
     CG_CUDA(c, e);
     c->tables.nmaps = c->nmaps;
