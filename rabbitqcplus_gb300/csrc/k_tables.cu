@@ -108,21 +108,53 @@ __global__ void table_fill_kernel(const unsigned long long* __restrict__ keys, u
     }
 }
 
-// one thread per final slot: insertion sort of the bucket's read ids
+// One warp per 32 slots of the final table: the read ids of each occupied
+// slot's bucket in ascending order.  Buckets of up to 96 ids are ranked in
+// registers (the ids of a bucket are distinct: a read adds one id per map);
+// larger ones take an insertion sort by one lane.
 __global__ void table_sort_kernel(const Slot* __restrict__ fin, uint64_t cap, uint32_t* __restrict__ values) {
-    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= cap) return;
-    const Slot t = fin[s];
-    if (t.key == kEmptyKey) return;
-    uint32_t* v = values + t.offset;
-    for (uint32_t i = 1; i < t.count; i++) {
-        const uint32_t x = v[i];
-        int j = (int)i - 1;
-        while (j >= 0 && v[j] > x) {
-            v[j + 1] = v[j];
-            j--;
+    constexpr unsigned kFull = 0xffffffffu;
+    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;  // blockDim: a multiple of 32
+    const int lane = (int)(threadIdx.x & 31u);
+    Slot t{};
+    bool occ = false;
+    if (s < cap) {
+        t = fin[s];
+        occ = t.key != kEmptyKey && t.count > 1;
+    }
+    for (unsigned m = __ballot_sync(kFull, occ); m; m &= m - 1) {
+        const int src = __ffs(m) - 1;
+        const uint32_t off = __shfl_sync(kFull, t.offset, src), cnt = __shfl_sync(kFull, t.count, src);
+        uint32_t* v = values + off;
+        if (cnt <= 96) {
+            uint32_t x[3], r[3] = {0u, 0u, 0u};
+#pragma unroll
+            for (int k = 0; k < 3; k++) x[k] = (uint32_t)(lane + 32 * k) < cnt ? v[lane + 32 * k] : 0xffffffffu;
+#pragma unroll
+            for (int k2 = 0; k2 < 3; k2++) {
+                if ((uint32_t)(32 * k2) >= cnt) break;
+                for (int j = 0; j < 32; j++) {
+                    const uint32_t y = __shfl_sync(kFull, x[k2], j);
+#pragma unroll
+                    for (int k = 0; k < 3; k++) r[k] += y < x[k];
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int k = 0; k < 3; k++)
+                if ((uint32_t)(lane + 32 * k) < cnt) v[r[k]] = x[k];
+        } else if (lane == src) {
+            for (uint32_t i = 1; i < cnt; i++) {
+                const uint32_t x = v[i];
+                int j = (int)i - 1;
+                while (j >= 0 && v[j] > x) {
+                    v[j + 1] = v[j];
+                    j--;
+                }
+                v[j + 1] = x;
+            }
         }
-        v[j + 1] = x;
+        __syncwarp();
     }
 }
 
