@@ -31,30 +31,96 @@ using namespace cg;
 
 namespace {
 
-// grow-only device buffer
+// Device blocks released by the contexts of this process, kept for reuse
+// (like a caching allocator): a later context of the same shapes allocates
+// without cudaMalloc and frees without cudaFree.  A block is cached only after
+// the device has finished every queued kernel (the release synchronises, as
+// cudaFree would), and the cache is emptied before an allocation fails.
+class BlockCache {
+public:
+    cudaError_t alloc(void** p, size_t n, size_t* got) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            // the smallest cached block of this device that holds n bytes, if
+            // it is at most twice as large
+            for (auto it = free_.lower_bound(n); it != free_.end() && it->first <= 2 * n + 4096; ++it) {
+                if (it->second.first != dev) continue;
+                *p = it->second.second;
+                *got = it->first;
+                free_.erase(it);
+                return cudaSuccess;
+            }
+        }
+        cudaError_t e = cudaMalloc(p, n);
+        if (e == cudaErrorMemoryAllocation) {
+            cudaGetLastError();
+            trim(dev);
+            e = cudaMalloc(p, n);
+        }
+        if (e == cudaSuccess) *got = n;
+        return e;
+    }
+    void release(void* p, size_t bytes) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceSynchronize();
+        std::lock_guard<std::mutex> lock(mu_);
+        free_.emplace(bytes, std::make_pair(dev, p));
+    }
+    void trim(int dev) {
+        std::lock_guard<std::mutex> lock(mu_);
+        for (auto it = free_.begin(); it != free_.end();) {
+            if (it->second.first == dev) {
+                cudaFree(it->second.second);
+                it = free_.erase(it);
+            } else {
+                ++it;
+            }
+        }
+    }
+
+private:
+    std::mutex mu_;
+    std::multimap<size_t, std::pair<int, void*>> free_;
+};
+
+BlockCache& block_cache() {
+    static BlockCache* c = new BlockCache();  // never destroyed: the driver may be gone at exit
+    return *c;
+}
+
+// grow-only device buffer; blocks come from and go back to the block cache,
+// except adopted ones (cached = false), which are freed
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
+    bool cached = true;
     cudaError_t ensure(size_t n) {
         if (n <= bytes) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-        size_t want = std::max(n, bytes + bytes / 2);
-        cudaError_t e = cudaMalloc(&p, want);
+        size_t want = std::max(n, bytes + bytes / 2), got = 0;
+        release();
+        cudaError_t e = block_cache().alloc(&p, want, &got);
         if (e != cudaSuccess) {
             cudaGetLastError();
-            e = cudaMalloc(&p, n);
-            if (e != cudaSuccess) return e;
-            want = n;
+            e = block_cache().alloc(&p, n, &got);
+            if (e != cudaSuccess) {
+                p = nullptr;
+                return e;
+            }
         }
-        bytes = want;
+        bytes = got;
         return cudaSuccess;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (cached) block_cache().release(p, bytes);
+            else cudaFree(p);
+        }
         p = nullptr;
         bytes = 0;
+        cached = true;
     }
     template <class T>
     T* as() const {
@@ -1582,11 +1648,14 @@ int append_device_chunk(cg_ctx* c, void* dChars, uint64_t* dOffs, void* dQual, u
     ch.reads = n;
     ch.chars.p = dChars;  // the chunk owns the buffers from here on (freed after the build)
     ch.chars.bytes = 1;
+    ch.chars.cached = false;
     ch.offs.p = dOffs;
     ch.offs.bytes = (n + 1) * sizeof(uint64_t);
+    ch.offs.cached = false;
     if (c->o.use_quality_scores) {
         ch.qual.p = dQual;
         ch.qual.bytes = 1;
+        ch.qual.cached = false;
     } else if (dQual) {
         cudaFree(dQual);
     }
