@@ -511,16 +511,13 @@ __device__ __forceinline__ void seq_scan_fast(uint32_t (&S)[2][MAXW + 1], const 
             }
         };
         // shifts where the lanes' tiers differ: each lane tests its own
+        // (selected, not branched on, so the lanes stay together)
         auto mixed = [&](int e) {
             for (; bb < e; bb++) {
                 const int sl = base + bb;
-                const int m1 = __popc(diff(bb, 0));
-                if (sl <= slFast) {
-                    if (m1 + __popc(diff(bb, 1)) >= tabMax) continue;
-                } else if (sl <= slFast1 && m1 >= tab63) {
-                    continue;
-                }
-                step(bb);
+                const bool two = sl <= slFast, one = sl <= slFast1;
+                const int m = __popc(diff(bb, 0)) + (two ? __popc(diff(bb, 1)) : 0);
+                if (m < (two ? tabMax : one ? tab63 : 0x7fffffff)) step(bb);
             }
         };
         for (const int e = min(ge, fastAll + 1 - base); bb < e; bb++)  // all lanes: two words
