@@ -151,8 +151,14 @@ void cg_default_options(cg_options* o);
 /* Create a context on o->device.  *out is set only on CG_OK. */
 int cg_create(const cg_options* o, cg_ctx** out);
 
-/* Release the context and all its device memory. */
+/* Release the context.  Its device blocks go to a per-process cache that
+ * later contexts allocate from; cg_release_cached_memory returns them. */
 void cg_destroy(cg_ctx* ctx);
+
+/* Free the device blocks cached for reuse on `device` (all devices if < 0);
+ * an allocation that would fail does the same first.  No counterpart in the
+ * reference (its CPU path keeps no device memory). */
+int cg_release_cached_memory(int device);
 
 /* Message of the last failing call on this context (never NULL). */
 const char* cg_last_error(const cg_ctx* ctx);

@@ -100,7 +100,7 @@ EXPORTED = ["cg_default_options", "cg_create", "cg_destroy", "cg_last_error", "c
             "cg_build_tables", "cg_correct", "cg_get_stats", "cg_get_read_info", "cg_get_signatures",
             "cg_get_candidates", "cg_correct_files", "cg_load_forest", "cg_get_candidates_noalloc",
             "cg_classifier_size", "cg_load_classifier", "cg_get_columns", "cg_default_train_options",
-            "cg_train_classifier", "cg_classifier_gradients", "cg_classifier_logits"]
+            "cg_train_classifier", "cg_classifier_gradients", "cg_classifier_logits", "cg_release_cached_memory"]
 CLASSIFIER_FEATURES = 32
 CLASSIFIER_PARAMS = 6337  # w1 64x32, w2 64x64, w3 64, b1 64, b2 64, b3
 
@@ -160,6 +160,7 @@ def gpu_lib() -> ctypes.CDLL:
         L.cg_classifier_gradients.argtypes = [ctypes.c_int, P, ctypes.c_size_t, P, P, ctypes.c_uint32, P,
                                               ctypes.POINTER(ctypes.c_float)]
         L.cg_classifier_logits.argtypes = [ctypes.c_int, P, ctypes.c_size_t, P, ctypes.c_uint64, P]
+        L.cg_release_cached_memory.argtypes = [ctypes.c_int]
         for f in EXPORTED:
             if f not in ("cg_destroy", "cg_default_options", "cg_last_error", "cg_classifier_size",
                          "cg_default_train_options"):

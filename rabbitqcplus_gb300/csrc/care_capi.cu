@@ -69,16 +69,21 @@ public:
         std::lock_guard<std::mutex> lock(mu_);
         free_.emplace(bytes, std::make_pair(dev, p));
     }
+    // frees the cached blocks of device dev (every device if dev < 0)
     void trim(int dev) {
         std::lock_guard<std::mutex> lock(mu_);
+        int cur = 0;
+        cudaGetDevice(&cur);
         for (auto it = free_.begin(); it != free_.end();) {
-            if (it->second.first == dev) {
+            if (dev < 0 || it->second.first == dev) {
+                cudaSetDevice(it->second.first);
                 cudaFree(it->second.second);
                 it = free_.erase(it);
             } else {
                 ++it;
             }
         }
+        cudaSetDevice(cur);
     }
 
 private:
@@ -1186,6 +1191,11 @@ int cg_create(const cg_options* o, cg_ctx** out) {
     if (e != cudaSuccess) return bail(e);
     *out = c;
     return CG_OK;
+}
+
+int cg_release_cached_memory(int device) {
+    block_cache().trim(device);
+    return cudaGetLastError() == cudaSuccess ? CG_OK : CG_ERR_CUDA;
 }
 
 void cg_destroy(cg_ctx* c) {
