@@ -346,9 +346,8 @@ def main():
     achieved = bytes_launch / dur / 1e9
     traffic = None
     if dom == "align":
-        # DRAM bytes (read + write) of align_lane_kernel per candidate, from an ncu capture of one
-        # 65536-anchor launch of this workload at 2 Mbp: 83.3 MB for 3.777M candidates; scaled here
-        # by the candidates of an average launch (the traffic grows with the candidates processed)
+        # DRAM bytes per candidate measured by ncu (ALIGN_DRAM_BYTES_PER_CANDIDATE), scaled by the
+        # candidates of an average launch (the traffic grows with the candidates processed)
         traffic = ALIGN_DRAM_BYTES_PER_CANDIDATE * per_step_cands * args.steps / max(launches_k, 1)
     roof = {"bound": "hbm", "kernel": kname, "form": "plain", "achieved": achieved, "peak": hbm_peak,
             "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic, "peak_kind": peak_kind,
