@@ -158,7 +158,7 @@ struct GraphSig {
 // One batch pipeline of the batched driver: its buffers, stream and graph.
 struct BatchSet {
     DevBuf rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, flen, nfinal, uoff, scanTmp, cursor,
-        work, colFeat, colMeta, colCount, order, orderScratch, bigScratch;
+        work, colFeat, colMeta, colCount, order, orderScratch, bigScratch, perm;
     cudaStream_t stream = nullptr;
     cudaEvent_t joined = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -171,7 +171,7 @@ struct BatchSet {
         joined = nullptr;
         for (DevBuf* b : {&rawCount, &cand, &ncand, &paired, &aln, &fid, &fshift, &forient, &fweight, &flen, &nfinal,
                           &uoff, &scanTmp, &cursor, &work, &colFeat, &colMeta, &colCount, &order, &orderScratch,
-                          &bigScratch})
+                          &bigScratch, &perm})
             b->release();
         if (stream) cudaStreamDestroy(stream);
         stream = nullptr;
@@ -224,8 +224,9 @@ struct cg_ctx {
 
     // batch buffers
     DevBuf qrange, rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, flen, nfinal, flags, out, counters;
-    DevBuf scanTmp, uoff, msaOrder, orderScratch, bigScratch;
+    DevBuf scanTmp, uoff, msaOrder, orderScratch, bigScratch, perm, lenRange;
     uint32_t* hPinned = nullptr;  // 2 words: total raw, max raw
+    bool lenVaries = false;       // reads of different lengths: candidates aligned in length order
 
     // batched driver
     BatchSet sets[kMaxSets];
@@ -401,6 +402,11 @@ int build_store(cg_ctx* c) {
     c->chunks.clear();
     StoreArg st = store_arg(c);
     CG_CUDA(c, launch_hilo(st, c->hilo.as<uint32_t>(), c->stream));
+    // shortest and longest read (read back once the build has finished)
+    CG_CUDA(c, c->lenRange.ensure(2 * sizeof(unsigned int)));
+    CG_CUDA(c, cudaMemsetAsync(c->lenRange.p, 0xff, sizeof(unsigned int), c->stream));
+    CG_CUDA(c, cudaMemsetAsync(c->lenRange.as<unsigned int>() + 1, 0, sizeof(unsigned int), c->stream));
+    CG_CUDA(c, launch_len_range(st.len, st.n, c->lenRange.as<unsigned int>(), c->stream));
     return CG_OK;
 }
 
@@ -558,6 +564,7 @@ BatchArg batch_arg(cg_ctx* c, uint64_t first, int count) {
     b.fweight = c->fweight.as<float>();
     b.flen = c->flen.as<uint16_t>();
     b.nfinal = c->nfinal.as<uint32_t>();
+    b.perm = c->lenVaries ? c->perm.as<uint32_t>() : nullptr;
     b.flags = c->flags.as<uint8_t>();
     b.out = c->out.as<char>();
     b.outPitch = c->lmax;
@@ -612,6 +619,7 @@ int run_candidates(cg_ctx* c, uint64_t first, int count) {
     const uint32_t maxRaw = c->hPinned[1];
     const size_t cap = std::max<uint64_t>(total, 1);
     CG_CUDA(c, c->cand.ensure(cap * sizeof(uint32_t)));
+    if (c->lenVaries) CG_CUDA(c, c->perm.ensure(cap * sizeof(uint32_t)));
     CG_CUDA(c, c->paired.ensure(cap));
     CG_CUDA(c, c->aln.ensure(cap * sizeof(uint2)));
     CG_CUDA(c, c->fid.ensure(cap * sizeof(uint32_t)));
@@ -723,6 +731,7 @@ BatchArg set_arg(cg_ctx* c, BatchSet& s, int count) {
     b.fweight = s.fweight.as<float>();
     b.flen = s.flen.as<uint16_t>();
     b.nfinal = s.nfinal.as<uint32_t>();
+    b.perm = c->lenVaries ? s.perm.as<uint32_t>() : nullptr;
     b.flags = c->flagsRange.as<uint8_t>();
     b.out = c->outRange.as<char>();
     b.outPitch = c->lmax;
@@ -745,6 +754,7 @@ int ensure_set(cg_ctx* c, BatchSet& s, int count, uint64_t capRaw) {
     CG_CUDA(c, s.nfinal.ensure(n * sizeof(uint32_t)));
     CG_CUDA(c, s.scanTmp.ensure(scan_tmp_bytes(n + 1)));
     CG_CUDA(c, s.cand.ensure(capRaw * sizeof(uint32_t)));
+    if (c->lenVaries) CG_CUDA(c, s.perm.ensure(capRaw * sizeof(uint32_t)));
     CG_CUDA(c, s.paired.ensure(capRaw));
     CG_CUDA(c, s.aln.ensure(capRaw * sizeof(uint2)));
     CG_CUDA(c, s.fid.ensure(capRaw * sizeof(uint32_t)));
@@ -819,7 +829,7 @@ int capture_set(cg_ctx* c, BatchSet& s, int count, unsigned long long stride, co
     g.maxRows = maxRows;
     for (const DevBuf* d : {&s.rawCount, &s.cand, &s.ncand, &s.paired, &s.aln, &s.fid, &s.fshift, &s.forient,
                             &s.fweight, &s.flen, &s.nfinal, &s.uoff, &s.scanTmp, &s.cursor, &s.work, &s.colFeat,
-                            &s.colMeta, &s.colCount, &s.order, &s.orderScratch, &s.bigScratch, &c->mlp,
+                            &s.colMeta, &s.colCount, &s.order, &s.orderScratch, &s.bigScratch, &s.perm, &c->mlp,
                             &c->outRange,
                             &c->flagsRange, &c->rangeOff, &c->counters, &c->sig})
         g.ptrs.push_back(d->p);
@@ -1206,7 +1216,7 @@ void cg_destroy(cg_ctx* c) {
     for (DevBuf* b : {&c->enc, &c->len, &c->hilo, &c->qual, &c->ambig, &c->sig, &c->qrange, &c->rawCount, &c->cand,
                       &c->ncand, &c->paired, &c->aln, &c->fid, &c->fshift, &c->forient, &c->fweight, &c->flen, &c->nfinal,
                       &c->flags, &c->out, &c->counters, &c->scanTmp, &c->uoff, &c->forestNodes, &c->treeOffsets,
-                      &c->msaOrder, &c->orderScratch, &c->bigScratch})
+                      &c->msaOrder, &c->orderScratch, &c->bigScratch, &c->perm, &c->lenRange})
         b->release();
     for (cg_ctx::Chunk& ch : c->chunks) {
         ch.chars.release();
@@ -1293,6 +1303,11 @@ int cg_build_tables(cg_ctx* c) {
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     c->stats.seconds_build = ms / 1000.0;
+    {
+        unsigned int range[2] = {0, 0};
+        CG_CUDA(c, cudaMemcpy(range, c->lenRange.p, sizeof(range), cudaMemcpyDeviceToHost));
+        c->lenVaries = range[0] != range[1];
+    }
     c->stats.num_reads = c->n;
     c->stats.kmerlength = c->k;
     c->stats.num_maps = c->nmaps;

@@ -122,6 +122,8 @@ cudaError_t launch_encode(const char* chars, const uint64_t* offs, const char* q
                           cudaStream_t s);
 cudaError_t launch_hilo(StoreArg st, uint32_t* hilo, cudaStream_t s);
 cudaError_t launch_signatures(StoreArg st, int k, int nmaps, unsigned long long* sig, cudaStream_t s);
+// out[0] = shortest, out[1] = longest read of the store (out preset to {~0, 0})
+cudaError_t launch_len_range(const uint16_t* len, uint64_t n, unsigned int* out, cudaStream_t s);
 
 // hash tables
 cudaError_t launch_table_init(Slot* t, uint64_t cap, cudaStream_t s);
@@ -153,6 +155,10 @@ struct BatchArg {
     float* fweight;         // [totalRaw]
     uint16_t* flen;         // [totalRaw] candidate length
     uint32_t* nfinal;       // [count]
+    // [totalRaw] or null: per anchor, its candidates' positions in the order of
+    // their lengths (read lengths vary); the alignment gives lane j of an
+    // anchor its candidate perm[j], so a warp's lanes see similar lengths
+    uint32_t* perm;
     uint8_t* flags;         // [count] CG_RESULT_*
     char* out;              // [count][outPitch]
     int outPitch;

@@ -607,7 +607,7 @@ __global__ void __launch_bounds__(kLaneThreads, MAXW <= 5 ? 8 : 1) align_lane_ke
             }
             const int a = lo;
             const uint32_t j = t - uoff[a];
-            const uint32_t slot = rawOff[a] + j;
+            const uint32_t slot = rawOff[a] + (b.perm ? b.perm[rawOff[a] + j] : j);
             const uint64_t aid = first + (uint64_t)a;
             const uint32_t id = b.cand[slot];
             const int La = st.len[aid], Lc = st.len[id];

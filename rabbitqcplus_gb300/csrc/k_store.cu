@@ -278,6 +278,27 @@ cudaError_t launch_hilo(StoreArg st, uint32_t* hilo, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+namespace {
+__global__ void len_range_kernel(const uint16_t* __restrict__ len, uint64_t n, unsigned int* out) {
+    unsigned int lo = 0xffffffffu, hi = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        lo = min(lo, (unsigned int)len[i]);
+        hi = max(hi, (unsigned int)len[i]);
+    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&out[0], lo);
+        atomicMax(&out[1], hi);
+    }
+}
+}  // namespace
+
+cudaError_t launch_len_range(const uint16_t* len, uint64_t n, unsigned int* out, cudaStream_t s) {
+    len_range_kernel<<<(unsigned)std::min<uint64_t>((n + 255) / 256, 1216), 256, 0, s>>>(len, n, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_signatures(StoreArg st, int k, int nmaps, unsigned long long* sig, cudaStream_t s) {
     const unsigned blocks = (unsigned)((st.n + kSigReads - 1) / kSigReads);
     signature_kernel<<<blocks, kSigReads * 3, 0, s>>>(st, k, nmaps, sig);

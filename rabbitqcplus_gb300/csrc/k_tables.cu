@@ -354,6 +354,48 @@ __device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params
         }
         for (uint32_t i = tid; i < U; i += kGatherThreads) out[i] = table[i];
     }
+    if (b.perm) {
+        // the alignment's order: positions grouped by words per read
+        // (length / 32, up to 8), in position order within a group -- a
+        // counting sort by one warp; the list's space holds the groups
+        __syncthreads();
+        if (tid < 32) {
+            constexpr unsigned kFull = 0xffffffffu;
+            constexpr int kGroups = 9;
+            const int lane = tid;
+            uint32_t cnt = 0;  // lane g < kGroups: size of group g, then its start
+            for (uint32_t i0 = 0; i0 < U; i0 += 32) {
+                const uint32_t i = i0 + (uint32_t)lane;
+                const uint32_t g = i < U ? min((uint32_t)st.len[out[i]] >> 5, (uint32_t)(kGroups - 1)) : kGroups;
+                if (i < U) list[i] = g;
+#pragma unroll
+                for (int v = 0; v < kGroups; v++) {
+                    const uint32_t n = __popc(__ballot_sync(kFull, g == (uint32_t)v));
+                    if (lane == v) cnt += n;
+                }
+            }
+            uint32_t start = cnt;  // exclusive scan over the groups
+#pragma unroll
+            for (int d = 1; d < 16; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(kFull, start, d);
+                if (lane >= d) start += y;
+            }
+            start -= cnt;
+            for (uint32_t i0 = 0; i0 < U; i0 += 32) {
+                const uint32_t i = i0 + (uint32_t)lane;
+                const uint32_t g = i < U ? list[i] : kGroups;
+                uint32_t r = 0;
+#pragma unroll
+                for (int v = 0; v < kGroups; v++) {
+                    const uint32_t m = __ballot_sync(kFull, g == (uint32_t)v);
+                    const uint32_t s0 = __shfl_sync(kFull, start, v);
+                    if (g == (uint32_t)v) r = s0 + __popc(m & ((1u << lane) - 1u));
+                    if (lane == v) start += __popc(m);
+                }
+                if (i < U) b.perm[off + r] = i;
+            }
+        }
+    }
     if (tid == 0) {
         b.ncand[a] = U;
         atomicAdd(&b.counters[kCounterRaw], (unsigned long long)raw);
