@@ -570,7 +570,7 @@ constexpr int kLaneThreads = 128;
 // sequential scan, the orientation choice, the packed result at the
 // candidate's slot.  uoff = exclusive scan of the per-anchor candidate counts.
 template <int MAXW>
-__global__ void __launch_bounds__(kLaneThreads, MAXW <= 5 ? 8 : 1) align_lane_kernel(StoreArg st, Params p, BatchArg b,
+__global__ void __launch_bounds__(kLaneThreads, 8) align_lane_kernel(StoreArg st, Params p, BatchArg b,
                                                                   const uint32_t* __restrict__ rawOff,
                                                                   const uint32_t* __restrict__ uoff, uint32_t total) {
     __shared__ int16_t maxErrTab[CG_MAX_READ_LENGTH + 2];
