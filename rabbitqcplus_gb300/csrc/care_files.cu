@@ -334,7 +334,7 @@ unsigned grid_for(uint64_t threads, int block) { return (unsigned)((threads + bl
 
 }  // namespace
 
-int correct_fastq_on_device(const cg_options& options, const std::vector<const std::vector<char>*>& inputs,
+int correct_fastq_on_device(const cg_options& options, const std::vector<ByteSpan>& inputs,
                             bool paired, bool qualityLabels, int numOutputs, const std::vector<char>* forest,
                             uint32_t maxTrees, const std::vector<char>* classifier, FastqRun* run,
                             std::string* error) {
@@ -355,12 +355,12 @@ int correct_fastq_on_device(const cg_options& options, const std::vector<const s
     std::vector<DMem> fileDev(nf), nlDev(nf);
     std::vector<uint64_t> recs(nf);
     for (size_t k = 0; k < nf; k++) {
-        const std::vector<char>& f = *inputs[k];
-        const bool needNl = f.empty() || f.back() != '\n';
-        const uint64_t size = f.size() + (needNl ? 1 : 0);
+        const ByteSpan f = inputs[k];
+        const bool needNl = f.size == 0 || f.data[f.size - 1] != '\n';
+        const uint64_t size = f.size + (needNl ? 1 : 0);
         DCHECK(fileDev[k].alloc(size));
-        if (!f.empty()) DCHECK(cudaMemcpyAsync(fileDev[k].p, f.data(), f.size(), cudaMemcpyHostToDevice, s));
-        if (needNl) DCHECK(cudaMemsetAsync(fileDev[k].as<char>() + f.size(), '\n', 1, s));
+        if (f.size) DCHECK(cudaMemcpyAsync(fileDev[k].p, f.data, f.size, cudaMemcpyHostToDevice, s));
+        if (needNl) DCHECK(cudaMemsetAsync(fileDev[k].as<char>() + f.size, '\n', 1, s));
         const uint64_t blocks = (size + kIdxBlockBytes - 1) / kIdxBlockBytes;
         DMem counts, tmp;
         DCHECK(counts.alloc((blocks + 1) * sizeof(unsigned long long)));

@@ -22,6 +22,12 @@
 
 namespace cg {
 
+// A caller's bytes (a whole input file).
+struct ByteSpan {
+    const char* data;
+    size_t size;
+};
+
 struct FastqRun {
     uint64_t reads = 0;
     uint64_t records = 0;                    // correction records (changNum)
@@ -42,7 +48,7 @@ struct FastqRun {
 // with '+' or whose quality length differs, a read over CG_MAX_READ_LENGTH) --
 // nothing has been written then and the caller takes the host path; any other
 // code is an error (message in *error).
-int correct_fastq_on_device(const cg_options& options, const std::vector<const std::vector<char>*>& inputs,
+int correct_fastq_on_device(const cg_options& options, const std::vector<ByteSpan>& inputs,
                             bool paired, bool qualityLabels, int numOutputs, const std::vector<char>* forest,
                             uint32_t maxTrees, const std::vector<char>* classifier, FastqRun* run,
                             std::string* error);

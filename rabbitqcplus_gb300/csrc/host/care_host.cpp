@@ -194,10 +194,10 @@ bool correctOnDevice(const ProgramOptions& o, cg::FastqRun* run) {
         if (fmt != FileFormat::FASTQ && fmt != FileFormat::FASTQGZ) return false;
     }
     const bool paired = o.pairType == SequencePairType::PairedEnd && o.inputfiles.size() == 2;
-    std::vector<std::vector<char>> data;
-    for (const auto& f : o.inputfiles) data.push_back(readWholeFile(f));
-    std::vector<const std::vector<char>*> inputs;
-    for (const auto& d : data) inputs.push_back(&d);
+    std::vector<FileBytes> data;
+    for (const auto& f : o.inputfiles) data.push_back(readFileBytes(f));
+    std::vector<cg::ByteSpan> inputs;
+    for (const auto& d : data) inputs.push_back(cg::ByteSpan{d.data.get(), d.size});
     std::vector<char> forest, classifier;
     if (o.correctionType == CorrectionType::Forest) forest = loadFile(o.mlForestfileAnchor, "forest");
     if (o.correctionType == CorrectionType::Learned) classifier = loadFile(o.mlClassifierFileAnchor, "classifier");

@@ -1,9 +1,16 @@
 #include "seqio.h"
 
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
+#include <atomic>
+#include <cerrno>
 #include <cstdio>
 #include <cstring>
 #include <stdexcept>
+#include <thread>
 
 #ifdef CG_HAVE_ZLIB
 #include <zlib.h>
@@ -214,62 +221,102 @@ void SequenceWriter::write(const std::string& header, const char* seq, size_t le
     if (b.size() > (1u << 22)) impl->flush();
 }
 
-void SequenceWriter::writeRaw(const char* data, size_t len) {
-    impl->flush();
-    const size_t step = 1u << 30;  // gzwrite takes an unsigned count
-    for (size_t done = 0; done < len; done += step) {
-        const size_t k = len - done < step ? len - done : step;
-#ifdef CG_HAVE_ZLIB
-        if (impl->gz) {
-            if (gzwrite(impl->gz, data + done, (unsigned)k) != (int)k) throw std::runtime_error("gzip write failed");
-            continue;
+namespace {
+
+// len bytes of the file at offset off into buf, as 32 MiB parts read by up to
+// 16 threads (one thread copies page-cache data at a few GB/s)
+bool parallelRead(int fd, char* buf, size_t len, off_t off) {
+    constexpr size_t kPart = size_t(32) << 20;
+    const size_t parts = (len + kPart - 1) / kPart;
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nthreads = std::min<size_t>({parts, hw, 16});
+    std::atomic<size_t> next{0};
+    std::atomic<bool> ok{true};
+    auto work = [&]() {
+        for (size_t p = next.fetch_add(1); p < parts && ok; p = next.fetch_add(1)) {
+            size_t done = p * kPart;
+            const size_t end = std::min(len, done + kPart);
+            while (done < end) {
+                const ssize_t r = ::pread(fd, buf + done, end - done, off + (off_t)done);
+                if (r < 0 && errno == EINTR) continue;
+                if (r <= 0) {
+                    ok = false;
+                    return;
+                }
+                done += (size_t)r;
+            }
         }
-#endif
-        if (std::fwrite(data + done, 1, k, impl->f) != k) throw std::runtime_error("write failed");
-    }
+    };
+    std::vector<std::thread> threads;
+    for (size_t t = 1; t < nthreads; t++) threads.emplace_back(work);
+    work();
+    for (std::thread& t : threads) t.join();
+    return ok;
 }
 
-std::vector<char> readWholeFile(const std::string& path) {
-    std::vector<char> out;
-    bool gzipped = false;
-    {
-        FILE* f = std::fopen(path.c_str(), "rb");
-        if (!f) throw std::runtime_error("cannot open " + path);
-        unsigned char magic[2] = {0, 0};
-        gzipped = std::fread(magic, 1, 2, f) == 2 && magic[0] == 0x1f && magic[1] == 0x8b;
-        if (!gzipped) {  // plain: one read of the whole file
-            std::fseek(f, 0, SEEK_END);
-            const long size = std::ftell(f);
-            std::fseek(f, 0, SEEK_SET);
-            out.resize(size > 0 ? (size_t)size : 0);
-            const bool ok = out.empty() || std::fread(out.data(), 1, out.size(), f) == out.size();
-            std::fclose(f);
-            if (!ok) throw std::runtime_error("cannot read " + path);
-            return out;
+}  // namespace
+
+void SequenceWriter::writeRaw(const char* data, size_t len) {
+    impl->flush();
+#ifdef CG_HAVE_ZLIB
+    if (impl->gz) {
+        const size_t step = 1u << 30;  // gzwrite takes an unsigned count
+        for (size_t done = 0; done < len; done += step) {
+            const size_t k = len - done < step ? len - done : step;
+            if (gzwrite(impl->gz, data + done, (unsigned)k) != (int)k) throw std::runtime_error("gzip write failed");
         }
-        std::fclose(f);
+        return;
     }
+#endif
+    // plain: one stream (writes to one file do not run in parallel: the
+    // kernel serialises them on the file)
+    if (len > 0 && std::fwrite(data, 1, len, impl->f) != len) throw std::runtime_error("write failed");
+}
+
+FileBytes readFileBytes(const std::string& path) {
+    FileBytes out;
+    const int fd = ::open(path.c_str(), O_RDONLY);
+    if (fd < 0) throw std::runtime_error("cannot open " + path);
+    struct stat sb;
+    unsigned char magic[2] = {0, 0};
+    const bool gzipped = ::pread(fd, magic, 2, 0) == 2 && magic[0] == 0x1f && magic[1] == 0x8b;
+    if (!gzipped) {  // plain: the whole file by parallel reads
+        if (::fstat(fd, &sb) != 0) {
+            ::close(fd);
+            throw std::runtime_error("cannot read " + path);
+        }
+        out.size = (size_t)sb.st_size;
+        out.data.reset(new char[std::max<size_t>(out.size, 1)]);
+        const bool ok = parallelRead(fd, out.data.get(), out.size, 0);
+        ::close(fd);
+        if (!ok) throw std::runtime_error("cannot read " + path);
+        return out;
+    }
+    ::close(fd);
 #ifdef CG_HAVE_ZLIB
     gzFile gz = gzopen(path.c_str(), "rb");
     if (!gz) throw std::runtime_error("cannot open " + path);
     gzbuffer(gz, 1 << 20);
-    size_t used = 0;
-    out.resize(1 << 24);
+    size_t cap = size_t(1) << 24;
+    out.data.reset(new char[cap]);
     while (true) {
-        if (used == out.size()) out.resize(out.size() * 2);
-        const size_t want = std::min<size_t>(out.size() - used, 1u << 30);
-        const int got = gzread(gz, out.data() + used, (unsigned)want);
+        if (out.size == cap) {
+            std::unique_ptr<char[]> bigger(new char[2 * cap]);
+            std::memcpy(bigger.get(), out.data.get(), out.size);
+            out.data = std::move(bigger);
+            cap *= 2;
+        }
+        const size_t want = std::min<size_t>(cap - out.size, 1u << 30);
+        const int got = gzread(gz, out.data.get() + out.size, (unsigned)want);
         if (got < 0) {
             gzclose(gz);
             throw std::runtime_error("cannot read " + path);
         }
         if (got == 0) break;
-        used += (size_t)got;
+        out.size += (size_t)got;
     }
     gzclose(gz);
-    out.resize(used);
 #else
-    (void)gzipped;
     throw std::runtime_error("gzip input needs zlib: " + path);
 #endif
     return out;

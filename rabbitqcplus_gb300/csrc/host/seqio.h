@@ -62,8 +62,13 @@ private:
     std::unique_ptr<Impl> impl;
 };
 
-// The whole (decompressed) content of a plain or gzip file.
-std::vector<char> readWholeFile(const std::string& path);
+// The whole (decompressed) content of a plain or gzip file, in a buffer that
+// is not zero-filled first; a plain file is read by parallel pread calls.
+struct FileBytes {
+    std::unique_ptr<char[]> data;
+    size_t size = 0;
+};
+FileBytes readFileBytes(const std::string& path);
 
 // Reads all files of one input group: a single-end file, an interleaved
 // paired file, or two paired files read alternately.
