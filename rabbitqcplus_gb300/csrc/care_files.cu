@@ -462,49 +462,64 @@ int correct_fastq_on_device(const cg_options& options, const std::vector<ByteSpa
     DMem flagsOut, seqOut;
     DCHECK(flagsOut.alloc(n));
     DCHECK(seqOut.alloc(n * (uint64_t)pitch));
-    LCHECK(ctx.c, correct_into_device(ctx.c, 0, n, flagsOut.as<uint8_t>(), seqOut.as<char>(), (size_t)pitch));
-    LCHECK(ctx.c, cg_get_stats(ctx.c, &run->stats));
 
-    // ---- STEP3: records
-    DMem mode, status, size, recCount;
+    // ---- STEP2 and STEP3 per range of reads (one range unless the caller
+    // takes the output range by range): correction into device memory, then
+    // the range's records of every output file
+    DMem mode, status, size, recCount, pos, tmp;
     DCHECK(mode.alloc(n));
     DCHECK(status.alloc(n));
     DCHECK(size.alloc(n * sizeof(unsigned long long)));
     DCHECK(recCount.alloc(sizeof(unsigned long long)));
     DCHECK(cudaMemsetAsync(recCount.p, 0, sizeof(unsigned long long), s));
-    plan_kernel<<<grid_for(n, 256), 256, 0, s>>>(reads, n, flagsOut.as<uint8_t>(), seqOut.as<char>(), pitch,
-                                                 qualityLabels ? 1 : 0, mode.as<uint8_t>(), status.as<uint8_t>(),
-                                                 size.as<unsigned long long>(), recCount.as<unsigned long long>());
-    DCHECK(cudaGetLastError());
-    unsigned long long records = 0;
-    DCHECK(cudaMemcpyAsync(&records, recCount.p, sizeof(records), cudaMemcpyDeviceToHost, s));
+    DCHECK(pos.alloc((n + 1) * sizeof(unsigned long long)));
+    DCHECK(tmp.alloc(scan_tmp_bytes(n + 1)));
     run->outputs.clear();
     run->outputs.resize((size_t)numOutputs);
     run->outputSizes.assign((size_t)numOutputs, 0);
-    DMem pos, tmp;
-    DCHECK(pos.alloc((n + 1) * sizeof(unsigned long long)));
-    DCHECK(tmp.alloc(scan_tmp_bytes(n + 1)));
-    for (int f = 0; f < numOutputs; f++) {
-        mask_kernel<<<grid_for(n + 1, 256), 256, 0, s>>>(size.as<unsigned long long>(), readOut.as<uint8_t>(), n,
-                                                         (uint8_t)f, pos.as<unsigned long long>());
+    const uint64_t range = run->onChunk ? std::max<uint64_t>(262144, (n / 4 + 1) & ~1ull) : n;  // even
+    for (uint64_t r0 = 0; r0 < n; r0 += range) {
+        const uint64_t m = std::min(range, n - r0);
+        uint8_t* fl = flagsOut.as<uint8_t>() + r0;
+        char* sq = seqOut.as<char>() + r0 * (uint64_t)pitch;
+        LCHECK(ctx.c, correct_into_device(ctx.c, r0, m, fl, sq, (size_t)pitch));
+        plan_kernel<<<grid_for(m, 256), 256, 0, s>>>(reads + r0, m, fl, sq, pitch, qualityLabels ? 1 : 0,
+                                                     mode.as<uint8_t>() + r0, status.as<uint8_t>() + r0,
+                                                     size.as<unsigned long long>() + r0,
+                                                     recCount.as<unsigned long long>());
         DCHECK(cudaGetLastError());
-        DCHECK(scan_exclusive_u64(pos.as<unsigned long long>(), n + 1, tmp.p, s));
-        unsigned long long total = 0;
-        DCHECK(cudaMemcpyAsync(&total, pos.as<unsigned long long>() + n, sizeof(total), cudaMemcpyDeviceToHost, s));
-        DCHECK(cudaStreamSynchronize(s));
-        if (total == 0) continue;
-        DMem outDev;
-        DCHECK(outDev.alloc(total));
-        write_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(reads, n, readOut.as<uint8_t>(), (uint8_t)f,
-                                                           pos.as<unsigned long long>(), mode.as<uint8_t>(),
-                                                           status.as<uint8_t>(), seqOut.as<char>(), pitch,
-                                                           qualityLabels ? 1 : 0, outDev.as<char>());
-        DCHECK(cudaGetLastError());
-        run->outputs[f].reset(new char[total]);  // left uninitialised: the copy fills it
-        run->outputSizes[f] = total;
-        DCHECK(cudaMemcpyAsync(run->outputs[f].get(), outDev.p, total, cudaMemcpyDeviceToHost, s));
-        DCHECK(cudaStreamSynchronize(s));
+        for (int f = 0; f < numOutputs; f++) {
+            mask_kernel<<<grid_for(m + 1, 256), 256, 0, s>>>(size.as<unsigned long long>() + r0,
+                                                             readOut.as<uint8_t>() + r0, m, (uint8_t)f,
+                                                             pos.as<unsigned long long>());
+            DCHECK(cudaGetLastError());
+            DCHECK(scan_exclusive_u64(pos.as<unsigned long long>(), m + 1, tmp.p, s));
+            unsigned long long total = 0;
+            DCHECK(cudaMemcpyAsync(&total, pos.as<unsigned long long>() + m, sizeof(total), cudaMemcpyDeviceToHost,
+                                   s));
+            DCHECK(cudaStreamSynchronize(s));
+            if (total == 0) continue;
+            DMem outDev;
+            DCHECK(outDev.alloc(total));
+            write_kernel<<<grid_for(m * 32, 256), 256, 0, s>>>(reads + r0, m, readOut.as<uint8_t>() + r0, (uint8_t)f,
+                                                               pos.as<unsigned long long>(), mode.as<uint8_t>() + r0,
+                                                               status.as<uint8_t>() + r0, sq, pitch,
+                                                               qualityLabels ? 1 : 0, outDev.as<char>());
+            DCHECK(cudaGetLastError());
+            std::unique_ptr<char[]> bytes(new char[total]);  // left uninitialised: the copy fills it
+            DCHECK(cudaMemcpyAsync(bytes.get(), outDev.p, total, cudaMemcpyDeviceToHost, s));
+            DCHECK(cudaStreamSynchronize(s));
+            if (run->onChunk) {
+                run->onChunk(f, std::move(bytes), total);
+            } else {
+                run->outputs[f] = std::move(bytes);
+                run->outputSizes[f] = total;
+            }
+        }
     }
+    LCHECK(ctx.c, cg_get_stats(ctx.c, &run->stats));
+    unsigned long long records = 0;
+    DCHECK(cudaMemcpyAsync(&records, recCount.p, sizeof(records), cudaMemcpyDeviceToHost, s));
     DCHECK(cudaStreamSynchronize(s));
     run->reads = n;
     run->records = records;

@@ -14,6 +14,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <functional>
 #include <memory>
 #include <string>
 #include <vector>
@@ -35,6 +36,10 @@ struct FastqRun {
     // bytes of every output file
     std::vector<std::unique_ptr<char[]>> outputs;
     std::vector<size_t> outputSizes;
+    // if set, the reads are corrected in a few ranges and each range's bytes
+    // of output file f go here in order (outputs stays empty), so that the
+    // caller can write one range while the next is corrected
+    std::function<void(int f, std::unique_ptr<char[]> bytes, size_t size)> onChunk;
 };
 
 // Corrects the reads of `inputs` (the bytes of whole FASTQ files) and returns

@@ -2,13 +2,18 @@
 #include "care_host.h"
 
 #include <algorithm>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <deque>
+#include <exception>
 #include <fstream>
 #include <iterator>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "care_files.h"
@@ -234,15 +239,76 @@ std::string labelled(const std::string& header, uint8_t status, bool labels) {
 
 }  // namespace
 
-RunReport performCorrection(const ProgramOptions& o) {
-    {
-        cg::FastqRun dr;
-        if (correctOnDevice(o, &dr)) {
-            const FileFormat fmt = outputFormat(o);
-            for (size_t f = 0; f < o.outputfilenames.size(); f++) {
-                SequenceWriter w(o.outputdirectory + "/" + o.outputfilenames[f], fmt);
-                w.writeRaw(dr.outputs[f].get(), dr.outputSizes[f]);
+namespace {
+
+// Output files written by a thread of their own, in the order the ranges
+// arrive, while the device corrects the next range.
+class RangeWriter {
+public:
+    RangeWriter(const ProgramOptions& o, FileFormat fmt) {
+        for (const auto& name : o.outputfilenames)
+            writers_.emplace_back(new SequenceWriter(o.outputdirectory + "/" + name, fmt));
+        thread_ = std::thread([this] { loop(); });
+    }
+    ~RangeWriter() { finish(false); }
+    void put(int f, std::unique_ptr<char[]> bytes, size_t size) {
+        std::lock_guard<std::mutex> lock(mu_);
+        queue_.push_back(Item{f, std::move(bytes), size});
+        cv_.notify_one();
+    }
+    // waits for every range to be written; rethrows a write error
+    void finish(bool rethrow = true) {
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            done_ = true;
+            cv_.notify_one();
+        }
+        if (thread_.joinable()) thread_.join();
+        if (rethrow && error_) std::rethrow_exception(error_);
+    }
+
+private:
+    struct Item {
+        int f;
+        std::unique_ptr<char[]> bytes;
+        size_t size;
+    };
+    void loop() {
+        while (true) {
+            Item it;
+            {
+                std::unique_lock<std::mutex> lock(mu_);
+                cv_.wait(lock, [this] { return done_ || !queue_.empty(); });
+                if (queue_.empty()) return;
+                it = std::move(queue_.front());
+                queue_.pop_front();
             }
+            if (error_) continue;  // drain after a failure
+            try {
+                writers_[it.f]->writeRaw(it.bytes.get(), it.size);
+            } catch (...) {
+                error_ = std::current_exception();
+            }
+        }
+    }
+    std::vector<std::unique_ptr<SequenceWriter>> writers_;
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::deque<Item> queue_;
+    bool done_ = false;
+    std::exception_ptr error_;
+    std::thread thread_;
+};
+
+}  // namespace
+
+RunReport performCorrection(const ProgramOptions& o) {
+    if (!o.outputfilenames.empty() && !o.inputfiles.empty()) {
+        cg::FastqRun dr;
+        RangeWriter out(o, outputFormat(o));
+        dr.onChunk = [&out](int f, std::unique_ptr<char[]> bytes, size_t size) { out.put(f, std::move(bytes), size); };
+        if (correctOnDevice(o, &dr)) {
+            out.finish();
             RunReport rep;
             rep.reads = dr.reads;
             rep.records = dr.records;

@@ -89,3 +89,26 @@ def test_input_the_device_path_does_not_take(tmp_path):
     nh, host = run(capi.CareOptions.defaults(30.0), [fq], tmp_path / "host", 1, host=True)
     assert nd == nh
     assert md5(dev[0]) == md5(host[0])
+
+
+@pytest.mark.parametrize("paired", [False, True])
+def test_large_input_corrected_and_written_range_by_range(tmp_path, paired):
+    # more than 262144 reads: the device path corrects and writes the output in
+    # several ranges (the writer thread writes one while the next is corrected)
+    cfg = sim.SimConfig(seed=54, genome_length=400_000, num_reads=600_000, paired=paired, sub_rate_5p=0.002,
+                        sub_rate_3p=0.02)
+    r = sim.SimReads(cfg)
+    if paired:
+        ins = [str(tmp_path / "in_1.fq"), str(tmp_path / "in_2.fq")]
+        r.write_fastq(ins[0], ins[1])
+        mk = lambda: capi.CareOptions.defaults(30.0, pair_mode=capi.CG_PAIR_PE, driver=capi.CG_DRIVER_BATCHED)
+        nout = 2
+    else:
+        ins = [str(tmp_path / "in.fq")]
+        r.write_fastq(ins[0])
+        mk = lambda: capi.CareOptions.defaults(30.0, driver=capi.CG_DRIVER_BATCHED)
+        nout = 1
+    nd, dev = run(mk(), ins, tmp_path / "dev", nout, labels=True)
+    nh, host = run(mk(), ins, tmp_path / "host", nout, labels=True, host=True)
+    assert nd == nh > 0
+    assert [md5(p) for p in dev] == [md5(p) for p in host]
