@@ -156,8 +156,10 @@ int cg_create(const cg_options* o, cg_ctx** out);
 void cg_destroy(cg_ctx* ctx);
 
 /* Free the device blocks cached for reuse on `device` (all devices if < 0);
- * an allocation that would fail does the same first.  No counterpart in the
- * reference (its CPU path keeps no device memory). */
+ * an allocation that would fail does the same first.  A program that resets
+ * a device (cudaDeviceReset) calls this for it first, as the cached blocks
+ * die with the reset.  No counterpart in the reference (its CPU path keeps no
+ * device memory). */
 int cg_release_cached_memory(int device);
 
 /* Message of the last failing call on this context (never NULL). */

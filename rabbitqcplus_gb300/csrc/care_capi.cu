@@ -44,9 +44,21 @@ public:
         {
             std::lock_guard<std::mutex> lock(mu_);
             // the smallest cached block of this device that holds n bytes, if
-            // it is at most twice as large
-            for (auto it = free_.lower_bound(n); it != free_.end() && it->first <= 2 * n + 4096; ++it) {
-                if (it->second.first != dev) continue;
+            // it is at most twice as large and still a live allocation (a
+            // cudaDeviceReset of the program's would have released it)
+            for (auto it = free_.lower_bound(n); it != free_.end() && it->first <= 2 * n + 4096;) {
+                if (it->second.first != dev) {
+                    ++it;
+                    continue;
+                }
+                cudaPointerAttributes attr{};
+                const bool live = cudaPointerGetAttributes(&attr, it->second.second) == cudaSuccess &&
+                                  attr.type == cudaMemoryTypeDevice && attr.device == dev;
+                if (!live) {
+                    cudaGetLastError();
+                    it = free_.erase(it);
+                    continue;
+                }
                 *p = it->second.second;
                 *got = it->first;
                 free_.erase(it);
