@@ -520,8 +520,19 @@ __device__ __forceinline__ void seq_scan_fast(uint32_t (&S)[2][MAXW + 1], const 
                 if (m < (two ? tabMax : one ? tab63 : 0x7fffffff)) step(bb);
             }
         };
-        for (const int e = min(ge, fastAll + 1 - base); bb < e; bb++)  // all lanes: two words
-            if (__popc(diff(bb, 0)) + __popc(diff(bb, 1)) < tabMax) step(bb);
+        {  // all lanes: two words
+            const int e = min(ge, fastAll + 1 - base);
+            if (MAXW <= 5) {  // two shifts per iteration: independent tests, steps in order
+                for (; bb + 1 < e; bb += 2) {
+                    const int ma = __popc(diff(bb, 0)) + __popc(diff(bb, 1));
+                    const int mb = __popc(diff(bb + 1, 0)) + __popc(diff(bb + 1, 1));
+                    if (ma < tabMax) step(bb);
+                    if (mb < tabMax) step(bb + 1);
+                }
+            }
+            for (; bb < e; bb++)
+                if (__popc(diff(bb, 0)) + __popc(diff(bb, 1)) < tabMax) step(bb);
+        }
         mixed(min(ge, max(bb, fastAny + 1 - base)));
         for (const int e = min(ge, fast1All + 1 - base); bb < e; bb++)  // all lanes: one word
             if (__popc(diff(bb, 0)) < tab63) step(bb);
