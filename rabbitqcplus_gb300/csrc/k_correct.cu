@@ -534,8 +534,18 @@ __device__ __forceinline__ void seq_scan_fast(uint32_t (&S)[2][MAXW + 1], const 
                 if (__popc(diff(bb, 0)) + __popc(diff(bb, 1)) < tabMax) step(bb);
         }
         mixed(min(ge, max(bb, fastAny + 1 - base)));
-        for (const int e = min(ge, fast1All + 1 - base); bb < e; bb++)  // all lanes: one word
-            if (__popc(diff(bb, 0)) < tab63) step(bb);
+        {  // all lanes: one word
+            const int e = min(ge, fast1All + 1 - base);
+            if (MAXW <= 5) {  // two shifts per iteration
+                for (; bb + 1 < e; bb += 2) {
+                    const int ma = __popc(diff(bb, 0)), mb = __popc(diff(bb + 1, 0));
+                    if (ma < tab63) step(bb);
+                    if (mb < tab63) step(bb + 1);
+                }
+            }
+            for (; bb < e; bb++)
+                if (__popc(diff(bb, 0)) < tab63) step(bb);
+        }
         mixed(ge);
 #pragma unroll
         for (int k = 0; k < MAXW; k++) {
