@@ -323,7 +323,34 @@ __device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params
     __syncthreads();
     const uint32_t U = nUnique;
     uint32_t* out = b.cand + off;
-    if (U <= 512) {
+    if (U <= 64) {
+        // one warp: a bitonic network over 64 slots in registers, ids i and
+        // i + 32 in lane i (padding sorts last; the ids are distinct)
+        if (tid < 32) {
+            constexpr unsigned kFull = 0xffffffffu;
+            const uint32_t lane = (uint32_t)tid;
+            uint32_t x0 = lane < U ? list[lane] : 0xffffffffu, x1 = lane + 32 < U ? list[lane + 32] : 0xffffffffu;
+#pragma unroll
+            for (uint32_t k = 2; k <= 64; k <<= 1) {
+#pragma unroll
+                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                    if (j == 32) {  // slots i and i + 32 meet in one lane (k == 64: ascending)
+                        const uint32_t lo = min(x0, x1), hi = max(x0, x1);
+                        x0 = lo;
+                        x1 = hi;
+                    } else {
+                        const uint32_t y0 = __shfl_xor_sync(kFull, x0, j), y1 = __shfl_xor_sync(kFull, x1, j);
+                        const bool lower = (lane & j) == 0;
+                        const bool asc0 = (lane & k) == 0, asc1 = ((lane + 32) & k) == 0;
+                        x0 = lower == asc0 ? min(x0, y0) : max(x0, y0);
+                        x1 = lower == asc1 ? min(x1, y1) : max(x1, y1);
+                    }
+                }
+            }
+            if (lane < U) out[lane] = x0;
+            if (lane + 32 < U) out[lane + 32] = x1;
+        }
+    } else if (U <= 512) {
         // rank of each id among the unique ids = its position in ascending order
         for (uint32_t i = tid; i < U; i += kGatherThreads) {
             const uint32_t v = list[i];
