@@ -54,6 +54,10 @@ extern "C" {
 /* per-anchor result flags */
 #define CG_RESULT_CORRECTED 1u /* anchor has a correction (TempCorrectedSequence exists) */
 #define CG_RESULT_HQ 2u        /* MSA properties marked the anchor high quality */
+/* set by cg_combine_results (candidate correction only) */
+#define CG_RESULT_CANDIDATES 4u      /* LQ correction kept: all of its >= 2 candidate corrections agree */
+#define CG_RESULT_REJECTED 8u        /* LQ correction dropped: its >= 2 candidate corrections disagree */
+#define CG_RESULT_CANDIDATE_RECORD 16u /* the read has at least one saved candidate correction record */
 
 /*
  * Options: the fields of care::ProgramOptions that change what the correction
@@ -71,10 +75,10 @@ typedef struct cg_options {
     float min_overlap_ratio;          /* min_overlap_ratio (0.3) */
     int32_t min_overlap;              /* min_overlap (30) */
     float paired_filter_threshold;    /* pairedFilterThreshold (0.06) */
-    int32_t new_columns_to_correct;   /* new_columns_to_correct (15) */
+    int32_t new_columns_to_correct;   /* new_columns_to_correct (15; 0..256 with candidate correction) */
     int32_t use_quality_scores;       /* useQualityScores */
     int32_t exclude_ambiguous_reads;  /* excludeAmbiguousReads */
-    int32_t correct_candidates;       /* correctCandidates (not supported: CG_ERR_UNSUPPORTED) */
+    int32_t correct_candidates;       /* correctCandidates (classic candidate correction; cg_combine_results) */
     int32_t pair_mode;                /* CG_PAIR_SE / CG_PAIR_PE (pairType) */
     int32_t correction_type;          /* CG_CORR_* (correctionType) */
     float threshold_anchor;           /* thresholdAnchor for the learned decision (0.5) */
@@ -143,6 +147,8 @@ typedef struct cg_stats {
     uint64_t learned_columns;         /* columns scored by the classifier */
     uint64_t learned_corrections;     /* columns it set to the consensus */
     uint64_t learned_overflow;        /* columns beyond the per-batch records (fallback decision) */
+    /* candidate correction (correct_candidates) */
+    uint64_t candidate_corrections;   /* candidates corrected by HQ anchors, accumulated */
 } cg_stats;
 
 /* Fill *o with the reference defaults. */
@@ -196,6 +202,32 @@ int cg_build_tables(cg_ctx* ctx);
  */
 int cg_correct(cg_ctx* ctx, uint64_t first_read, uint64_t num_anchors,
                uint8_t* out_flags, char* out_sequences, size_t out_pitch);
+
+/*
+ * Candidate correction (options.correct_candidates): the combine step of the
+ * output stage (reference: combineMultipleCorrectionResults1_rawtcs2,
+ * src/correctionresultoutput.cpp:1256-1551).  While correct_candidates is
+ * set, every anchor whose MSA is high quality also corrects the candidates of
+ * its final MSA that start within new_columns_to_correct columns of the
+ * anchor and end at most that far past it (reference: src/msa.cpp:457-522,
+ * include/corrector.hpp:293-299, 1504-1512, 1674-1748), and cg_correct keeps
+ * those candidate corrections in the context.  A pass is the set of
+ * cg_correct calls since the last cg_build_tables; a call on an anchor that
+ * the pass already corrected starts a new pass.  After a pass has covered
+ * every read, cg_combine_results rewrites flags[j] of read first_read + j,
+ * as cg_correct returned it, by the reference's rule: a low-quality anchor
+ * correction (CG_RESULT_CORRECTED without CG_RESULT_HQ) with two or more
+ * candidate corrections stays only if all of them equal it
+ * (CG_RESULT_CANDIDATES, label care:q=2), else the read is written unchanged
+ * (CG_RESULT_REJECTED, label care:q=0); CG_RESULT_CANDIDATE_RECORD marks
+ * reads with a candidate correction record as a single-threaded reference run
+ * saves them (a candidate record of read c made by anchor a is dropped when c
+ * < a and c is a corrected HQ anchor; include/corrector.hpp:1678-1681).  The
+ * corrected sequences need no change.  *num_candidate_records (may be NULL)
+ * gets the number of those records among the reads of the call.
+ */
+int cg_combine_results(cg_ctx* ctx, uint64_t first_read, uint64_t num_reads, uint8_t* flags,
+                       uint64_t* num_candidate_records);
 
 /*
  * Load the anchor classifier for CG_CORR_FOREST from a file image in the

@@ -109,12 +109,14 @@ class Oracle:
         return out[:cnt.value].copy()
 
     def correct(self, first: int = 0, count: int | None = None, threads: int | None = None):
-        """Returns (flags[count], corrected[count, max_length], counters[7])."""
+        """Returns (flags[count], corrected[count, max_length], counters[8]).  With
+        candidate correction the range is the whole read set and the flags are
+        combined as cg_combine_results combines them."""
         if count is None:
             count = self.n - first
         flags = np.zeros(count, dtype=np.uint8)
         seqs = np.zeros((count, max(self.max_length, 1)), dtype=np.uint8)
-        counters = np.zeros(7, dtype=np.uint64)
+        counters = np.zeros(8, dtype=np.uint64)
         rc = self._L.orc_correct(self._h, first, count, flags.ctypes.data, seqs.ctypes.data, seqs.shape[1],
                                  threads or self.threads, counters.ctypes.data)
         if rc != 0:

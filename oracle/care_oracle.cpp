@@ -139,6 +139,15 @@ struct Forest {
     float thresh = 0.5f;
 };
 
+// A candidate correction record (reference: TempCorrectedSequence of type
+// Candidate, include/corrector.hpp:1674-1748): read `read` corrected by the
+// MSA of anchor `anchor`, in the read's forward orientation.
+struct CandRec {
+    uint32_t read;
+    uint32_t anchor;
+    std::string seq;
+};
+
 struct Oracle {
     cg_options o;
     Forest forest;
@@ -661,11 +670,36 @@ struct Counters {
     uint64_t raw = 0, uniq = 0, aligned = 0, msaCands = 0, msaBuilds = 0, corrected = 0, hq = 0;
 };
 
+// reference: include/corrector.hpp:1504-1512 (correctCandidatesClassic) and
+// src/msa.cpp:457-522 (getCorrectedCandidates): every candidate of the final
+// MSA whose first column lies within nc columns of the anchor's first column
+// and whose last column ends at most nc columns past the anchor's end gets
+// the consensus of its columns (the support and coverage test computed there
+// is overwritten by `candidateShouldBeCorrected = true`).  A reverse-
+// complement candidate's record holds the reverse complement of that slice
+// (include/corrector.hpp:1686-1702).
+void candidateCorrections(const Msa& m, const std::vector<Cand>& kept, int nc, uint64_t anchor,
+                          std::vector<CandRec>& out) {
+    for (const auto& c : kept) {
+        const int qb = m.begin + c.aln.shift;
+        const int qe = qb + c.len;
+        if (!(m.begin - nc <= qb && qb <= m.begin + nc && qe <= m.end + nc)) continue;
+        std::string s(m.cons.begin() + qb, m.cons.begin() + qe);
+        if (c.orient == 2) {
+            std::string f(s.size(), 'A');
+            for (size_t i = 0; i < s.size(); i++) f[i] = complementChar(s[s.size() - 1 - i]);
+            s.swap(f);
+        }
+        out.push_back(CandRec{c.id, uint32_t(anchor), std::move(s)});
+    }
+}
+
 // reference: include/corrector.hpp:145-312 (process) and 325-513 (processMulti):
 // candidates -> alignments -> orientation -> filters -> MSA -> refinement ->
 // anchor correction.  Returns the CG_RESULT_* flags.
 uint8_t correctOne(const Oracle& O, uint64_t anchor, const std::vector<uint32_t>& candIds,
-                   const std::vector<char>& paired, std::string& corrected, Counters& cnt) {
+                   const std::vector<char>& paired, std::string& corrected, Counters& cnt,
+                   std::vector<CandRec>& recs) {
     const Store& s = O.s;
     const cg_options& o = O.o;
     const int La = s.len[anchor];
@@ -701,8 +735,17 @@ uint8_t correctOne(const Oracle& O, uint64_t anchor, const std::vector<uint32_t>
         c.paired = paired.empty() ? false : paired[i] != 0;
         c.seq = ori == 1 ? fwd : rcs;
         if (o.use_quality_scores) {
-            c.qual.assign(&s.qual[id * size_t(s.Lmax)], Lc);
-            if (ori == 2) std::reverse(c.qual.begin(), c.qual.end());
+            // include/corrector.hpp:1214-1239: rows of Lmax qualities (zero past
+            // the read's end, include/chunkedreadstorage.hpp:532-610); a reverse-
+            // complement candidate's whole row is reversed, so a read shorter than
+            // Lmax takes zeros first
+            const char* row = &s.qual[id * size_t(s.Lmax)];
+            if (ori == 2) {
+                c.qual.assign(size_t(Lc), 0);
+                for (int i = 0; i < Lc; i++) c.qual[i] = row[s.Lmax - 1 - i];
+            } else {
+                c.qual.assign(row, Lc);
+            }
         }
         cs.push_back(std::move(c));
     }
@@ -756,6 +799,8 @@ uint8_t correctOne(const Oracle& O, uint64_t anchor, const std::vector<uint32_t>
         cnt.msaBuilds++;
     }
     const Props p = msaProperties(m, o.estimated_errorrate, o.estimated_coverage, o.m_coverage);
+    // include/corrector.hpp:293-299: candidates are corrected by HQ anchors
+    if (o.correct_candidates && p.isHQ) candidateCorrections(m, kept, o.new_columns_to_correct, anchor, recs);
     if (o.correction_type == CG_CORR_FOREST) {
         // correctAnchorClf: include/corrector.hpp:1448-1472
         corrected.assign(m.cons.begin() + m.begin, m.cons.begin() + m.end);
@@ -777,6 +822,41 @@ uint8_t correctOne(const Oracle& O, uint64_t anchor, const std::vector<uint32_t>
     cnt.corrected++;
     if (p.isHQ) cnt.hq++;
     return uint8_t(CG_RESULT_CORRECTED | (p.isHQ ? CG_RESULT_HQ : 0));
+}
+
+// reference: src/correctionresultoutput.cpp:1256-1551
+// (combineMultipleCorrectionResults1_rawtcs2) over the records of a whole run,
+// with the record filter of include/corrector.hpp:1678-1681 as a
+// single-threaded run applies it (anchors in id order; a candidate record of
+// read c made by anchor a is dropped when c < a and c was corrected as an HQ
+// anchor).  Only a low-quality anchor correction with two or more candidate
+// records changes: it stays if every record equals it, else the read is
+// written unchanged.  Returns the number of saved candidate records.
+uint64_t combine(std::vector<CandRec>& recs, uint8_t* flags, const char* out, size_t pitch, const Store& s) {
+    std::sort(recs.begin(), recs.end(), [](const CandRec& x, const CandRec& y) {
+        return x.read != y.read ? x.read < y.read : x.anchor < y.anchor;
+    });
+    uint64_t saved = 0;
+    for (size_t i = 0; i < recs.size();) {
+        size_t j = i;
+        while (j < recs.size() && recs[j].read == recs[i].read) j++;
+        const uint32_t r = recs[i].read;
+        const uint8_t f = flags[r];
+        const bool hqAnchor = (f & CG_RESULT_CORRECTED) && (f & CG_RESULT_HQ);
+        uint64_t k = 0;
+        bool same = true;
+        for (size_t t = i; t < j; t++) {
+            if (hqAnchor && r < recs[t].anchor) continue;
+            k++;
+            if (f & CG_RESULT_CORRECTED) same &= recs[t].seq.compare(0, std::string::npos, out + r * pitch, s.len[r]) == 0;
+        }
+        saved += k;
+        if (k > 0) flags[r] |= CG_RESULT_CANDIDATE_RECORD;
+        if ((f & CG_RESULT_CORRECTED) && !(f & CG_RESULT_HQ) && k >= 2)
+            flags[r] |= same ? CG_RESULT_CANDIDATES : CG_RESULT_REJECTED;
+        i = j;
+    }
+    return saved;
 }
 
 }  // namespace
@@ -899,15 +979,19 @@ int orc_candidates(void* h, uint64_t anchor, uint32_t* out, uint32_t cap, uint32
 }
 
 // Corrects anchors [first, first+count); flags and corrected sequences as in
-// cg_correct.  counters (7 entries, may be NULL): raw ids, unique candidates,
-// aligned, msa candidates, msa builds, corrected, hq.
+// cg_correct.  With candidate correction the range must be the whole read set
+// and the flags come out as cg_combine_results leaves them.  counters (8
+// entries, may be NULL): raw ids, unique candidates, aligned, msa candidates,
+// msa builds, corrected, hq, saved candidate records.
 int orc_correct(void* h, uint64_t first, uint64_t count, uint8_t* flags, char* out, size_t pitch, int threads,
                 uint64_t* counters) {
     const Oracle* O = static_cast<Oracle*>(h);
     if (first + count > O->s.n) return CG_ERR_INVALID_ARGUMENT;
     const bool pe = O->o.pair_mode == CG_PAIR_PE;
     if (pe && ((first | count) & 1)) return CG_ERR_INVALID_ARGUMENT;
+    if (O->o.correct_candidates && (first != 0 || count != O->s.n)) return CG_ERR_INVALID_ARGUMENT;
     Counters total;
+    std::vector<CandRec> allRecs;
     const int64_t units = int64_t(pe ? count / 2 : count);
 #pragma omp parallel num_threads(threads)
     {
@@ -915,12 +999,13 @@ int orc_correct(void* h, uint64_t first, uint64_t count, uint8_t* flags, char* o
         std::vector<uint32_t> c1, c2;
         std::vector<char> f1, f2, none;
         std::string corr;
+        std::vector<CandRec> recs;
 #pragma omp for schedule(dynamic, 8)
         for (int64_t u = 0; u < units; u++) {
             if (!pe) {
                 const uint64_t a = first + uint64_t(u);
                 candidates(*O, a, c1, &cnt.raw);
-                const uint8_t f = correctOne(*O, a, c1, none, corr, cnt);
+                const uint8_t f = correctOne(*O, a, c1, none, corr, cnt, recs);
                 flags[a - first] = f;
                 if (f & CG_RESULT_CORRECTED) std::memcpy(out + (a - first) * pitch, corr.data(), corr.size());
             } else {
@@ -928,10 +1013,10 @@ int orc_correct(void* h, uint64_t first, uint64_t count, uint8_t* flags, char* o
                 candidates(*O, a, c1, &cnt.raw);
                 candidates(*O, a + 1, c2, &cnt.raw);
                 pairFlags(c1, c2, f1, f2);
-                const uint8_t fa = correctOne(*O, a, c1, f1, corr, cnt);
+                const uint8_t fa = correctOne(*O, a, c1, f1, corr, cnt, recs);
                 flags[a - first] = fa;
                 if (fa & CG_RESULT_CORRECTED) std::memcpy(out + (a - first) * pitch, corr.data(), corr.size());
-                const uint8_t fb = correctOne(*O, a + 1, c2, f2, corr, cnt);
+                const uint8_t fb = correctOne(*O, a + 1, c2, f2, corr, cnt, recs);
                 flags[a + 1 - first] = fb;
                 if (fb & CG_RESULT_CORRECTED) std::memcpy(out + (a + 1 - first) * pitch, corr.data(), corr.size());
             }
@@ -941,12 +1026,14 @@ int orc_correct(void* h, uint64_t first, uint64_t count, uint8_t* flags, char* o
             total.raw += cnt.raw; total.uniq += cnt.uniq; total.aligned += cnt.aligned;
             total.msaCands += cnt.msaCands; total.msaBuilds += cnt.msaBuilds;
             total.corrected += cnt.corrected; total.hq += cnt.hq;
+            for (auto& r : recs) allRecs.push_back(std::move(r));
         }
     }
+    const uint64_t saved = O->o.correct_candidates ? combine(allRecs, flags, out, pitch, O->s) : 0;
     if (counters) {
         counters[0] = total.raw; counters[1] = total.uniq; counters[2] = total.aligned;
         counters[3] = total.msaCands; counters[4] = total.msaBuilds; counters[5] = total.corrected;
-        counters[6] = total.hq;
+        counters[6] = total.hq; counters[7] = saved;
     }
     return 0;
 }

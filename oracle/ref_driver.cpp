@@ -26,7 +26,7 @@ static void usage() {
     std::fprintf(stderr,
                  "ref_driver -i in1 [-i in2] -o out1 [-o out2] -d outdir -c cov "
                  "[-k 20] [-h 48] [-t threads] [--pe] [-q] [--candidates] "
-                 "[--exclude-ambiguous] [--forest file] [--print] [--tempdir dir]\n");
+                 "[--exclude-ambiguous] [--forest file] [--print] [--labels] [--new-columns n] [--tempdir dir]\n");
 }
 
 int main(int argc, char** argv) {
@@ -69,6 +69,8 @@ int main(int argc, char** argv) {
         else if (a == "--print") {
             o.correctionType = care::CorrectionType::Print;
         }
+        else if (a == "--labels") o.outputCorrectionQualityLabels = true;
+        else if (a == "--new-columns") o.new_columns_to_correct = std::stoi(next());
         else if (a == "--tempdir") o.tempdirectory = next();
         else { usage(); return 2; }
     }

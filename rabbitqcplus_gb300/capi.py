@@ -20,6 +20,7 @@ CG_MAX_HASHMAPS = 48
 CG_PAIR_SE, CG_PAIR_PE = 0, 1
 CG_CORR_CLASSIC, CG_CORR_FOREST, CG_CORR_PRINT, CG_CORR_LEARNED = 0, 1, 2, 3
 CG_RESULT_CORRECTED, CG_RESULT_HQ = 1, 2
+CG_RESULT_CANDIDATES, CG_RESULT_REJECTED, CG_RESULT_CANDIDATE_RECORD = 4, 8, 16
 CG_DRIVER_PLAIN, CG_DRIVER_BATCHED = 0, 1
 
 
@@ -89,7 +90,8 @@ class CgStats(ctypes.Structure):
         ("seconds_filter", ctypes.c_double), ("batch_anchors", ctypes.c_int32), ("align_blocks", ctypes.c_int32),
         ("msa_warps", ctypes.c_int32), ("streams", ctypes.c_int32), ("seconds_tune", ctypes.c_double),
         ("graph_replays", ctypes.c_uint64), ("learned_columns", ctypes.c_uint64),
-        ("learned_corrections", ctypes.c_uint64), ("learned_overflow", ctypes.c_uint64)]
+        ("learned_corrections", ctypes.c_uint64), ("learned_overflow", ctypes.c_uint64),
+        ("candidate_corrections", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
@@ -100,7 +102,8 @@ EXPORTED = ["cg_default_options", "cg_create", "cg_destroy", "cg_last_error", "c
             "cg_build_tables", "cg_correct", "cg_get_stats", "cg_get_read_info", "cg_get_signatures",
             "cg_get_candidates", "cg_correct_files", "cg_load_forest", "cg_get_candidates_noalloc",
             "cg_classifier_size", "cg_load_classifier", "cg_get_columns", "cg_default_train_options",
-            "cg_train_classifier", "cg_classifier_gradients", "cg_classifier_logits", "cg_release_cached_memory"]
+            "cg_train_classifier", "cg_classifier_gradients", "cg_classifier_logits", "cg_release_cached_memory",
+            "cg_combine_results"]
 CLASSIFIER_FEATURES = 32
 CLASSIFIER_PARAMS = 6337  # w1 64x32, w2 64x64, w3 64, b1 64, b2 64, b3
 
@@ -141,6 +144,7 @@ def gpu_lib() -> ctypes.CDLL:
         L.cg_build_tables.argtypes = [P]
         L.cg_correct.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, P, P, ctypes.c_size_t]
         L.cg_get_stats.argtypes = [P, P]
+        L.cg_combine_results.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, P, ctypes.POINTER(ctypes.c_uint64)]
         L.cg_get_read_info.argtypes = [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int32)]
         L.cg_get_signatures.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, P]
         L.cg_get_candidates.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
@@ -210,7 +214,10 @@ class CareGpu:
         return n.value, l.value
 
     def correct(self, first: int = 0, count: int | None = None, flags: np.ndarray | None = None,
-                out: np.ndarray | None = None):
+                out: np.ndarray | None = None, combine: bool | None = None):
+        """cg_correct over [first, first + count).  With candidate correction and
+        a call that covers every read, the flags also go through
+        cg_combine_results (combine=False keeps cg_correct's flags)."""
         n, lmax = self.read_info()
         if count is None:
             count = n - first
@@ -220,7 +227,20 @@ class CareGpu:
             out = np.zeros((count, max(lmax, 1)), dtype=np.uint8)
         self._check(self._L.cg_correct(self._h, first, count, flags.ctypes.data, out.ctypes.data, out.strides[0]),
                     "cg_correct")
+        if combine is None:
+            combine = bool(self.options.correct_candidates) and first == 0 and count == n
+        if combine:
+            self.combine(0, flags)
         return flags, out
+
+    def combine(self, first: int, flags: np.ndarray) -> int:
+        """cg_combine_results on flags of reads [first, first + len(flags)), in
+        place; returns the number of saved candidate records among them."""
+        flags = np.ascontiguousarray(flags, dtype=np.uint8)
+        recs = ctypes.c_uint64()
+        self._check(self._L.cg_combine_results(self._h, first, len(flags), flags.ctypes.data, ctypes.byref(recs)),
+                    "cg_combine_results")
+        return recs.value
 
     def stats(self) -> dict:
         s = CgStats()
@@ -282,12 +302,13 @@ class CareGpu:
 
 def apply_corrections(sequences: np.ndarray, offsets: np.ndarray, flags: np.ndarray,
                       corrected: np.ndarray) -> np.ndarray:
-    """Output reads as the reference's STEP3 writes them for anchor-only
-    correction (src/correctionresultoutput.cpp:1256-1510): a read with a
-    correction record becomes its corrected sequence, others stay unchanged."""
+    """Output reads as the reference's STEP3 writes them
+    (src/correctionresultoutput.cpp:1256-1551): a read with an anchor
+    correction becomes its corrected sequence unless the combine step rejected
+    it (CG_RESULT_REJECTED); others stay unchanged."""
     out = np.array(sequences, dtype=np.uint8, copy=True)
     lens = np.diff(offsets).astype(np.int64)
-    idx = np.nonzero(flags & CG_RESULT_CORRECTED)[0]
+    idx = np.nonzero(((flags & CG_RESULT_CORRECTED) != 0) & ((flags & CG_RESULT_REJECTED) == 0))[0]
     for i in idx:
         b = int(offsets[i])
         out[b:b + lens[i]] = corrected[i, :lens[i]]

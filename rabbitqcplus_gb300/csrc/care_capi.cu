@@ -259,6 +259,11 @@ struct cg_ctx {
     DevBuf forestNodes, treeOffsets;
     int numTrees = 0;
 
+    // candidate correction (correct_candidates): per-read votes (Params) and
+    // the anchors the current pass has corrected, one bit per read
+    DevBuf candVotes, candAnd, candOr, combineFlags, combineCount;
+    std::vector<uint64_t> candPass;
+
     cg_stats stats{};
 };
 
@@ -337,11 +342,50 @@ void make_params(cg_ctx* c) {
     p.treeOffsets = c->treeOffsets.as<uint32_t>();
     p.numTrees = c->numTrees;
     p.forestThreshold = o.threshold_anchor;
+    p.candidates = o.correct_candidates != 0;
+    p.newColumns = o.new_columns_to_correct;
+    p.candPitch = (c->lmax + 31) / 32;
+    p.candVotes = c->candVotes.as<uint2>();
+    p.candAnd = c->candAnd.as<unsigned long long>();
+    p.candOr = c->candOr.as<unsigned long long>();
     // include/qualityscoreweights.hpp:17-33
     for (int i = 0; i < 256; i++) {
         const float e = i < 33 ? 1.0f : std::pow(10.0f, -(i - 33) / 10.0f);
         p.qweight[i] = std::max(0.001f, 1.0f - e);
     }
+}
+
+// A new candidate-correction pass: no votes, no anchors corrected.
+int reset_candidates(cg_ctx* c) {
+    const size_t words = c->n * (size_t)((c->lmax + 31) / 32);
+    CG_CUDA(c, cudaMemsetAsync(c->candVotes.p, 0, c->n * sizeof(uint2), c->stream));
+    CG_CUDA(c, cudaMemsetAsync(c->candAnd.p, 0xff, words * sizeof(unsigned long long), c->stream));
+    CG_CUDA(c, cudaMemsetAsync(c->candOr.p, 0, words * sizeof(unsigned long long), c->stream));
+    c->candPass.assign((c->n + 63) / 64, 0ull);
+    return CG_OK;
+}
+
+// Marks anchors [first, first + num) as corrected by the current pass; one
+// that the pass already corrected starts a new pass first.
+int mark_pass(cg_ctx* c, uint64_t first, uint64_t num) {
+    auto bits = [&](bool set) {
+        bool any = false;
+        for (uint64_t i = first; i < first + num;) {
+            const uint64_t w = i >> 6, b0 = i & 63;
+            const uint64_t cnt = std::min<uint64_t>(64 - b0, first + num - i);
+            const uint64_t m = (cnt == 64 ? ~0ull : ((1ull << cnt) - 1)) << b0;
+            any |= (c->candPass[w] & m) != 0;
+            if (set) c->candPass[w] |= m;
+            i += cnt;
+        }
+        return any;
+    };
+    if (bits(false)) {
+        const int rc = reset_candidates(c);
+        if (rc != CG_OK) return rc;
+    }
+    bits(true);
+    return CG_OK;
 }
 
 StoreArg store_arg(const cg_ctx* c) {
@@ -694,6 +738,10 @@ int run_batch(cg_ctx* c, uint64_t first, int count, uint8_t* hFlags, char* hOut,
                                     c->stream));
         c->stats.kernel_launches += 1;
     }
+    if (c->params.candidates) {
+        CG_CUDA(c, launch_anchor_vote(st, c->params, b, c->stream));
+        c->stats.kernel_launches += 1;
+    }
     CG_CUDA(c, cudaEventRecord(c->st3, c->stream));
     c->stats.kernel_launches += 3;
     c->stats.align_launches += 1;
@@ -821,6 +869,10 @@ cudaError_t enqueue_batch(cg_ctx* c, BatchSet& s, int count, unsigned long long 
     if (e == cudaSuccess && learned) {
         e = launch_mlp_infer(c->mlp.as<unsigned char>(), b.colFeat, b.colMeta, b.colCount, 0, b.colCap, c->minLogit,
                              b.out, b.outPitch, nullptr, b.counters, infer_blocks(c), s.stream);
+        k++;
+    }
+    if (e == cudaSuccess && c->params.candidates) {
+        e = launch_anchor_vote(st, c->params, b, s.stream);
         k++;
     }
     if (e == cudaSuccess) {
@@ -1040,6 +1092,12 @@ int plan_for(cg_ctx* c, uint64_t first, uint64_t num, Plan* out) {
     const size_t cbytes = kNumCounters * sizeof(unsigned long long);
     CG_CUDA(c, c->counterSave.ensure(cbytes));
     CG_CUDA(c, cudaMemcpyAsync(c->counterSave.p, c->counters.p, cbytes, cudaMemcpyDeviceToDevice, c->stream));
+    // the trials run without candidate correction: their votes would join the pass
+    const int cand = c->params.candidates;
+    if (cand) {
+        c->params.candidates = 0;
+        c->paramsVersion++;
+    }
     const StoreArg st = store_arg(c);
     const int sms = sm_count(c);
     const int occA = std::max(align_lane_occupancy(st), 1);
@@ -1080,6 +1138,10 @@ int plan_for(cg_ctx* c, uint64_t first, uint64_t num, Plan* out) {
             p.batch = bsz;
             if ((rc = trial(p)) != CG_OK) break;
         }
+    }
+    if (cand) {
+        c->params.candidates = cand;
+        c->paramsVersion++;
     }
     CG_CUDA(c, cudaMemcpyAsync(c->counters.p, c->counterSave.p, cbytes, cudaMemcpyDeviceToDevice, c->stream));
     CG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -1179,7 +1241,8 @@ int cg_create(const cg_options* o, cg_ctx** out) {
     if (o->kmerlength < 0 || o->kmerlength > 32) return CG_ERR_INVALID_ARGUMENT;
     if (!(o->estimated_coverage > 0.0f)) return CG_ERR_INVALID_ARGUMENT;
     if (o->pair_mode != CG_PAIR_SE && o->pair_mode != CG_PAIR_PE) return CG_ERR_INVALID_ARGUMENT;
-    if (o->correct_candidates) return CG_ERR_UNSUPPORTED;
+    if (o->correct_candidates && (o->new_columns_to_correct < 0 || o->new_columns_to_correct > 256))
+        return CG_ERR_UNSUPPORTED;
     if (o->correction_type != CG_CORR_CLASSIC && o->correction_type != CG_CORR_FOREST &&
         o->correction_type != CG_CORR_LEARNED)
         return CG_ERR_UNSUPPORTED;
@@ -1304,6 +1367,14 @@ int cg_build_tables(cg_ctx* c) {
     if (rc != CG_OK) return rc;
     rc = build_tables(c);
     if (rc != CG_OK) return rc;
+    if (c->o.correct_candidates) {
+        const size_t words = c->n * (size_t)((c->lmax + 31) / 32);
+        CG_CUDA(c, c->candVotes.ensure(c->n * sizeof(uint2)));
+        CG_CUDA(c, c->candAnd.ensure(words * sizeof(unsigned long long)));
+        CG_CUDA(c, c->candOr.ensure(words * sizeof(unsigned long long)));
+        rc = reset_candidates(c);
+        if (rc != CG_OK) return rc;
+    }
     make_params(c);
     if (c->o.driver == CG_DRIVER_BATCHED) {
         // raw id counts per read: part of the index the batched driver reads
@@ -1343,6 +1414,10 @@ int cg_correct(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* out_flags, char
     if (c->o.correction_type == CG_CORR_LEARNED && c->lmax > 256)
         return fail(c, CG_ERR_UNSUPPORTED, "learned correction supports reads up to 256 bp (longest is %d)", c->lmax);
     CG_CUDA(c, cudaSetDevice(c->device));
+    if (c->params.candidates) {
+        const int rc = mark_pass(c, first, num);
+        if (rc != CG_OK) return rc;
+    }
     if (c->o.driver == CG_DRIVER_BATCHED) return correct_batched(c, first, num, out_flags, out_seq, out_pitch);
     int B = c->o.batch_anchors > 0 ? c->o.batch_anchors : 65536;
     if (c->params.paired && (B & 1)) B++;
@@ -1358,6 +1433,23 @@ int cg_correct(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* out_flags, char
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     c->stats.seconds_correct = ms / 1000.0;
     c->stats.num_anchors_processed += num;
+    return CG_OK;
+}
+
+int cg_combine_results(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* flags, uint64_t* num_candidate_records) {
+    if (!c) return CG_ERR_INVALID_ARGUMENT;
+    if (!c->built) return fail(c, CG_ERR_STATE, "cg_build_tables has not run");
+    if (!c->params.candidates) return fail(c, CG_ERR_STATE, "candidate correction is off (correct_candidates)");
+    if (first + num > c->n || first + num < first) return fail(c, CG_ERR_INVALID_ARGUMENT, "read range out of bounds");
+    if (num_candidate_records) *num_candidate_records = 0;
+    if (num == 0) return CG_OK;
+    if (!flags) return fail(c, CG_ERR_INVALID_ARGUMENT, "flags missing");
+    CG_CUDA(c, cudaSetDevice(c->device));
+    CG_CUDA(c, c->combineFlags.ensure(num));
+    CG_CUDA(c, cudaMemcpyAsync(c->combineFlags.p, flags, num, cudaMemcpyHostToDevice, c->stream));
+    const int rc = cg::combine_into_device(c, first, num, c->combineFlags.as<uint8_t>(), num_candidate_records);
+    if (rc != CG_OK) return rc;
+    CG_CUDA(c, cudaMemcpy(flags, c->combineFlags.p, num, cudaMemcpyDeviceToHost));
     return CG_OK;
 }
 
@@ -1380,6 +1472,7 @@ int cg_get_stats(const cg_ctx* c, cg_stats* out) {
     s.learned_columns = cnt[kCounterColumns];
     s.learned_corrections = cnt[kCounterLearnedTaken];
     s.learned_overflow = cnt[kCounterColumnOverflow];
+    s.candidate_corrections = cnt[kCounterCandidateVotes];
     *out = s;
     return CG_OK;
 }
@@ -1698,6 +1791,20 @@ int append_device_chunk(cg_ctx* c, void* dChars, uint64_t* dOffs, void* dQual, u
     }
     c->appended += n;
     c->appendLmax = std::max(c->appendLmax, lmax);
+    return CG_OK;
+}
+
+int combine_into_device(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* dFlags, uint64_t* records) {
+    if (!c || !c->params.candidates) return CG_ERR_STATE;
+    CG_CUDA(c, c->combineCount.ensure(sizeof(unsigned long long)));
+    CG_CUDA(c, cudaMemsetAsync(c->combineCount.p, 0, sizeof(unsigned long long), c->stream));
+    CG_CUDA(c, launch_combine(store_arg(c), c->params, first, num, dFlags, c->combineCount.as<unsigned long long>(),
+                              c->stream));
+    c->stats.kernel_launches += 1;
+    unsigned long long n = 0;
+    CG_CUDA(c, cudaMemcpyAsync(&n, c->combineCount.p, sizeof(n), cudaMemcpyDeviceToHost, c->stream));
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (records) *records = n;
     return CG_OK;
 }
 

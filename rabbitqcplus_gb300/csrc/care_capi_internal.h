@@ -19,6 +19,10 @@ int append_device_chunk(cg_ctx* c, void* dChars, uint64_t* dOffs, void* dQual, u
 // cg_correct with flags[num] and sequences[num][pitch] in device memory.
 int correct_into_device(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* dFlags, char* dSeq, size_t pitch);
 
+// cg_combine_results with flags[num] in device memory (candidate correction
+// on); *records (may be null) gets the saved candidate records of the reads.
+int combine_into_device(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* dFlags, uint64_t* records);
+
 }  // namespace cg
 
 #endif

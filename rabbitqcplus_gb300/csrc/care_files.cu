@@ -181,14 +181,17 @@ __device__ __forceinline__ char upper_acgt(char ch) {
 constexpr int kLabelLen = 9;  // " care:q=N"
 
 // Record rules per read: mode 0 original sequence, 1 corrected bases as
-// edits, 2 corrected sequence whole; status 0 (no record), 1 or 3 (HQ); the
-// size of the read's FASTQ record.
+// edits, 2 corrected sequence whole; status = the quality label (0 none, 1 LQ
+// anchor only, 2 LQ confirmed by candidates, 3 HQ); the size of the read's
+// FASTQ record without the label.  *last = 1 + the index (base + i) of the
+// last read with a correction record (anchor or candidate): the reference
+// labels no read after it (src/correctionresultoutput.cpp:370-377, 896-901).
 __global__ void plan_kernel(const ReadIdx* __restrict__ reads, uint64_t n, const uint8_t* __restrict__ flags,
-                            const char* __restrict__ corr, int pitch, int labels, uint8_t* __restrict__ mode,
+                            const char* __restrict__ corr, int pitch, uint8_t* __restrict__ mode,
                             uint8_t* __restrict__ status, unsigned long long* __restrict__ size,
-                            unsigned long long* records) {
+                            unsigned long long* records, unsigned int* last, uint64_t base) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t rec = 0;
+    uint32_t rec = 0, lastHere = 0;
     if (i < n) {
         const ReadIdx r = reads[i];
         const int len = (int)r.seqLen;
@@ -215,33 +218,51 @@ __global__ void plan_kernel(const ReadIdx* __restrict__ reads, uint64_t n, const
                 }
             }
         }
+        rec = st != 0;
+        // the combine step (candidate correction): a rejected LQ correction
+        // keeps its record but writes the read unchanged
+        if (f & CG_RESULT_REJECTED) {
+            md = 0;
+            st = 0;
+        } else if (st == 1 && (f & CG_RESULT_CANDIDATES)) {
+            st = 2;
+        }
         mode[i] = md;
         status[i] = st;
-        rec = st != 0;
-        size[i] = 2ull * len + r.hdrLen + 6 + (labels ? kLabelLen : 0);
+        if (rec || (f & CG_RESULT_CANDIDATE_RECORD)) lastHere = (uint32_t)(base + i + 1);
+        size[i] = 2ull * len + r.hdrLen + 6;
     }
     rec = __reduce_add_sync(0xffffffffu, rec);
+    lastHere = __reduce_max_sync(0xffffffffu, lastHere);
     if ((threadIdx.x & 31) == 0 && rec) atomicAdd(records, (unsigned long long)rec);
+    if ((threadIdx.x & 31) == 0 && lastHere) atomicMax(last, lastHere);
+}
+
+// labelled(k) = labels and read k is not after the last record
+__device__ __forceinline__ bool labelled(int labels, uint64_t k, const unsigned int* last) {
+    return labels && k < (uint64_t)*last;
 }
 
 __global__ void mask_kernel(const unsigned long long* __restrict__ size, const uint8_t* __restrict__ readOut,
-                            uint64_t n, uint8_t f, unsigned long long* __restrict__ out) {
+                            uint64_t n, uint8_t f, int labels, const unsigned int* __restrict__ last, uint64_t base,
+                            unsigned long long* __restrict__ out) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i <= n) out[i] = i < n && readOut[i] == f ? size[i] : 0ull;
+    if (i <= n)
+        out[i] = i < n && readOut[i] == f ? size[i] + (labelled(labels, base + i, last) ? kLabelLen : 0) : 0ull;
 }
 
 // one warp per read of output f: "@header[ care:q=N]\nSEQ\n+\nQUAL\n"
 __global__ void write_kernel(const ReadIdx* __restrict__ reads, uint64_t n, const uint8_t* __restrict__ readOut,
                              uint8_t f, const unsigned long long* __restrict__ pos, const uint8_t* __restrict__ mode,
                              const uint8_t* __restrict__ status, const char* __restrict__ corr, int pitch, int labels,
-                             char* __restrict__ out) {
+                             const unsigned int* __restrict__ last, uint64_t base, char* __restrict__ out) {
     const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= n || readOut[i] != f) return;
     const uint32_t lane = threadIdx.x & 31;
     const ReadIdx r = reads[i];
     char* o = out + pos[i];
-    const uint32_t hl = r.hdrLen, lab = labels ? kLabelLen : 0;
-    const char st = status[i] == 3 ? '3' : status[i] == 1 ? '1' : '0';
+    const uint32_t hl = r.hdrLen, lab = labelled(labels, base + i, last) ? kLabelLen : 0;
+    const char st = (char)('0' + status[i]);
     const char* label = " care:q=";  // src/correctionresultoutput.cpp:403-414
     for (uint32_t k = lane; k < hl + lab + 2; k += 32) {
         char ch;
@@ -466,31 +487,40 @@ int correct_fastq_on_device(const cg_options& options, const std::vector<ByteSpa
     // ---- STEP2 and STEP3 per range of reads (one range unless the caller
     // takes the output range by range): correction into device memory, then
     // the range's records of every output file
-    DMem mode, status, size, recCount, pos, tmp;
+    DMem mode, status, size, recCount, lastRec, pos, tmp;
     DCHECK(mode.alloc(n));
     DCHECK(status.alloc(n));
     DCHECK(size.alloc(n * sizeof(unsigned long long)));
     DCHECK(recCount.alloc(sizeof(unsigned long long)));
     DCHECK(cudaMemsetAsync(recCount.p, 0, sizeof(unsigned long long), s));
+    DCHECK(lastRec.alloc(sizeof(unsigned int)));
+    DCHECK(cudaMemsetAsync(lastRec.p, 0, sizeof(unsigned int), s));
     DCHECK(pos.alloc((n + 1) * sizeof(unsigned long long)));
     DCHECK(tmp.alloc(scan_tmp_bytes(n + 1)));
     run->outputs.clear();
     run->outputs.resize((size_t)numOutputs);
     run->outputSizes.assign((size_t)numOutputs, 0);
-    const uint64_t range = run->onChunk ? std::max<uint64_t>(262144, (n / 4 + 1) & ~1ull) : n;  // even
+    // One range when a read's output depends on reads after it: candidate
+    // corrections come from any anchor, and the labels stop after the last
+    // record of the whole run.
+    const bool oneRange = !run->onChunk || qualityLabels || options.correct_candidates;
+    const uint64_t range = oneRange ? n : std::max<uint64_t>(262144, (n / 4 + 1) & ~1ull);  // even
+    uint64_t candRecords = 0;
     for (uint64_t r0 = 0; r0 < n; r0 += range) {
         const uint64_t m = std::min(range, n - r0);
         uint8_t* fl = flagsOut.as<uint8_t>() + r0;
         char* sq = seqOut.as<char>() + r0 * (uint64_t)pitch;
         LCHECK(ctx.c, correct_into_device(ctx.c, r0, m, fl, sq, (size_t)pitch));
-        plan_kernel<<<grid_for(m, 256), 256, 0, s>>>(reads + r0, m, fl, sq, pitch, qualityLabels ? 1 : 0,
-                                                     mode.as<uint8_t>() + r0, status.as<uint8_t>() + r0,
-                                                     size.as<unsigned long long>() + r0,
-                                                     recCount.as<unsigned long long>());
+        if (options.correct_candidates) LCHECK(ctx.c, combine_into_device(ctx.c, r0, m, fl, &candRecords));
+        plan_kernel<<<grid_for(m, 256), 256, 0, s>>>(reads + r0, m, fl, sq, pitch, mode.as<uint8_t>() + r0,
+                                                     status.as<uint8_t>() + r0, size.as<unsigned long long>() + r0,
+                                                     recCount.as<unsigned long long>(),
+                                                     lastRec.as<unsigned int>(), r0);
         DCHECK(cudaGetLastError());
         for (int f = 0; f < numOutputs; f++) {
             mask_kernel<<<grid_for(m + 1, 256), 256, 0, s>>>(size.as<unsigned long long>() + r0,
                                                              readOut.as<uint8_t>() + r0, m, (uint8_t)f,
+                                                             qualityLabels ? 1 : 0, lastRec.as<unsigned int>(), r0,
                                                              pos.as<unsigned long long>());
             DCHECK(cudaGetLastError());
             DCHECK(scan_exclusive_u64(pos.as<unsigned long long>(), m + 1, tmp.p, s));
@@ -504,7 +534,8 @@ int correct_fastq_on_device(const cg_options& options, const std::vector<ByteSpa
             write_kernel<<<grid_for(m * 32, 256), 256, 0, s>>>(reads + r0, m, readOut.as<uint8_t>() + r0, (uint8_t)f,
                                                                pos.as<unsigned long long>(), mode.as<uint8_t>() + r0,
                                                                status.as<uint8_t>() + r0, sq, pitch,
-                                                               qualityLabels ? 1 : 0, outDev.as<char>());
+                                                               qualityLabels ? 1 : 0, lastRec.as<unsigned int>(), r0,
+                                                               outDev.as<char>());
             DCHECK(cudaGetLastError());
             std::unique_ptr<char[]> bytes(new char[total]);  // left uninitialised: the copy fills it
             DCHECK(cudaMemcpyAsync(bytes.get(), outDev.p, total, cudaMemcpyDeviceToHost, s));
@@ -522,7 +553,7 @@ int correct_fastq_on_device(const cg_options& options, const std::vector<ByteSpa
     DCHECK(cudaMemcpyAsync(&records, recCount.p, sizeof(records), cudaMemcpyDeviceToHost, s));
     DCHECK(cudaStreamSynchronize(s));
     run->reads = n;
-    run->records = records;
+    run->records = records + candRecords;
     return CG_OK;
 }
 

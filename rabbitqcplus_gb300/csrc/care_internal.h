@@ -91,6 +91,19 @@ struct Params {
     int numTrees;
     float forestThreshold;
     float qweight[256];
+    // Candidate correction (correct_candidates).  Per read: votes = {number of
+    // candidate corrections made by anchors with a smaller id, by anchors with a
+    // larger id}; candAnd / candOr = bitwise AND / OR of every sequence voted
+    // for the read (its candidate corrections and its own low-quality anchor
+    // correction), 2 bits per base, 32 bases per word, first base in the most
+    // significant bits, zero past the read's end.  All of them are equal
+    // exactly when AND == OR over the read's words.
+    int candidates;
+    int newColumns;               // new_columns_to_correct
+    int candPitch;                // words per read = ceil(Lmax / 32)
+    uint2* candVotes;             // [N]
+    unsigned long long* candAnd;  // [N][candPitch]
+    unsigned long long* candOr;   // [N][candPitch]
 };
 
 // One forest node (reference: include/forest.hpp:21-30): go left when
@@ -202,6 +215,7 @@ enum {
     kCounterColumns,         // learned decision: columns recorded for the classifier
     kCounterColumnOverflow,  // columns beyond the buffer (decided by the fallback rule)
     kCounterLearnedTaken,    // columns the classifier corrected
+    kCounterCandidateVotes,  // candidate corrections made by HQ anchors
     kNumCounters
 };
 
@@ -246,6 +260,14 @@ int msa_warp_occupancy(StoreArg st, Params p, int warps);
 // order[count] = the batch's anchors by decreasing b.nfinal (log2 buckets);
 // scratch = 32 words, cleared by the launcher
 cudaError_t launch_msa_order(BatchArg b, unsigned int* scratch, uint32_t* order, cudaStream_t s);
+// candidate correction: the batch's low-quality anchor corrections join their
+// reads' votes (after the MSA and any classifier pass)
+cudaError_t launch_anchor_vote(StoreArg st, Params p, BatchArg b, cudaStream_t s);
+// the combine step for reads [first, first + n): flags[i] of read first + i is
+// rewritten (CG_RESULT_CANDIDATES / _REJECTED / _CANDIDATE_RECORD), *records
+// (zeroed by the caller) gains the number of saved candidate records
+cudaError_t launch_combine(StoreArg st, Params p, uint64_t first, uint64_t n, uint8_t* flags,
+                           unsigned long long* records, cudaStream_t s);
 // cursor[0] += stride, work[0] = work[1] = 0 (the last node of a batch)
 cudaError_t launch_batch_advance(unsigned long long* cursor, unsigned int* work, unsigned long long stride,
                                  cudaStream_t s);

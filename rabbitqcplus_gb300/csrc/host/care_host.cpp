@@ -80,11 +80,15 @@ char upper(char ch) {
 
 // STEP1-2: reads of the input group, device build and correction.
 // Output per read: final sequence written into `seqOut` (same offsets as the
-// input) and a status byte (0 no record, 1 LQ record, 3 HQ record).
+// input) and its quality label (0 none, 1 LQ anchor correction, 2 LQ
+// correction confirmed by candidate corrections, 3 HQ); lastRecord = the last
+// read with a correction record (-1: none), after which the reference writes
+// no labels (src/correctionresultoutput.cpp:370-377, 896-901).
 struct Corrected {
     ReadSet reads;
     std::vector<char> seqOut;
     std::vector<uint8_t> status;
+    int64_t lastRecord = -1;
     uint64_t records = 0;
     cg_stats stats{};
 };
@@ -142,9 +146,11 @@ Corrected runCorrection(const ProgramOptions& o) {
     const uint64_t chunk = 1u << 20;
     std::vector<uint8_t> flags(chunk);
     std::vector<char> seqs(chunk * (size_t)lmax);
+    std::vector<uint8_t> allFlags(o.correctCandidates ? n : 0);  // for the combine step
     for (uint64_t first = 0; first < n; first += chunk) {
         const uint64_t cnt = std::min(chunk, n - first);
         check(ctx.c, cg_correct(ctx.c, first, cnt, flags.data(), seqs.data(), (size_t)lmax), "cg_correct");
+        if (o.correctCandidates) std::memcpy(allFlags.data() + first, flags.data(), cnt);
         for (uint64_t j = 0; j < cnt; j++) {
             if (!(flags[j] & CG_RESULT_CORRECTED)) continue;
             const uint64_t id = first + j;
@@ -161,6 +167,7 @@ Corrected runCorrection(const ProgramOptions& o) {
                 std::memcpy(dst, corr, len);
                 r.status[id] = hq ? 3 : 1;
                 r.records++;
+                r.lastRecord = (int64_t)id;
                 continue;
             }
             const int maxEdits = len / 7;
@@ -175,6 +182,24 @@ Corrected runCorrection(const ProgramOptions& o) {
             }
             r.status[id] = hq ? 3 : 1;
             r.records++;
+            r.lastRecord = (int64_t)id;
+        }
+    }
+    if (o.correctCandidates) {
+        // the combine step (src/correctionresultoutput.cpp:1256-1551)
+        uint64_t candRecords = 0;
+        check(ctx.c, cg_combine_results(ctx.c, 0, n, allFlags.data(), &candRecords), "cg_combine_results");
+        r.records += candRecords;
+        for (uint64_t i = 0; i < n; i++) {
+            const uint8_t f = allFlags[i];
+            if (f & CG_RESULT_CANDIDATE_RECORD) r.lastRecord = std::max(r.lastRecord, (int64_t)i);
+            if (f & CG_RESULT_REJECTED) {  // written unchanged
+                const uint64_t off = r.reads.offsets[i];
+                std::memcpy(r.seqOut.data() + off, r.reads.sequences.data() + off, r.reads.offsets[i + 1] - off);
+                r.status[i] = 0;
+            } else if (f & CG_RESULT_CANDIDATES) {
+                r.status[i] = 2;
+            }
         }
     }
     check(ctx.c, cg_get_stats(ctx.c, &r.stats), "cg_get_stats");
@@ -234,7 +259,7 @@ FileFormat outputFormat(const ProgramOptions& o) {
 std::string labelled(const std::string& header, uint8_t status, bool labels) {
     if (!labels) return header;
     // src/correctionresultoutput.cpp:403-414
-    return header + (status == 3 ? " care:q=3" : status == 1 ? " care:q=1" : " care:q=0");
+    return header + " care:q=" + char('0' + status);
 }
 
 }  // namespace
@@ -331,8 +356,8 @@ RunReport performCorrection(const ProgramOptions& o) {
         const size_t len = r.reads.offsets[i + 1] - off;
         const int w = writers.size() == 1 ? 0 : std::min<int>(r.reads.fileId[i], (int)writers.size() - 1);
         const std::string q = r.reads.hasQualities ? std::string(r.reads.qualities.data() + off, len) : empty;
-        writers[w]->write(labelled(r.reads.headers[i], r.status[i], o.outputCorrectionQualityLabels),
-                          r.seqOut.data() + off, len, q);
+        const bool lab = o.outputCorrectionQualityLabels && (int64_t)i <= r.lastRecord;
+        writers[w]->write(labelled(r.reads.headers[i], r.status[i], lab), r.seqOut.data() + off, len, q);
     }
     RunReport rep;
     rep.reads = n;
@@ -408,7 +433,8 @@ RunReport performCorrectionToSink(const ProgramOptions& o, const std::function<v
         const uint64_t off = r.reads.offsets[i];
         const size_t len = r.reads.offsets[i + 1] - off;
         const int f = nfiles == 1 ? 0 : r.reads.fileId[i];
-        const std::string hdr = labelled(r.reads.headers[i], r.status[i], o.outputCorrectionQualityLabels);
+        const bool lab = o.outputCorrectionQualityLabels && (int64_t)i <= r.lastRecord;
+        const std::string hdr = labelled(r.reads.headers[i], r.status[i], lab);
         const size_t need = hdr.size() + 2 * len + 6;
         if (need >= (size_t)cap) throw std::runtime_error("record larger than a 1 MiB chunk");
         if (used[f] + need >= (size_t)cap) {

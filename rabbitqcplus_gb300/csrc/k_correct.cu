@@ -728,6 +728,56 @@ __device__ bool forest_decide(const Params& p, const float* f) {
     return false;
 }
 
+__device__ __forceinline__ int base_index(char c) { return c == 'A' ? 0 : c == 'C' ? 1 : c == 'G' ? 2 : 3; }
+
+// ---------------------------------------------------------------- candidate correction
+//
+// reference: src/msa.cpp:457-522 (getCorrectedCandidates), include/corrector.hpp
+// :293-299 and 1504-1512 (HQ anchors correct their candidates), :1674-1748 (the
+// record: the consensus slice, reverse complemented back for a reverse-
+// complement candidate).  A row of the final MSA with shift s and length len
+// qualifies when -nc <= s <= nc and s + len <= La + nc (nc =
+// new_columns_to_correct; the support and coverage test computed there is
+// overwritten by `candidateShouldBeCorrected = true`).  Its record votes for
+// read `id` (see Params::candVotes).
+
+__device__ __forceinline__ void vote_word(const Params& p, uint64_t read, int w, unsigned long long v) {
+    const uint64_t i = read * (uint64_t)p.candPitch + (uint64_t)w;
+    atomicAnd(&p.candAnd[i], v);
+    atomicOr(&p.candOr[i], v);
+}
+
+// One thread votes for one row: cons(col) gives the consensus base code of
+// column col (relative to the anchor's first column).  Returns 1 if it voted.
+template <class Cons>
+__device__ __forceinline__ int vote_candidate(const Params& p, int s, int len, bool rc, uint32_t id, uint64_t aid,
+                                              int La, Cons cons) {
+    const int nc = p.newColumns;
+    if (s < -nc || s > nc || s + len > La + nc) return 0;
+    for (int w = 0; w * 32 < len; w++) {
+        unsigned long long v = 0;
+        const int pe = min(len, w * 32 + 32);
+        for (int q = w * 32; q < pe; q++) {
+            uint32_t bb = cons(s + (rc ? len - 1 - q : q));
+            if (rc) bb = 3u - bb;
+            v |= (unsigned long long)bb << (62 - 2 * (q & 31));
+        }
+        vote_word(p, id, w, v);
+    }
+    atomicAdd((uint64_t)id > aid ? &p.candVotes[id].x : &p.candVotes[id].y, 1u);
+    return 1;
+}
+
+// Quality score of position `pos` (aligned orientation) of a candidate row
+// (reference: include/corrector.hpp:1214-1239).  Rows hold Lmax scores, zero
+// past the read's end (include/chunkedreadstorage.hpp:532-610), and a reverse-
+// complement candidate's whole row is reversed, so a read shorter than Lmax
+// starts with the zero padding: its position pos reads score Lmax - 1 - pos.
+__device__ __forceinline__ uint8_t row_quality(const uint8_t* q, int lmax, int len, bool rc, int pos) {
+    const int qi = rc ? lmax - 1 - pos : pos;
+    return qi < len ? q[qi] : (uint8_t)0;
+}
+
 __global__ void __launch_bounds__(1024) msa_correct_kernel(StoreArg st, Params p, BatchArg b,
                                                           const uint32_t* __restrict__ rawOff, int maxCols,
                                                           int bitsetWords, int storeWeights) {
@@ -852,7 +902,7 @@ __global__ void __launch_bounds__(1024) msa_correct_kernel(StoreArg st, Params p
                         uint32_t bb = get2bit(m.enc, sp);
                         if (m.rc) bb = 3u - bb;
                         float w = m.weight;
-                        if (p.useQuality) w = __fmul_rn(w, qw[m.qual[sp]]);
+                        if (p.useQuality) w = __fmul_rn(w, qw[row_quality(m.qual, st.lmax, (int)m.len, m.rc, pos)]);
                         add(k, bb, w);
                     }
                 }
@@ -983,6 +1033,19 @@ __global__ void __launch_bounds__(1024) msa_correct_kernel(StoreArg st, Params p
         b.flags[oi] = corrected ? (uint8_t)(CG_RESULT_CORRECTED | (hq ? CG_RESULT_HQ : 0)) : (uint8_t)0;
     }
     __syncthreads();
+    if (p.candidates && sHQ) {
+        // candidate correction: one thread per row of the final MSA, whose
+        // consensus covers every column of the rows
+        int votes = 0;
+        for (uint32_t j = tid; j < nf; j += bd) {
+            if (isRemoved(j)) continue;
+            const uint32_t g = base + j;
+            votes += vote_candidate(p, b.fshift[g], b.flen[g], b.forient[g] == 2, b.fid[g], aid, La,
+                                    [&](int col) { return (uint32_t)base_index(cons[aBegin + col]); });
+        }
+        votes = block_reduce<int>(votes, redi, 2);
+        if (tid == 0 && votes) atomicAdd(&b.counters[kCounterCandidateVotes], (unsigned long long)votes);
+    }
     if (p.correctionType == CG_CORR_FOREST) {
         const bool hq = sHQ;
         const float avg = sAvg;
@@ -1062,8 +1125,6 @@ __device__ __forceinline__ ColInfo col_info(const uint2* wc, int cp, int c) {
     r.colW = __fadd_rn(__fadd_rn(__fadd_rn(wA, wC), wG), wT);
     return r;
 }
-
-__device__ __forceinline__ int base_index(char c) { return c == 'A' ? 0 : c == 'C' ? 1 : c == 'G' ? 2 : 3; }
 
 // One warp per anchor (one warp per block) for reads up to 256 bp.
 //
@@ -1151,9 +1212,12 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
                 int sp = rc ? len - 1 - (c - shift) : c - shift;
                 const int dsp = rc ? -32 : 32, dwi = rc ? -2 : 2;
                 const uint32_t sh = 30u - 2u * (uint32_t)(sp & 15), flip = rc ? 3u : 0u;
+                // quality index: sp, or for a reverse complement row Lmax - 1 - (c - shift)
+                const int qd = rc ? st.lmax - len : 0;
                 for (int wi = sp >> 4; c < c1; c += 32, wi += dwi, sp += dsp) {
                     const uint32_t bb = ((e[wi] >> sh) & 3u) ^ flip;
-                    const float wt = p.useQuality ? __fmul_rn(weight, qw[q[sp]]) : weight;
+                    const int qi = sp + qd;
+                    const float wt = p.useQuality ? __fmul_rn(weight, qw[qi < len ? q[qi] : 0]) : weight;
                     uint2 v = wc[bb * lp + c];
                     if (add) {
                         v.x = __float_as_uint(__fadd_rn(__uint_as_float(v.x), wt));
@@ -1361,6 +1425,91 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
         }
         out[c] = r;
     }
+    if (p.candidates && hq) {
+        // Candidate correction.  The MSA above holds the anchor's columns
+        // only; the consensus of the nc columns on either side is summed here,
+        // rows in list order, lane e0 + lane owning extension column e (column
+        // e - nc left of the anchor, or La + e - nc right of it).  cons8[x] =
+        // consensus base code of column x - nc, for x in [0, La + 2 nc).
+        const int nc = p.newColumns;
+        uint8_t* cons8 = reinterpret_cast<uint8_t*>(meta + 32);
+        for (int c = lane; c < La; c += 32) cons8[nc + c] = (uint8_t)base_index(col_info(wc, lp, c).cons);
+        for (int e0 = 0; e0 < 2 * nc; e0 += 32) {  // warp-uniform trip count
+            const int e = e0 + lane;
+            const int col = e < nc ? e - nc : La + (e - nc);
+            float w4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            for (uint32_t j0 = 0; j0 < nf; j0 += 32) {
+                const uint32_t jr = j0 + lane;
+                const int rows = (int)min(32u, nf - j0);
+                uint32_t mo = kRm, mid = 0;
+                int mshift = 0, mlen = 0;
+                float mw = 0.0f;
+                if (jr < nf) {
+                    mo = b.forient[base + jr];
+                    mshift = b.fshift[base + jr];
+                    mlen = b.flen[base + jr];
+                    mid = b.fid[base + jr];
+                    mw = b.fweight[base + jr];
+                }
+                // rows still in the MSA that reach past either end of the anchor
+                const bool sel = jr < nf && !(mo & kRm) && (mshift < 0 || mshift + mlen > La);
+                const unsigned selRows = __ballot_sync(kFull, sel);
+                if (!selRows) continue;
+                for (int i0 = 0; i0 < rows * pitch; i0 += 32) {
+                    const int idx = i0 + lane;
+                    const int r = min(idx / pitch, rows - 1);
+                    const uint32_t rid = __shfl_sync(kFull, mid, r);
+                    if (idx < rows * pitch && ((selRows >> r) & 1u))
+                        stage[idx] = st.enc[(uint64_t)rid * pitch + (idx - r * pitch)];
+                }
+                meta[lane] = make_int4(mshift, mlen | (int)((mo & 3u) << 16), __float_as_int(mw), (int)mid);
+                __syncwarp();
+                for (int r = 0; r < rows; r++) {
+                    if (!((selRows >> r) & 1u)) continue;
+                    const int4 md = meta[r];
+                    const bool rc = ((uint32_t)md.y >> 16) == 2;
+                    const int len = md.y & 0xffff;
+                    const int pos = col - md.x;
+                    if (e >= 2 * nc || pos < 0 || pos >= len) continue;
+                    const int sp = rc ? len - 1 - pos : pos;
+                    const uint32_t bb = ((stage[r * pitch + (sp >> 4)] >> (30u - 2u * (uint32_t)(sp & 15))) & 3u) ^
+                                        (rc ? 3u : 0u);
+                    float wt = __int_as_float(md.z);
+                    if (p.useQuality)
+                        wt = __fmul_rn(wt, qw[row_quality(st.qual + (uint64_t)(uint32_t)md.w * st.lmax, st.lmax,
+                                                          len, rc, pos)]);
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if ((uint32_t)q == bb) w4[q] = __fadd_rn(w4[q], wt);
+                }
+                __syncwarp();  // the next chunk overwrites the staged rows
+            }
+            if (e < 2 * nc) {  // src/msa.cpp:135-157: the first largest weight, A C G T
+                int cb = 0;
+                float cw = w4[0];
+#pragma unroll
+                for (int q = 1; q < 4; q++)
+                    if (w4[q] > cw) {
+                        cb = q;
+                        cw = w4[q];
+                    }
+                cons8[e < nc ? e : La + e] = (uint8_t)cb;
+            }
+        }
+        __syncwarp();
+        // one row per lane
+        int votes = 0;
+        for (uint32_t j = lane; j < nf; j += 32) {
+            const uint32_t g = base + j;
+            const uint8_t o = b.forient[g];
+            if (o & kRm) continue;
+            votes += vote_candidate(p, b.fshift[g], b.flen[g], (o & 3) == 2, b.fid[g], aid, La,
+                                    [&](int col) { return (uint32_t)cons8[nc + col]; });
+        }
+        votes = __reduce_add_sync(kFull, votes);
+        if (lane == 0 && votes) atomicAdd(&b.counters[kCounterCandidateVotes], (unsigned long long)votes);
+        return;
+    }
     if (p.correctionType != CG_CORR_LEARNED || hq) return;
     // Learned decision: record every column whose consensus differs from the
     // anchor's base, with its features; the classifier then replaces the
@@ -1437,9 +1586,12 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
     }
 }
 
-// Bytes of shared memory one warp of msa_warp_kernel works in.
-__host__ __device__ inline size_t msa_warp_slice_bytes(int lp, int pitch) {
-    return (size_t)lp * (9 * sizeof(float)) + (size_t)32 * pitch * sizeof(uint32_t) + 32 * sizeof(int4);
+// Bytes of shared memory one warp of msa_warp_kernel works in (with candidate
+// correction, the consensus codes of Lmax + 2 new_columns_to_correct columns
+// follow the row metadata).
+__host__ __device__ inline size_t msa_warp_slice_bytes(int lp, int pitch, const Params& p) {
+    const size_t cand = p.candidates ? ((size_t)lp + 2 * (size_t)p.newColumns + 15) / 16 * 16 : 0;
+    return (size_t)lp * (9 * sizeof(float)) + (size_t)32 * pitch * sizeof(uint32_t) + 32 * sizeof(int4) + cand;
 }
 
 // `warps` warps per block, each on its own anchors.  Plain form: anchor
@@ -1451,7 +1603,7 @@ __global__ void __launch_bounds__(256, 4) msa_warp_kernel(StoreArg st, Params p,
     float* qw = reinterpret_cast<float*>(sm);  // [256] (quality scores only)
     const int warp = (int)(threadIdx.x >> 5), warps = (int)(blockDim.x >> 5);
     const size_t qbytes = p.useQuality ? 256 * sizeof(float) : 0;
-    unsigned char* slice = sm + qbytes + (size_t)warp * msa_warp_slice_bytes(lp, st.pitch);
+    unsigned char* slice = sm + qbytes + (size_t)warp * msa_warp_slice_bytes(lp, st.pitch, p);
     if (p.useQuality) {
         for (int i = threadIdx.x; i < 256; i += blockDim.x) qw[i] = p.qweight[i];
         __syncthreads();
@@ -1579,7 +1731,7 @@ namespace {
 
 size_t msa_warp_smem(StoreArg st, Params p, int warps) {
     const int lp = (st.lmax + 31) / 32 * 32;
-    return (p.useQuality ? 256 * sizeof(float) : 0) + (size_t)warps * msa_warp_slice_bytes(lp, st.pitch);
+    return (p.useQuality ? 256 * sizeof(float) : 0) + (size_t)warps * msa_warp_slice_bytes(lp, st.pitch, p);
 }
 
 cudaError_t msa_warp_prepare(size_t smem) {
@@ -1650,12 +1802,76 @@ cudaError_t launch_msa_order(BatchArg b, unsigned int* scratch, uint32_t* order,
 }
 
 namespace {
+
+// one warp per anchor of the batch; lane w packs word w of a low-quality
+// anchor correction (the output row's bases) and votes with it
+__global__ void __launch_bounds__(256) anchor_vote_kernel(StoreArg st, Params p, BatchArg b) {
+    const int a = (int)(((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (a >= b.count) return;
+    const uint64_t first = batch_first(b);
+    const uint64_t aid = first + (uint64_t)a;
+    const uint64_t oi = (first - out_first(b)) + (uint64_t)a;
+    const uint8_t f = b.flags[oi];
+    if (!(f & CG_RESULT_CORRECTED) || (f & CG_RESULT_HQ)) return;
+    const int len = st.len[aid];
+    const int w = (int)lane_id();
+    if (w * 32 >= len) return;
+    const char* o = b.out + oi * (uint64_t)b.outPitch;
+    unsigned long long v = 0;
+    const int pe = min(len, w * 32 + 32);
+    for (int q = w * 32; q < pe; q++) v |= (unsigned long long)base_index(o[q]) << (62 - 2 * (q & 31));
+    vote_word(p, aid, w, v);
+}
+
+// reference: src/correctionresultoutput.cpp:1256-1551 (combine), with the
+// record filter of include/corrector.hpp:1678-1681 in a single-threaded run's
+// order: read c's candidate records from anchors above c are not saved when c
+// is a corrected HQ anchor.  One thread per read.
+__global__ void combine_kernel(StoreArg st, Params p, uint64_t first, uint64_t n, uint8_t* __restrict__ flags,
+                               unsigned long long* __restrict__ records) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long k = 0;
+    if (i < n) {
+        const uint64_t r = first + i;
+        uint8_t f = flags[i];
+        const uint2 v = p.candVotes[r];
+        const bool hqAnchor = (f & CG_RESULT_CORRECTED) && (f & CG_RESULT_HQ);
+        k = (unsigned long long)v.x + (hqAnchor ? 0ull : (unsigned long long)v.y);
+        if (k) f |= CG_RESULT_CANDIDATE_RECORD;
+        if ((f & CG_RESULT_CORRECTED) && !(f & CG_RESULT_HQ) && k >= 2) {
+            const int words = (st.len[r] + 31) / 32;
+            bool same = true;
+            for (int w = 0; w < words; w++) {
+                const uint64_t j = r * (uint64_t)p.candPitch + (uint64_t)w;
+                same &= p.candAnd[j] == p.candOr[j];
+            }
+            f |= same ? CG_RESULT_CANDIDATES : CG_RESULT_REJECTED;
+        }
+        flags[i] = f;
+    }
+    for (int d = 16; d > 0; d >>= 1) k += __shfl_xor_sync(kFull, k, d);
+    if ((threadIdx.x & 31) == 0 && k) atomicAdd(records, k);
+}
+
 __global__ void batch_advance_kernel(unsigned long long* cursor, unsigned int* work, unsigned long long stride) {
     cursor[0] += stride;
     work[0] = 0;
     work[1] = 0;
 }
 }  // namespace
+
+cudaError_t launch_anchor_vote(StoreArg st, Params p, BatchArg b, cudaStream_t s) {
+    if (b.count <= 0) return cudaSuccess;
+    anchor_vote_kernel<<<(unsigned)((b.count + 7) / 8), 256, 0, s>>>(st, p, b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_combine(StoreArg st, Params p, uint64_t first, uint64_t n, uint8_t* flags,
+                           unsigned long long* records, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    combine_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(st, p, first, n, flags, records);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_batch_advance(unsigned long long* cursor, unsigned int* work, unsigned long long stride,
                                  cudaStream_t s) {

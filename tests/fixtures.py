@@ -34,7 +34,9 @@ def options_for(entry: dict) -> capi.CareOptions:
         use_quality_scores=int(bool(o.get("quality"))),
         exclude_ambiguous_reads=int(bool(o.get("exclude_ambiguous"))),
         pair_mode=capi.CG_PAIR_PE if o.get("paired") else capi.CG_PAIR_SE,
-        correction_type=capi.CG_CORR_FOREST if o.get("forest") else capi.CG_CORR_CLASSIC)
+        correction_type=capi.CG_CORR_FOREST if o.get("forest") else capi.CG_CORR_CLASSIC,
+        correct_candidates=int(bool(o.get("candidates"))),
+        new_columns_to_correct=int(o.get("new_columns", 15)))
 
 
 def forest_bytes(entry: dict) -> bytes | None:

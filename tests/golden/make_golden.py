@@ -66,6 +66,31 @@ CASES = {
     "pe_basic": (sim.SimConfig(seed=109, genome_length=50_000, num_reads=10_000, paired=True,
                                repeat_families=3, repeat_copies=3, indel_rate=0.0001),
                  {"coverage": 30, "k": 20, "paired": True}, 0),
+    # reads shorter than the longest with quality scores: a reverse-complement
+    # candidate's reversed quality row starts with the padding
+    "se_varlen_quality": (sim.SimConfig(seed=114, genome_length=60_000, repeat_families=4, repeat_copies=4,
+                                        num_reads=12_000, read_len_min=60, read_len_max=240, sub_rate_5p=0.002,
+                                        sub_rate_3p=0.02),
+                          {"coverage": 30, "k": 20, "quality": True}, 0),
+    # candidate correction (--candidateCorrection) and the combine step
+    "se_candidates": (sim.SimConfig(seed=110, genome_length=60_000, repeat_families=6, repeat_copies=4,
+                                    repeat_min_len=1000, repeat_max_len=3000, repeat_divergence=0.02,
+                                    num_reads=12_000, sub_rate_5p=0.002, sub_rate_3p=0.02),
+                      {"coverage": 30, "k": 20, "candidates": True}, 0),
+    "pe_candidates": (sim.SimConfig(seed=111, genome_length=50_000, num_reads=10_000, paired=True,
+                                    repeat_families=3, repeat_copies=3),
+                      {"coverage": 30, "k": 20, "paired": True, "candidates": True}, 0),
+    "se_candidates_varlen_quality": (sim.SimConfig(seed=112, genome_length=60_000, repeat_families=4,
+                                                   repeat_copies=4, num_reads=12_000, read_len_min=50,
+                                                   read_len_max=250, sub_rate_5p=0.002, sub_rate_3p=0.02),
+                                     {"coverage": 30, "k": 20, "quality": True, "candidates": True,
+                                      "new_columns": 25}, 0),
+    # the last three reads are ambiguous and excluded, so they have no record:
+    # the reference writes no quality label for reads after the last record
+    "se_label_tail": (sim.SimConfig(seed=118, genome_length=40_000, num_reads=8_000, n_read_fraction=0.3),
+                      {"coverage": 30, "k": 20, "exclude_ambiguous": True}, 0),
+    "se_candidates_tail": (sim.SimConfig(seed=118, genome_length=40_000, num_reads=8_000, n_read_fraction=0.3),
+                           {"coverage": 30, "k": 20, "exclude_ambiguous": True, "candidates": True}, 0),
 }
 
 
@@ -104,9 +129,25 @@ def run_case(name: str, cfg: sim.SimConfig, opts: dict, stage_anchors: int, work
         cmd.append("--exclude-ambiguous")
     if paired:
         cmd.append("--pe")
+    if opts.get("candidates"):
+        cmd.append("--candidates")
+    if "new_columns" in opts:
+        cmd += ["--new-columns", str(opts["new_columns"])]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"reference failed on {name}:\n{r.stdout[-3000:]}")
+    # the same run with " care:q=N" header labels, into its own directory
+    ld = os.path.join(d, "labels")
+    os.makedirs(ld, exist_ok=True)
+    lcmd = list(cmd)
+    lcmd[lcmd.index("-d") + 1] = ld
+    r = subprocess.run(lcmd + ["--labels"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference (labels) failed on {name}:\n{r.stdout[-3000:]}")
+    labels_md5 = []
+    for i in range(len(inputs)):
+        with open(os.path.join(ld, f"out_{i}.fq"), "rb") as f:
+            labels_md5.append(md5(f.read()))
     # output sequences in read-id order (paired: interleave file 1 and file 2)
     if paired:
         s1 = fastq_sequences(os.path.join(d, "out_0.fq"), reads.n // 2)
@@ -139,6 +180,7 @@ def run_case(name: str, cfg: sim.SimConfig, opts: dict, stage_anchors: int, work
         "num_reads": reads.n,
         "input_file_md5": in_files_md5,
         "output_file_md5": out_files_md5,
+        "labels_file_md5": labels_md5,
         "input_md5": md5(reads.sequences.tobytes()),
         "input_qual_md5": md5(reads.qualities.tobytes()),
         "output_md5": md5(out_all.tobytes()),

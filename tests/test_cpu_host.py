@@ -59,7 +59,8 @@ def test_invalid_options_are_rejected_before_touching_the_device():
                {"estimated_coverage": 0.0}, {"pair_mode": 7}):
         o = capi.CareOptions.defaults(30.0, **kw)
         assert L.cg_create(ctypes.byref(o), ctypes.byref(h)) == 1, kw  # CG_ERR_INVALID_ARGUMENT
-    for kw in ({"correct_candidates": 1}, {"correction_type": capi.CG_CORR_PRINT}):
+    for kw in ({"correct_candidates": 1, "new_columns_to_correct": 257},
+               {"correct_candidates": 1, "new_columns_to_correct": -1}, {"correction_type": capi.CG_CORR_PRINT}):
         o = capi.CareOptions.defaults(30.0, **kw)
         assert L.cg_create(ctypes.byref(o), ctypes.byref(h)) == 2, kw  # CG_ERR_UNSUPPORTED
 
