@@ -212,8 +212,10 @@ def main():
     def form_options(form):
         o = capi.CareOptions.defaults(opts.estimated_coverage, kmerlength=20, pair_mode=opts.pair_mode,
                                       device=local)
-        if form in ("batched", "batched_learned"):
+        if form in ("batched", "batched_learned", "batched_candidates"):
             o.driver = capi.CG_DRIVER_BATCHED
+        if form == "batched_candidates":
+            o.correct_candidates = 1
         if form == "batched_learned":
             o.correction_type = capi.CG_CORR_LEARNED
         if form == "forest":
@@ -289,6 +291,7 @@ def main():
         plain = run_form("plain", args.steps, args.warmup, clk)
         bat = run_form("batched", args.steps, args.warmup, clk)
         bl = run_form("batched_learned", args.steps, args.warmup, clk)
+        cand = run_form("batched_candidates", args.steps, args.warmup, clk)
     forest_run = run_form("forest", 1, 0)
     st0, st1 = bl["st0"], bl["st1"]
     n = bl["n"]
@@ -305,6 +308,9 @@ def main():
         same = bool(np.array_equal(np.where(mask, po, 0), np.where(mask, bo, 0)))
     forms = {"plain": summary(plain, args.steps), "batched": summary(bat, args.steps),
              "batched_learned": summary(bl, args.steps),
+             # --candidateCorrection: device time of cg_correct; the combine step after it is one
+             # thread per read
+             "batched_candidates": summary(cand, args.steps),
              "forest": {"tp": forest_run["score"]["tp"], "fp": forest_run["score"]["fp"],
                         "fn": forest_run["score"]["fn"], "driver": "plain", "timed": False},
              "batched_bit_exact_with_plain": same,
