@@ -30,7 +30,7 @@ def case_names() -> list[str]:
 def options_for(entry: dict) -> capi.CareOptions:
     o = entry["options"]
     return capi.CareOptions.defaults(
-        float(o["coverage"]), kmerlength=int(o["k"]),
+        float(o["coverage"]), kmerlength=int(o["k"]), num_hash_functions=int(o.get("maps", 48)),
         use_quality_scores=int(bool(o.get("quality"))),
         exclude_ambiguous_reads=int(bool(o.get("exclude_ambiguous"))),
         pair_mode=capi.CG_PAIR_PE if o.get("paired") else capi.CG_PAIR_SE,

@@ -72,6 +72,18 @@ CASES = {
                                         num_reads=12_000, read_len_min=60, read_len_max=240, sub_rate_5p=0.002,
                                         sub_rate_3p=0.02),
                           {"coverage": 30, "k": 20, "quality": True}, 0),
+    # reads longer than 256 bp (block-per-anchor kernels), k autodetected (32)
+    "se_long_quality": (sim.SimConfig(seed=115, genome_length=60_000, repeat_families=4, repeat_copies=4,
+                                      num_reads=5_000, read_len_min=180, read_len_max=400, sub_rate_5p=0.002,
+                                      sub_rate_3p=0.02),
+                        {"coverage": 25, "k": 0, "quality": True}, 0),
+    "pe_quality_varlen": (sim.SimConfig(seed=116, genome_length=50_000, num_reads=10_000, paired=True,
+                                        repeat_families=3, repeat_copies=3, read_len_min=100, read_len_max=150),
+                          {"coverage": 25, "k": 20, "paired": True, "quality": True}, 0),
+    # fewer maps and a shorter k
+    "se_maps24_k16": (sim.SimConfig(seed=117, genome_length=50_000, num_reads=10_000, repeat_families=3,
+                                    repeat_copies=3),
+                      {"coverage": 30, "k": 16, "maps": 24}, 0),
     # candidate correction (--candidateCorrection) and the combine step
     "se_candidates": (sim.SimConfig(seed=110, genome_length=60_000, repeat_families=6, repeat_copies=4,
                                     repeat_min_len=1000, repeat_max_len=3000, repeat_divergence=0.02,
@@ -120,7 +132,7 @@ def run_case(name: str, cfg: sim.SimConfig, opts: dict, stage_anchors: int, work
         reads.write_fastq(in1)
         inputs = [in1]
     cmd = [os.path.join(REPO, "oracle", "_ref", "ref_care"), "-d", d, "-c", str(opts["coverage"]),
-           "-k", str(opts["k"]), "-h", "48", "-t", str(threads)]
+           "-k", str(opts["k"]), "-h", str(opts.get("maps", 48)), "-t", str(threads)]
     for i, p in enumerate(inputs):
         cmd += ["-i", p, "-o", f"out_{i}.fq"]
     if opts.get("quality"):
