@@ -10,7 +10,8 @@ se_candidates_varlen_quality, se_candidates_tail; checked by the fixture tests
 of test_gpu_parity.py, test_gpu_batched.py and test_gpu_files.py); here the
 oracle, pinned to those fixtures, checks the paths they do not reach: reads
 longer than 256 bp (the block-per-anchor MSA), the forest decision, a wide
-new_columns_to_correct, passes over several calls, and the batched driver.
+new_columns_to_correct, passes over several calls, the batched driver and the
+learned decision.
 """
 import numpy as np
 import pytest
@@ -146,6 +147,29 @@ def test_pass_over_several_calls_and_repeated_passes():
     g.combine(1000, sub)
     assert np.array_equal(sub, whole[1000:3000])
     g.close()
+
+
+def test_learned_decision_with_candidates_batched_matches_plain():
+    # the learned decision has no reference counterpart: both drivers must
+    # agree, and only LQ corrections may be kept or rejected by the combine
+    from rabbitqcplus_gb300 import learned
+    model = open(learned.DEFAULT_MODEL, "rb").read()
+    r = repeats(69, n=10_000)
+    res = []
+    for drv in (C.CG_DRIVER_PLAIN, C.CG_DRIVER_BATCHED):
+        o = cand_opts(correction_type=C.CG_CORR_LEARNED, driver=drv, batch_anchors=2048)
+        g = capi.CareGpu(o)
+        g.append_reads(r.sequences, r.offsets)
+        g.build_tables()
+        g.load_classifier(model)
+        res.append(g.correct())
+        g.close()
+    (pf, ps), (bf, bs) = res
+    assert_same(r, bf, bs, pf, ps)
+    lq = (pf & C.CG_RESULT_CORRECTED) != 0
+    lq &= (pf & C.CG_RESULT_HQ) == 0
+    combined = (pf & (C.CG_RESULT_CANDIDATES | C.CG_RESULT_REJECTED)) != 0
+    assert combined.any() and not (combined & ~lq).any()
 
 
 def test_combine_needs_candidate_correction():
