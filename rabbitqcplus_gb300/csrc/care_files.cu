@@ -500,6 +500,8 @@ int correct_fastq_on_device(const cg_options& options, const std::vector<ByteSpa
     run->outputs.clear();
     run->outputs.resize((size_t)numOutputs);
     run->outputSizes.assign((size_t)numOutputs, 0);
+    run->deviceOutputs.clear();
+    run->deviceOutputs.resize((size_t)numOutputs);
     // One range when a read's output depends on reads after it: candidate
     // corrections come from any anchor, and the labels stop after the last
     // record of the whole run.
@@ -537,6 +539,30 @@ int correct_fastq_on_device(const cg_options& options, const std::vector<ByteSpa
                                                                qualityLabels ? 1 : 0, lastRec.as<unsigned int>(), r0,
                                                                outDev.as<char>());
             DCHECK(cudaGetLastError());
+            if (run->queueChunkBytes && !run->onChunk) {
+                // queue chunks: cut at record ends, each chunk the longest run of
+                // whole records under queueChunkBytes (src/correctionresultoutput.cpp:
+                // 733-745); the bytes stay on the device until emit_queue_chunks
+                std::vector<unsigned long long> ends(m + 1);
+                DCHECK(cudaMemcpyAsync(ends.data(), pos.p, (m + 1) * sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, s));
+                DCHECK(cudaStreamSynchronize(s));
+                const size_t cap = run->queueChunkBytes;
+                auto& dout = run->deviceOutputs[(size_t)f];
+                size_t begin = 0;
+                for (uint64_t i = 0; i < m; i++) {
+                    const size_t a = ends[i], b = ends[i + 1];
+                    if (b == a) continue;  // a read of another output file
+                    if (b - a >= cap) return failf(error, CG_ERR_INVALID_ARGUMENT, "record larger than a chunk");
+                    if (b - begin >= cap) {
+                        dout.chunks.emplace_back(begin, a);
+                        begin = a;
+                    }
+                }
+                dout.chunks.emplace_back(begin, (size_t)total);
+                dout.bytes = outDev.release();
+                continue;
+            }
             std::unique_ptr<char[]> bytes(new char[total]);  // left uninitialised: the copy fills it
             DCHECK(cudaMemcpyAsync(bytes.get(), outDev.p, total, cudaMemcpyDeviceToHost, s));
             DCHECK(cudaStreamSynchronize(s));
@@ -555,6 +581,43 @@ int correct_fastq_on_device(const cg_options& options, const std::vector<ByteSpa
     run->reads = n;
     run->records = records + candRecords;
     return CG_OK;
+}
+
+FastqRun::~FastqRun() {
+    for (auto& d : deviceOutputs)
+        if (d.bytes) cudaFree(d.bytes);
+}
+
+int emit_queue_chunks(FastqRun* run, const std::function<bool(int f, char* chunk, int size)>& sink,
+                      std::string* error) {
+    const size_t cap = run->queueChunkBytes;
+    int rc = CG_OK;
+    bool stop = false;
+    for (size_t k = 0; !stop && rc == CG_OK; k++) {
+        bool any = false;
+        for (size_t f = 0; f < run->deviceOutputs.size() && !stop && rc == CG_OK; f++) {
+            const auto& d = run->deviceOutputs[f];
+            if (k >= d.chunks.size()) continue;
+            any = true;
+            const size_t b = d.chunks[k].first, e = d.chunks[k].second;
+            char* chunk = new char[cap];
+            const cudaError_t ce = cudaMemcpy(chunk, static_cast<const char*>(d.bytes) + b, e - b,
+                                              cudaMemcpyDeviceToHost);
+            if (ce != cudaSuccess) {
+                delete[] chunk;
+                rc = failf(error, CG_ERR_CUDA, "chunk copy: %s", cudaGetErrorString(ce));
+            } else if (!sink((int)f, chunk, (int)(e - b))) {
+                stop = true;  // the consumer is gone
+            }
+        }
+        if (!any) break;
+    }
+    for (auto& d : run->deviceOutputs) {
+        if (d.bytes) cudaFree(d.bytes);
+        d.bytes = nullptr;
+        d.chunks.clear();
+    }
+    return rc;
 }
 
 }  // namespace cg

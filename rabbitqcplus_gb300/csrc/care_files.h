@@ -17,6 +17,7 @@
 #include <functional>
 #include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "care_gpu.h"
@@ -40,6 +41,21 @@ struct FastqRun {
     // of output file f go here in order (outputs stays empty), so that the
     // caller can write one range while the next is corrected
     std::function<void(int f, std::unique_ptr<char[]> bytes, size_t size)> onChunk;
+    // Queue protocol: with queueChunkBytes set (and onChunk unset) the output
+    // files stay in device memory, cut into chunks of whole records of under
+    // queueChunkBytes bytes each (the host writer's cut points), and
+    // emit_queue_chunks hands them over (outputs stays empty).
+    size_t queueChunkBytes = 0;
+    struct DeviceOutput {
+        void* bytes = nullptr;                          // device memory
+        std::vector<std::pair<size_t, size_t>> chunks;  // [begin, end) byte ranges
+    };
+    std::vector<DeviceOutput> deviceOutputs;
+
+    FastqRun() = default;
+    FastqRun(const FastqRun&) = delete;
+    FastqRun& operator=(const FastqRun&) = delete;
+    ~FastqRun();  // frees deviceOutputs
 };
 
 // Corrects the reads of `inputs` (the bytes of whole FASTQ files) and returns
@@ -57,6 +73,15 @@ int correct_fastq_on_device(const cg_options& options, const std::vector<ByteSpa
                             bool paired, bool qualityLabels, int numOutputs, const std::vector<char>* forest,
                             uint32_t maxTrees, const std::vector<char>* classifier, FastqRun* run,
                             std::string* error);
+
+// Queue protocol, after correct_fastq_on_device with run->queueChunkBytes set:
+// sink(f, chunk, size) gets every chunk of output file f, the files' chunks
+// alternating (file 0's first, file 1's first, file 0's second, ...); each
+// chunk is copied from device memory straight into a new char[queueChunkBytes]
+// that the sink owns.  Stops when the sink returns false.  Frees the device
+// outputs.  Returns CG_OK or CG_ERR_CUDA (message in *error).
+int emit_queue_chunks(FastqRun* run, const std::function<bool(int f, char* chunk, int size)>& sink,
+                      std::string* error);
 
 }  // namespace cg
 

@@ -370,6 +370,7 @@ RunReport performCorrectionToSink(const ProgramOptions& o, const std::function<v
                                   const ChunkSink& sink) {
     {
         cg::FastqRun dr;
+        dr.queueChunkBytes = 1u << 20;  // the queue protocol's chunks (src/correctionresultoutput.cpp:733-745)
         ProgramOptions od = o;
         const int nfiles = (o.pairType == SequencePairType::PairedEnd && o.inputfiles.size() == 2) ? 2 : 1;
         od.outputfilenames.assign(nfiles, "queue");  // one record stream per queue
@@ -381,34 +382,11 @@ RunReport performCorrectionToSink(const ProgramOptions& o, const std::function<v
             rep.deviceFileIO = true;
             onStart((int)dr.records);  // src/correctionresultoutput.cpp:465-466
             if (dr.records == 0) return rep;
-            // whole records into chunks of under 1 MiB, the host writer's cut points
-            const size_t cap = 1u << 20;
-            std::vector<size_t> at(nfiles, 0);
-            bool ok = true, more = true;
-            while (ok && more) {
-                more = false;
-                for (int f = 0; f < nfiles && ok; f++) {  // the files' chunks alternate
-                    const char* b = dr.outputs[f].get();
-                    const size_t bsize = dr.outputSizes[f];
-                    size_t end = at[f];
-                    while (end < bsize) {
-                        size_t rec = end;
-                        for (int line = 0; line < 4; line++) {
-                            const void* nl = std::memchr(b + rec, '\n', bsize - rec);
-                            rec = (const char*)nl - b + 1;
-                        }
-                        if (rec - end >= cap) throw std::runtime_error("record larger than a 1 MiB chunk");
-                        if (rec - at[f] >= cap) break;
-                        end = rec;
-                    }
-                    if (end == at[f]) continue;
-                    char* chunk = new char[cap];
-                    std::memcpy(chunk, b + at[f], end - at[f]);
-                    ok = sink(f, chunk, (int)(end - at[f]));
-                    at[f] = end;
-                    more |= at[f] < bsize;
-                }
-            }
+            // whole records into chunks of under 1 MiB (the host writer's cut
+            // points), copied from device memory straight into the chunks
+            std::string err;
+            if (cg::emit_queue_chunks(&dr, sink, &err) != CG_OK)
+                throw std::runtime_error("queue chunks: " + err);
             return rep;
         }
     }

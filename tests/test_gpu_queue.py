@@ -1,6 +1,7 @@
 """The queue protocol of the host layer (performCorrectionOutToQueue, through
 its sink form): 1 MiB chunks of whole records whose concatenation is the
-output file, the same from the device file path and the host path.
+output file, the same from the device file path (chunks copied from device
+memory straight into the consumer's buffers) and the host path.
 
 tests/queue_driver.cpp is compiled against the library here (g++).
 """
@@ -60,6 +61,7 @@ def test_queue_chunks_equal_the_output_files(driver, tmp_path, pe):
     assert dev["device"] == 1 and host["device"] == 0
     assert dev["records"] == host["records"] > 0
     assert dev["chunks"] > 1  # 40k reads of ~330 bytes span several 1 MiB chunks
+    assert dev["chunks"] == host["chunks"]  # the same cut points
     o = capi.CareOptions.defaults(30.0, pair_mode=capi.CG_PAIR_PE if pe else capi.CG_PAIR_SE)
     outs = [f"out_{i}.fq" for i in range(len(ins))]
     capi.correct_files(o, ins, str(tmp_path), outs)
