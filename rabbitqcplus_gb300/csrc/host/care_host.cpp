@@ -96,6 +96,8 @@ struct Corrected {
 Corrected runCorrection(const ProgramOptions& o) {
     if (o.inputfiles.empty()) throw std::runtime_error("no input files");
     if (o.correctionType == CorrectionType::Print) throw std::runtime_error("correction type Print is not supported");
+    if (o.correctCandidates && o.correctionTypeCands != CorrectionType::Classic)
+        throw std::runtime_error("candidate correction supports correctionTypeCands Classic only");
     Corrected r;
     std::vector<uint64_t> groupStarts;  // one device append call per input group
     if (o.pairType == SequencePairType::PairedEnd && o.inputfiles.size() == 2) {
@@ -219,6 +221,7 @@ std::vector<char> loadFile(const std::string& path, const char* what) {
 bool correctOnDevice(const ProgramOptions& o, cg::FastqRun* run) {
     if (!o.deviceFileIO || o.inputfiles.empty() || o.outputfilenames.empty()) return false;
     if (o.correctionType == CorrectionType::Print) return false;
+    if (o.correctCandidates && o.correctionTypeCands != CorrectionType::Classic) return false;
     for (const auto& f : o.inputfiles) {
         const FileFormat fmt = detectFormat(f);
         if (fmt != FileFormat::FASTQ && fmt != FileFormat::FASTQGZ) return false;
