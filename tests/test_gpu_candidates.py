@@ -119,6 +119,18 @@ def test_batched_driver_matches_plain():
     assert bat[2]["candidate_corrections"] == plain[2]["candidate_corrections"]
 
 
+def test_batched_driver_with_autotuning_matches_plain():
+    # enough anchors for the tuner (a read count of its own, so that no earlier
+    # test's tuned shape is reused): its trials must not vote
+    cfg = sim.SimConfig(seed=70, genome_length=700_000, repeat_families=20, repeat_copies=4, num_reads=140_000,
+                        sub_rate_5p=0.002, sub_rate_3p=0.02)
+    r = sim.SimReads(cfg)
+    plain = gpu_run(cand_opts(), r)
+    bat = gpu_run(cand_opts(driver=C.CG_DRIVER_BATCHED), r)
+    assert_same(r, bat[0], bat[1], plain[0], plain[1])
+    assert bat[2]["candidate_corrections"] == plain[2]["candidate_corrections"]
+
+
 def test_pass_over_several_calls_and_repeated_passes():
     r = repeats(67)
     n = r.n
