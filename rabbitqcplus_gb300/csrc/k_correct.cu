@@ -1497,14 +1497,50 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
             }
         }
         __syncwarp();
+        // The consensus packed 32 columns per word, forward (fw: column x at
+        // position x) and reverse complemented (rv: position y holds the
+        // complement of column X - 1 - y), one zero word past each; a row's
+        // slice is then a run of whole words at a bit offset in one of them.
+        const int X = La + 2 * nc, nw = (X + 31) / 32;
+        unsigned long long* fw =
+            reinterpret_cast<unsigned long long*>(cons8 + ((size_t)lp + 2 * (size_t)nc + 15) / 16 * 16);
+        unsigned long long* rv = fw + nw + 1;
+        __syncwarp();
+        for (int u = lane; u <= nw; u += 32) {
+            unsigned long long f = 0, r = 0;
+            for (int t = 0; t < 32; t++) {
+                const int x = 32 * u + t;
+                if (x < X) {
+                    f |= (unsigned long long)cons8[x] << (62 - 2 * t);
+                    r |= (unsigned long long)(3u - cons8[X - 1 - x]) << (62 - 2 * t);
+                }
+            }
+            fw[u] = f;
+            rv[u] = r;
+        }
+        __syncwarp();
         // one row per lane
         int votes = 0;
         for (uint32_t j = lane; j < nf; j += 32) {
             const uint32_t g = base + j;
             const uint8_t o = b.forient[g];
             if (o & kRm) continue;
-            votes += vote_candidate(p, b.fshift[g], b.flen[g], (o & 3) == 2, b.fid[g], aid, La,
-                                    [&](int col) { return (uint32_t)cons8[nc + col]; });
+            const int s = b.fshift[g], len = b.flen[g];
+            if (s < -nc || s > nc || s + len > La + nc) continue;
+            const bool rc = (o & 3) == 2;
+            const unsigned long long* src = rc ? rv : fw;
+            const int y0 = rc ? X - (nc + s) - len : nc + s;  // the slice's first position in src
+            const uint32_t id = b.fid[g];
+            for (int w = 0; w * 32 < len; w++) {
+                const int y = y0 + 32 * w, u = y >> 5, off = 2 * (y & 31);
+                unsigned long long v = src[u] << off;
+                if (off) v |= src[u + 1] >> (64 - off);
+                const int rest = len - 32 * w;
+                if (rest < 32) v &= ~0ull << (64 - 2 * rest);
+                vote_word(p, id, w, v);
+            }
+            atomicAdd((uint64_t)id > aid ? &p.candVotes[id].x : &p.candVotes[id].y, 1u);
+            votes++;
         }
         votes = __reduce_add_sync(kFull, votes);
         if (lane == 0 && votes) atomicAdd(&b.counters[kCounterCandidateVotes], (unsigned long long)votes);
@@ -1590,7 +1626,8 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
 // correction, the consensus codes of Lmax + 2 new_columns_to_correct columns
 // follow the row metadata).
 __host__ __device__ inline size_t msa_warp_slice_bytes(int lp, int pitch, const Params& p) {
-    const size_t cand = p.candidates ? ((size_t)lp + 2 * (size_t)p.newColumns + 15) / 16 * 16 : 0;
+    const size_t cols = (size_t)lp + 2 * (size_t)p.newColumns;
+    const size_t cand = p.candidates ? (cols + 15) / 16 * 16 + 2 * ((cols + 31) / 32 + 1) * sizeof(uint64_t) : 0;
     return (size_t)lp * (9 * sizeof(float)) + (size_t)32 * pitch * sizeof(uint32_t) + 32 * sizeof(int4) + cand;
 }
 
