@@ -97,6 +97,10 @@ CASES = {
                                                    read_len_max=250, sub_rate_5p=0.002, sub_rate_3p=0.02),
                                      {"coverage": 30, "k": 20, "quality": True, "candidates": True,
                                       "new_columns": 25}, 0),
+    "se_long_candidates": (sim.SimConfig(seed=119, genome_length=60_000, repeat_families=4, repeat_copies=4,
+                                         num_reads=5_000, read_len_min=200, read_len_max=380, sub_rate_5p=0.002,
+                                         sub_rate_3p=0.02),
+                           {"coverage": 25, "k": 0, "quality": True, "candidates": True}, 0),
     # the last three reads are ambiguous and excluded, so they have no record:
     # the reference writes no quality label for reads after the last record
     "se_label_tail": (sim.SimConfig(seed=118, genome_length=40_000, num_reads=8_000, n_read_fraction=0.3),
