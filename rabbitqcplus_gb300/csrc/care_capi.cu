@@ -1604,6 +1604,9 @@ int cg_get_columns(cg_ctx* c, uint64_t first, uint64_t num, float* features, uin
     std::vector<uint2> hm;
     uint64_t total = 0;
     c->collecting = true;
+    // no candidate votes: this is not a correction pass
+    const int cand = c->params.candidates;
+    c->params.candidates = 0;
     int rc = CG_OK;
     for (uint64_t a = 0; a < num && rc == CG_OK; a += (uint64_t)B) {
         const int cnt = (int)std::min<uint64_t>((uint64_t)B, num - a);
@@ -1644,6 +1647,7 @@ int cg_get_columns(cg_ctx* c, uint64_t first, uint64_t num, float* features, uin
         total += k;
     }
     c->collecting = false;
+    c->params.candidates = cand;
     if (rc != CG_OK) return rc;
     *count = total;
     if (total > capacity)
