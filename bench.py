@@ -4,7 +4,7 @@ Workload (default): the 10 Mbp genome with 200 diverged repeat copies, 2M x
 150 bp single-end reads at 30x, substitution rate rising 0.2% -> 2% from 5'
 to 3' (seeded synthetic data of that shape; k=20, 48 maps, coverage 30).
 
-One step = correction of every anchor of that read set.  Three forms are
+One step = correction of every anchor of that read set.  Four forms are
 timed, each on its own context with the same reads:
   plain            stage kernels per batch, classic decision (bit-exact with the
                    reference)
@@ -12,6 +12,8 @@ timed, each on its own context with the same reads:
                    kernels, classic decision (bit-exact with plain)
   batched_learned  the batched driver with the learned decision (the trained
                    classifier shipped with the package)
+  batched_candidates  the batched driver with candidate correction
+                   (--candidateCorrection; the combine step follows cg_correct)
 and for each the base-level TP/FP/FN against the generator's truth (also for
 the forest decision, untimed).
   value  corrected reads/s of batched_learned with the read store and hash
