@@ -1,35 +1,52 @@
 """Benchmark of the CARE correction hot path on one GB300 (or N replicas).
 
-Workload (default): the 10 Mbp genome with 200 diverged repeat copies, 2M x
-150 bp single-end reads at 30x, substitution rate rising 0.2% -> 2% from 5'
-to 3' (seeded synthetic data of that shape; k=20, 48 maps, coverage 30).
+Workload (default, `--config c4_500mbp_se`): a 500 Mbp genome with 5% repeat
+content, 100M x 150 bp single-end reads at 30x, 1% substitutions, Phred
+qualities as the other workloads (seeded synthetic data of that shape: no
+public dataset is available offline); k = 20, 48 maps, coverage 30.  The read
+store, the 48 hash tables and the signatures of all 100M reads stay resident in
+HBM (inputs far larger than the 129 MB L2, so no flush is needed between
+steps).
 
-One step = correction of every anchor of that read set.  Four forms are
-timed, each on its own context with the same reads:
-  plain            stage kernels per batch, classic decision (bit-exact with the
-                   reference)
-  batched          captured per-batch graphs with persistent work-stealing
-                   kernels, classic decision (bit-exact with plain)
-  batched_learned  the batched driver with the learned decision (the trained
-                   classifier shipped with the package)
+One step = the correction of one window of anchors (4,194,304 by default)
+against the tables of the whole read set; the steps walk through the read
+set window by window (warm-up steps first), so `--warmup 5 --steps 20` covers
+every anchor once.  Forms, each on its own context with the same reads:
+  plain               stage kernels per batch, classic decision (bit-exact
+                      with the reference)
+  batched             captured per-batch graphs with persistent
+                      work-stealing kernels, classic decision (bit-exact with
+                      plain)
+  batched_learned     the batched driver with the learned decision (the
+                      trained classifier shipped with the package) -- `value`
   batched_candidates  the batched driver with candidate correction
-                   (--candidateCorrection; the combine step follows cg_correct)
-and for each the base-level TP/FP/FN against the generator's truth (also for
-the forest decision, untimed).
-  value  corrected reads/s of batched_learned with the read store and hash
-         tables resident in HBM (device time of cg_correct, CUDA events on the
-         library's streams); forms[...] has the same for every form
-  e2e    the same metric through the public C ABI with host buffers: append the
-         reads from host memory, build the store and the tables on the device,
-         load the classifier, correct every anchor and copy every result back
-         to host memory
-The read store (0.5 GB) and tables (several GB) exceed the 129 MB L2, so no
-separate flush is needed between steps.
+                      (--candidateCorrection)
+TP/FP/FN (bases, against the generator's truth) come from an untimed full
+pass of each form over every read (with the combine step for candidate
+correction), and from the forest decision (plain driver, untimed).
+
+  value   corrected reads/s of batched_learned over the timed windows (device
+          time of cg_correct, CUDA events on the library's streams, data
+          resident in HBM); forms[...] has the same for every form
+  e2e     the same metric end to end through the public C ABI from pinned
+          host buffers: per step a fresh context appends every read, builds
+          the read store and the tables on the device, loads the classifier,
+          corrects every anchor and copies every result back to pinned host
+          memory
+  roofline the dominant kernel of the plain form (CUDA events per stage) in
+          HBM bytes, plus its integer-issue fraction
+  cpu_baseline  the reference algorithm (oracle/, bit-exact restatement of
+          the reference's CPU path, pinned to its output) on every host core,
+          over a bounded sample of anchors of the same workload (tables built
+          once, not timed)
+  secondary  the same forms on the 2M-read, 10 Mbp workload with repeats
 
 `--impl reference` times the reference algorithm on the host cores: the
 reference's own build does not exist on the GPU machine, so this arm runs the
-CPU restatement of it (oracle/, bit-exact with the reference on the committed
-fixtures) with all host threads, each step a bounded sample of anchors.
+CPU restatement of it (oracle/, bit-exact with the reference; its speed
+against the reference's own build, measured where both exist, is
+PORT_VS_REFERENCE below) with all host threads: tables built once per
+process, then each step a fixed slice of anchors.
 """
 from __future__ import annotations
 
@@ -50,10 +67,18 @@ import numpy as np  # noqa: E402
 from rabbitqcplus_gb300 import capi, learned, sim  # noqa: E402
 
 METRIC = "corrected reads/s on 1 GB300: plain vs batched+learned, at equal TP/FP vs truth"
-# DRAM bytes (read + write) of align_lane_kernel per candidate, measured by ncu on one
-# 65536-anchor launch of this workload at 2 Mbp: 91.59 MB for 3.777M candidates
-ALIGN_DRAM_BYTES_PER_CANDIDATE = 91.59e6 / 3.777e6
 UNIT = "reads/s"
+WINDOW = 4_194_304  # anchors per step
+# DRAM bytes (read + write) of align_lane_kernel per candidate and its warp
+# instructions per candidate, measured by ncu on one 65536-anchor launch of the
+# 150 bp workload with repeats at 2 Mbp (profiles/align_lane_kernel_c1_2mbp.md:
+# 92.92 MB and 1.28639e9 warp instructions for 3.777M candidates)
+ALIGN_DRAM_BYTES_PER_CANDIDATE = 92.92e6 / 3.777e6
+ALIGN_WARP_INST_PER_CANDIDATE = 1.28639e9 / 3.777e6
+# STEP2 speed of the oracle (the port) over the reference's own build, both on
+# 8 threads of an Intel Xeon @ 2.70 GHz, 2M-read 150 bp workload with repeats,
+# outputs byte-identical (python oracle/port_speed.py --threads 8)
+PORT_VS_REFERENCE = None
 
 
 def env_rank():
@@ -126,71 +151,116 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_arm(reads, opts, sample_anchors: int, threads: int, seconds_target: float = 15.0):
-    """Reference algorithm (oracle restatement) on host cores over a bounded anchor sample."""
-    import oracle
-    t0 = time.perf_counter()
-    orc = oracle.Oracle(opts, reads.sequences, reads.offsets, None, threads=threads)
-    build_s = time.perf_counter() - t0
-    # grow the sample until it takes a few seconds, capped by seconds_target
-    n = min(sample_anchors, reads.n)
-    first = reads.n // 3
-    t0 = time.perf_counter()
-    probe = min(2000, n, reads.n - first)
-    orc.correct(first, probe, threads=threads)
-    dt = time.perf_counter() - t0
-    rate = probe / max(dt, 1e-6)
-    n = int(min(n, max(2000, rate * seconds_target), reads.n - first))
-    t0 = time.perf_counter()
-    orc.correct(first, n, threads=threads)
-    dt = time.perf_counter() - t0
-    orc.close()
-    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} anchors (ids {first}..{first + n - 1}) of the workload against its full "
-                      f"hash tables; table build {build_s:.1f}s not included"}
+def coverage_of(cfg: sim.SimConfig) -> int:
+    return round(cfg.num_reads * (cfg.read_len_min + cfg.read_len_max) / 2 / cfg.genome_length)
+
+
+def windows_of(n: int, w: int, paired: bool):
+    w = max(2, w & ~1) if paired else max(1, w)
+    return [(s, min(w, n - s)) for s in range(0, n, w)]
+
+
+def workload_desc(name: str, cfg: sim.SimConfig) -> dict:
+    cov = coverage_of(cfg)
+    return {"workload": f"{name}: genome {cfg.genome_length} bp, {cfg.num_reads} reads "
+                        f"{cfg.read_len_min}-{cfg.read_len_max} bp{' paired' if cfg.paired else ''}, {cov}x, "
+                        f"k=20, 48 maps",
+            "reads": cfg.num_reads, "coverage": cov, "kmerlength": 20, "hashmaps": 48, "paired": bool(cfg.paired),
+            "l2": "inputs larger than L2 (read store + tables > 129 MB); no flush"}
+
+
+class Oracle1:
+    """The oracle's tables of one read set, built once; slices of anchors timed."""
+
+    def __init__(self, reads, cfg, threads):
+        import oracle
+        self.threads = threads
+        opts = capi.CareOptions.defaults(float(coverage_of(cfg)), kmerlength=20,
+                                         pair_mode=capi.CG_PAIR_PE if cfg.paired else capi.CG_PAIR_SE)
+        t0 = time.perf_counter()
+        self.orc = oracle.Oracle(opts, reads.sequences, reads.offsets, None, threads=threads)
+        self.build_s = time.perf_counter() - t0
+        self.n = reads.n
+        self.paired = bool(cfg.paired)
+
+    def slice_size(self, seconds: float) -> int:
+        """Anchors that take about `seconds` on the host cores (probed)."""
+        first = (self.n // 3) & ~1
+        probe = min(20_000, self.n - first) & ~1
+        t0 = time.perf_counter()
+        self.orc.correct(first, probe, threads=self.threads)
+        rate = probe / max(time.perf_counter() - t0, 1e-6)
+        return max(2000, min(int(rate * seconds), self.n // 2)) & ~1
+
+    def time_slice(self, first: int, count: int) -> float:
+        first = min(first, self.n - count) & ~1
+        t0 = time.perf_counter()
+        self.orc.correct(first, count, threads=self.threads)
+        return time.perf_counter() - t0
+
+    def close(self):
+        self.orc.close()
+
+
+def cpu_baseline(reads, cfg, threads, seconds=15.0):
+    o = Oracle1(reads, cfg, threads)
+    count = o.slice_size(seconds / 3)
+    first = (reads.n // 3) & ~1
+    dt = o.time_slice(first, count * 3)
+    o.close()
+    return {"value": count * 3 / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{count * 3} anchors (ids {first}..{first + count * 3 - 1}) of the workload against the "
+                      f"tables of all {reads.n} reads (built once in {o.build_s:.1f} s, not timed)",
+            "port_vs_reference_step2": PORT_VS_REFERENCE}
+
+
+def reference_arm(args, cfg, name, threads):
+    reads = sim.SimReads(cfg)
+    o = Oracle1(reads, cfg, threads)
+    count = o.slice_size(4.0)
+    total_anchors, total_s = 0, 0.0
+    for i in range(args.warmup + args.steps):
+        first = (i * count * 7919) % max(reads.n - count, 1)  # slices spread over the read set
+        dt = o.time_slice(first, count)
+        if i >= args.warmup:
+            total_anchors += count
+            total_s += dt
+    o.close()
+    v = total_anchors / total_s
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": workload_desc(name, cfg), "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"each step {count} anchors of the workload against the tables of all "
+                                       f"{reads.n} reads (built once in {o.build_s:.1f} s, not timed)",
+                             "port_vs_reference_step2": PORT_VS_REFERENCE},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c1_10mbp_repeats_se")
+    ap.add_argument("--config", default="c4_500mbp_se")
     ap.add_argument("--genome", type=int, default=0, help="scale the config to this genome length")
-    ap.add_argument("--cpu-sample", type=int, default=200_000)
+    ap.add_argument("--window", type=int, default=WINDOW, help="anchors per step")
+    ap.add_argument("--secondary", default="c1_10mbp_repeats_se", help="second workload ('none' to skip)")
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--forms", default="plain,batched,batched_learned,batched_candidates")
     args = ap.parse_args()
     rank, world, local = env_rank()
     threads = os.cpu_count() or 1
-
     cfg = sim.scaled(args.config, args.genome) if args.genome else sim.CONFIGS[args.config]
-    coverage = round(cfg.num_reads * (cfg.read_len_min + cfg.read_len_max) / 2 / cfg.genome_length)
-    opts = capi.CareOptions.defaults(float(coverage), kmerlength=20,
-                                     pair_mode=capi.CG_PAIR_PE if cfg.paired else capi.CG_PAIR_SE)
-    config = {"workload": f"{args.config}: genome {cfg.genome_length} bp, {cfg.num_reads} reads "
-                          f"{cfg.read_len_min}-{cfg.read_len_max} bp, {coverage}x, k=20, 48 maps",
-              "reads": cfg.num_reads, "coverage": coverage, "kmerlength": 20, "hashmaps": 48,
-              "paired": bool(cfg.paired), "l2": "inputs larger than L2 (read store + tables > 129 MB)"}
 
     if args.impl == "reference":
-        if rank != 0:
-            return
-        reads = sim.SimReads(cfg)
-        vals = []
-        for i in range(args.warmup + args.steps):
-            r = cpu_arm(reads, capi.CareOptions.defaults(float(coverage), kmerlength=20), args.cpu_sample,
-                        threads, seconds_target=8.0)
-            if i >= args.warmup:
-                vals.append(r["value"])
-        v = statistics.median(vals)
-        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "u32", "data": "synthetic", "config": config, "impl": "reference",
-                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": r["sample"]},
-                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
+        if rank == 0:
+            reference_arm(args, cfg, args.config, threads)
         return
 
     import torch
@@ -199,21 +269,28 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    reads = sim.SimReads(cfg)
-    opts.device = local
 
     def barrier():
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
 
+    def max_over_ranks(x: float) -> float:
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        if dist is not None:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
     model = open(learned.DEFAULT_MODEL, "rb").read()
     forest = open(os.path.join(REPO, "tests", "golden", "forest_anchor.bin"), "rb").read()
-    n_total = reads.n
+    hbm_peak, peak_kind = measured_peaks()
+    forms_wanted = [f for f in args.forms.split(",") if f]
+    if "batched_learned" not in forms_wanted:
+        forms_wanted.append("batched_learned")
 
-    def form_options(form):
-        o = capi.CareOptions.defaults(opts.estimated_coverage, kmerlength=20, pair_mode=opts.pair_mode,
-                                      device=local)
+    def form_options(cfg_, form):
+        o = capi.CareOptions.defaults(float(coverage_of(cfg_)), kmerlength=20, device=local,
+                                      pair_mode=capi.CG_PAIR_PE if cfg_.paired else capi.CG_PAIR_SE)
         if form in ("batched", "batched_learned", "batched_candidates"):
             o.driver = capi.CG_DRIVER_BATCHED
         if form == "batched_candidates":
@@ -224,9 +301,9 @@ def main():
             o.correction_type = capi.CG_CORR_FOREST
         return o
 
-    def make_ctx(form):
-        g = capi.CareGpu(form_options(form))
-        g.append_reads(reads.sequences, reads.offsets)
+    def make_ctx(reads, cfg_, form, seqs=None, offs=None):
+        g = capi.CareGpu(form_options(cfg_, form))
+        g.append_reads(reads.sequences if seqs is None else seqs, reads.offsets if offs is None else offs)
         g.build_tables()
         if form == "batched_learned":
             g.load_classifier(model)
@@ -234,188 +311,242 @@ def main():
             g.load_forest(forest)
         return g
 
-    flags = np.zeros(n_total, np.uint8)
-    out = None
+    def window_digest(flags, rows, lengths):
+        """Order-dependent checksum of a window's flags and corrected bases (rows
+        of uncorrected anchors and bytes past a read's end do not count)."""
+        L = rows.shape[1]
+        w = (np.arange(1, L + 1, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15)) | np.uint64(1)
+        corr = (flags & capi.CG_RESULT_CORRECTED) != 0
+        h = int(np.sum(flags.astype(np.uint64) * np.arange(1, flags.size + 1, dtype=np.uint64)))
+        idx = np.nonzero(corr)[0]
+        for a in range(0, idx.size, 1 << 18):
+            sl = idx[a:a + (1 << 18)]
+            m = np.arange(L)[None, :] < lengths[sl][:, None]
+            v = np.where(m, rows[sl], 0).astype(np.uint64)
+            h = (h * 1000003 + int(np.sum((v * w[None, :]).sum(axis=1) * (sl.astype(np.uint64) + np.uint64(1))))) \
+                & 0xFFFFFFFFFFFFFFFF
+        return h
 
-    def run_form(form, steps, warmup, clk=None):
-        """Resident correction: build once, then time `steps` full passes (device time of cg_correct)."""
-        nonlocal out
-        g = make_ctx(form)
+    def score_pass(g, reads, wins, lmax, digest=False):
+        """Untimed pass over every window; TP/FP/FN of the whole read set (and
+        per-window checksums of the results)."""
+        cand = bool(g.options.correct_candidates)
+        wmax = max(c for _, c in wins)
+        if cand:
+            flags_all = np.zeros(reads.n, np.uint8)
+            rows_all = np.zeros((reads.n, lmax), np.uint8)
+            for s, c in wins:
+                g.correct(s, c, flags_all[s:s + c], rows_all[s:s + c], combine=False)
+            g.combine(0, flags_all)
+            return reads.score_results(0, flags_all, rows_all), None
+        flags = np.zeros(wmax, np.uint8)
+        rows = np.zeros((wmax, lmax), np.uint8)
+        tot = {"tp": 0, "fp": 0, "fn": 0, "reads_scored": 0}
+        digests = []
+        for s, c in wins:
+            g.correct(s, c, flags[:c], rows[:c])
+            sc = reads.score_results(s, flags[:c], rows[:c])
+            for k in tot:
+                tot[k] += sc[k]
+            if digest:
+                digests.append(window_digest(flags[:c], rows[:c], reads.lengths[s:s + c]))
+        return tot, (digests if digest else None)
+
+    def run_form(reads, cfg_, form, wins, steps, warmup, clk=None, digest=False):
+        g = make_ctx(reads, cfg_, form)
         n, lmax = g.read_info()
-        if out is None:
-            out = np.zeros((n, lmax), np.uint8)
-        for _ in range(warmup):
-            g.correct(0, n, flags, out)
-        st0 = g.stats()
+        wmax = max(c for _, c in wins)
+        flags = np.zeros(wmax, np.uint8)
+        rows = np.zeros((wmax, lmax), np.uint8)
+        dev, anchors = 0.0, 0
+        st0 = None
+        wall0 = 0.0
+        for i in range(warmup + steps):
+            if i == warmup:
+                barrier()
+                if clk:
+                    clk.resume()
+                st0 = g.stats()
+                wall0 = time.perf_counter()
+            s, c = wins[i % len(wins)]
+            g.correct(s, c, flags[:c], rows[:c], combine=False)
+            if i >= warmup:
+                dev += g.stats()["seconds_correct"]
+                anchors += c
         barrier()
-        if clk:
-            clk.resume()
-        t0 = time.perf_counter()
-        dev = 0.0
-        for _ in range(steps):
-            g.correct(0, n, flags, out)
-            dev += g.stats()["seconds_correct"]
-        barrier()
-        wall = time.perf_counter() - t0
+        wall = time.perf_counter() - wall0
         if clk:
             clk.pause()
         st1 = g.stats()
-        final = capi.apply_corrections(reads.sequences, reads.offsets, flags, out)
+        sc, res = score_pass(g, reads, wins, lmax, digest)
         g.close()
-        t = torch.tensor([dev], dtype=torch.float64, device="cuda")
-        if dist is not None:
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev = float(t.item())
-        return {"n": n, "lmax": lmax, "dev": dev, "wall": wall, "st0": st0, "st1": st1, "score": reads.score(final),
-                "flags": flags.copy() if form in ("plain", "batched") else None,
-                "out": out.copy() if form in ("plain", "batched") else None}
+        return {"n": n, "lmax": lmax, "dev": max_over_ranks(dev), "anchors": anchors, "wall": wall, "st0": st0,
+                "st1": st1, "score": sc, "res": res}
 
-    hbm_peak, peak_kind = measured_peaks()
-
-    def alg_bytes(r, steps):
-        # algorithmic bytes of one pass (per anchor: its 2-bit row 40 B, 48 keys 384 B, 48 lookup slots
-        # 768 B, 4 B per raw id, 44 B per unique candidate (row + length), the output record)
-        d = {k: (r["st1"][k] - r["st0"][k]) / steps for k in ("raw_candidate_ids", "unique_candidates")}
+    def summary(r):
+        sec = r["dev"]
+        d = {k: (r["st1"][k] - r["st0"][k]) for k in ("raw_candidate_ids", "unique_candidates", "kernel_launches")}
         pitch = (r["lmax"] + 15) // 16
-        return r["n"] * (4 * pitch + 48 * 8 + 48 * 16 + r["lmax"] + 1) + 4 * d["raw_candidate_ids"] + \
+        b = r["anchors"] * (4 * pitch + 48 * 8 + 48 * 16 + r["lmax"] + 1) + 4 * d["raw_candidate_ids"] + \
             (4 * pitch + 4) * d["unique_candidates"]
-
-    def summary(r, steps):
-        sec = r["dev"] / steps
-        b = alg_bytes(r, steps)
-        return {"value": world * r["n"] / sec, "unit": UNIT, "ms_per_step": sec * 1e3,
+        return {"value": world * r["anchors"] / sec, "unit": UNIT, "ms_per_step": sec / max(r["steps"], 1) * 1e3,
                 "alg_gbs": b / sec / 1e9, "hbm_frac": b / sec / 1e9 / hbm_peak,
                 "tp": r["score"]["tp"], "fp": r["score"]["fp"], "fn": r["score"]["fn"],
-                "gpu_launches_per_step": (r["st1"]["kernel_launches"] - r["st0"]["kernel_launches"]) / steps}
+                "gpu_launches_per_step": d["kernel_launches"] / max(r["steps"], 1)}
+
+    def run_workload(name, cfg_, steps, warmup, clk, with_roofline):
+        reads = sim.SimReads(cfg_)
+        wins = windows_of(reads.n, args.window, bool(cfg_.paired))
+        runs = {}
+        for form in forms_wanted:
+            runs[form] = run_form(reads, cfg_, form, wins, steps, warmup, clk, digest=form in ("plain", "batched"))
+            runs[form]["steps"] = steps
+        forest_run = run_form(reads, cfg_, "forest", wins, 0, 0)
+        forms = {f: summary(r) for f, r in runs.items()}
+        forms["forest"] = {"tp": forest_run["score"]["tp"], "fp": forest_run["score"]["fp"],
+                           "fn": forest_run["score"]["fn"], "driver": "plain", "timed": False}
+        if "plain" in runs and "batched" in runs:
+            # every flag and corrected base of every read, compared window by window
+            forms["batched_bit_exact_with_plain"] = runs["plain"]["res"] == runs["batched"]["res"] and \
+                runs["plain"]["score"] == runs["batched"]["score"]
+        bl = runs["batched_learned"]
+        forms["batched_shape"] = {k: bl["st1"][k] for k in ("batch_anchors", "align_blocks", "msa_warps",
+                                                          "streams", "seconds_tune")}
+        out = {"reads": reads, "runs": runs, "forms": forms, "wins": wins}
+        return out
+
+    def roofline_of(plain, clk_mhz):
+        p0, p1 = plain["st0"], plain["st1"]
+        steps = plain["steps"]
+        n_anchors = plain["anchors"]
+        lmax = plain["lmax"]
+        stages = {"align": p1["seconds_align"] - p0["seconds_align"],
+                  "filter": p1["seconds_filter"] - p0["seconds_filter"],
+                  "msa": p1["seconds_msa"] - p0["seconds_msa"],
+                  "candidates": p1["seconds_candidates"] - p0["seconds_candidates"]}
+        dom = max(stages, key=stages.get)
+        cands = p1["unique_candidates"] - p0["unique_candidates"]
+        msa_c = p1["msa_candidates"] - p0["msa_candidates"]
+        raw = p1["raw_candidate_ids"] - p0["raw_candidate_ids"]
+        wp = (lmax + 31) // 32 + 1
+        pitch = (lmax + 15) // 16
+        if dom == "align":
+            kbytes = cands * (4 + 2 + 16 * wp + 8) + n_anchors * (8 * wp + 10)
+            launches = p1["align_launches"] - p0["align_launches"]
+            kname = "align_lane_kernel"
+        elif dom == "msa":
+            kbytes = msa_c * (13 + 4 * pitch) + n_anchors * (4 * pitch + 2 + lmax + 1)
+            launches = p1["msa_launches"] - p0["msa_launches"]
+            kname = "msa_warp_kernel"
+        else:
+            kbytes = raw * 4 + n_anchors * 48 * 24
+            launches = max(p1["align_launches"] - p0["align_launches"], 1)
+            kname = "gather_unique_kernel"
+        launches = max(launches, 1)
+        dur = stages[dom] / launches
+        # the path's algorithmic bytes per anchor: 2-bit anchor row, 48 signature
+        # keys and 48 lookup slots probed, 4 B per raw id, the unique candidates'
+        # rows and lengths, the result written (flag and corrected bases); one
+        # launch of the dominant kernel processes one batch of anchors
+        path_bytes = n_anchors * (4 * pitch + 48 * 8 + 48 * 16 + 1 + lmax) + 4 * raw + cands * (4 * pitch + 4)
+        bytes_launch = path_bytes / launches
+        achieved = bytes_launch / dur / 1e9
+        roof = {"bound": "hbm", "kernel": kname, "form": "plain", "achieved": achieved, "peak": hbm_peak,
+                "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": (ALIGN_DRAM_BYTES_PER_CANDIDATE * cands / launches) if dom == "align" else None,
+                "peak_kind": peak_kind, "algorithmic_bytes_per_launch": bytes_launch,
+                "algorithmic_bytes_per_anchor": path_bytes / max(n_anchors, 1),
+                "kernel_bytes_per_launch": kbytes / launches, "avg_launch_ms": dur * 1e3,
+                "stage_seconds_per_step": {k: v / max(steps, 1) for k, v in stages.items()},
+                "note": "integer-issue bound, see `int`; the HBM fraction is low by construction and traffic "
+                        "(measured DRAM bytes, ncu per candidate x candidates per launch) is below the algorithmic "
+                        "bytes because the planes of candidates shared between anchors hit in L2"}
+        if dom == "align":
+            # warp instructions per candidate (ncu, committed profile) x the launch's candidates,
+            # over the launch's CUDA-event time, against 152 SMs x 4 schedulers x 1 instruction per
+            # cycle at the median SM clock sampled during the timed region
+            mhz = clk_mhz or 2070.0
+            inst = ALIGN_WARP_INST_PER_CANDIDATE * cands / launches
+            peak_i = 152 * 4 * mhz * 1e6
+            roof["int"] = {"bound": "int-issue", "achieved": inst / dur / 1e9, "peak": peak_i / 1e9,
+                           "unit": "G warp-instructions/s", "frac": inst / dur / peak_i, "sm_mhz": mhz,
+                           "warp_instructions_per_candidate": ALIGN_WARP_INST_PER_CANDIDATE,
+                           "source": "smsp__inst_executed.sum per candidate from ncu "
+                                     "(profiles/align_lane_kernel_c1_2mbp.md) x candidates of an average launch"}
+        return roof
 
     clk = ClockSampler(local, paused=True)
     with clk:
-        plain = run_form("plain", args.steps, args.warmup, clk)
-        bat = run_form("batched", args.steps, args.warmup, clk)
-        bl = run_form("batched_learned", args.steps, args.warmup, clk)
-        cand = run_form("batched_candidates", args.steps, args.warmup, clk)
-    forest_run = run_form("forest", 1, 0)
-    st0, st1 = bl["st0"], bl["st1"]
-    n = bl["n"]
-    lmax = bl["lmax"]
-    dev_seconds = bl["dev"]
-    value = world * n * args.steps / dev_seconds
-    launches = st1["kernel_launches"] - st0["kernel_launches"]
-    same = bool(np.array_equal(plain["flags"], bat["flags"]))
-    if same:
-        idx = np.nonzero(plain["flags"] & capi.CG_RESULT_CORRECTED)[0]
-        lens = reads.lengths[idx]
-        po, bo = plain["out"][idx], bat["out"][idx]
-        mask = np.arange(lmax)[None, :] < lens[:, None]
-        same = bool(np.array_equal(np.where(mask, po, 0), np.where(mask, bo, 0)))
-    forms = {"plain": summary(plain, args.steps), "batched": summary(bat, args.steps),
-             "batched_learned": summary(bl, args.steps),
-             # --candidateCorrection: device time of cg_correct; the combine step after it is one
-             # thread per read
-             "batched_candidates": summary(cand, args.steps),
-             "forest": {"tp": forest_run["score"]["tp"], "fp": forest_run["score"]["fp"],
-                        "fn": forest_run["score"]["fn"], "driver": "plain", "timed": False},
-             "batched_bit_exact_with_plain": same,
-             "batched_shape": {k: bl["st1"][k] for k in ("batch_anchors", "align_blocks", "msa_warps", "streams",
-                                                       "seconds_tune")}}
+        head = run_workload(args.config, cfg, args.steps, args.warmup, clk, True)
+    reads = head["reads"]
+    forms = head["forms"]
+    bl = head["runs"]["batched_learned"]
+    value = forms["batched_learned"]["value"]
+    launches = bl["st1"]["kernel_launches"] - bl["st0"]["kernel_launches"]
+    clocks = clk.summary()
+    roof = roofline_of(head["runs"]["plain"], clocks.get("sm_mhz")) if "plain" in head["runs"] else None
 
-    # roofline of the dominant kernel, from the plain form's per-stage CUDA events (the
-    # batched form runs the same kernels inside graph replays, where they are not timed apart)
-    p0, p1 = plain["st0"], plain["st1"]
-    stages = {"align": p1["seconds_align"] - p0["seconds_align"],
-              "filter": p1["seconds_filter"] - p0["seconds_filter"],
-              "msa": p1["seconds_msa"] - p0["seconds_msa"],
-              "candidates": p1["seconds_candidates"] - p0["seconds_candidates"]}
-    dom = max(stages, key=stages.get)
-    per_step_cands = (p1["unique_candidates"] - p0["unique_candidates"]) / args.steps
-    per_step_msa = (p1["msa_candidates"] - p0["msa_candidates"]) / args.steps
-    wp = (lmax + 31) // 32 + 1
-    pitch = (lmax + 15) // 16
-    if dom == "align":
-        # align_lane_kernel, per candidate: its id (4 B) and length (2 B), its forward and
-        # reverse-complement hi/lo planes (4*wp words), the packed result (8 B);
-        # per anchor: its forward planes (2*wp words), length and two offsets (10 B)
-        bytes_step = per_step_cands * (4 + 2 + 16 * wp + 8) + n * (8 * wp + 10)
-        launches_k = (p1["align_launches"] - p0["align_launches"])
-        kname = "align_lane_kernel"
-    elif dom == "msa":
-        # msa_warp_kernel, per kept candidate: its record (id, shift, length, orientation,
-        # weight = 13 B) and its 2-bit row; per anchor: its 2-bit row, length, the
-        # corrected bases and flags written
-        bytes_step = per_step_msa * (13 + 4 * pitch) + n * (4 * pitch + 2 + lmax + 1)
-        launches_k = (p1["msa_launches"] - p0["msa_launches"])
-        kname = "msa_warp_kernel"
-    else:
-        bytes_step = (p1["raw_candidate_ids"] - p0["raw_candidate_ids"]) / args.steps * 4 + n * 48 * 24
-        launches_k = max(p1["align_launches"] - p0["align_launches"], 1)
-        kname = "gather_unique_kernel"
-    dur = stages[dom] / max(launches_k, 1)
-    kernel_bytes_launch = bytes_step * args.steps / max(launches_k, 1)
-    # The path's algorithmic bytes per anchor (the scope's per-unit figure):
-    # 2-bit anchor row, 48 signature keys and 48 lookup slots probed, the raw
-    # ids (4 B each) and the unique candidates' rows and lengths (44 B each,
-    # at 150 bp), and the result written (flag and corrected bases); one
-    # launch of the dominant kernel processes the anchors of one batch.
-    per_step_raw = (p1["raw_candidate_ids"] - p0["raw_candidate_ids"]) / args.steps
-    path_bytes_step = n * (4 * pitch + 48 * 8 + 48 * 16 + 1 + lmax) + 4 * per_step_raw + \
-        per_step_cands * (4 * pitch + 4)
-    bytes_launch = path_bytes_step * args.steps / max(launches_k, 1)
-    achieved = bytes_launch / dur / 1e9
-    traffic = None
-    if dom == "align":
-        # DRAM bytes per candidate measured by ncu (ALIGN_DRAM_BYTES_PER_CANDIDATE), scaled by the
-        # candidates of an average launch (the traffic grows with the candidates processed)
-        traffic = ALIGN_DRAM_BYTES_PER_CANDIDATE * per_step_cands * args.steps / max(launches_k, 1)
-    roof = {"bound": "hbm", "kernel": kname, "form": "plain", "achieved": achieved, "peak": hbm_peak,
-            "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic, "peak_kind": peak_kind,
-            "algorithmic_bytes_per_launch": bytes_launch,
-            "algorithmic_bytes_per_anchor": path_bytes_step / max(n, 1),
-            "kernel_bytes_per_launch": kernel_bytes_launch,
-            "avg_launch_ms": dur * 1e3,
-            "stage_seconds_per_step": {k: v / args.steps for k, v in stages.items()},
-            "note": "integer-pipe bound (ALU pipe 75% active in ncu); the fraction is of the HBM roofline, and "
-                    "traffic (measured DRAM bytes) is below the algorithmic bytes because candidate planes "
-                    "shared between anchors hit in L2"}
-
-    # e2e through the C ABI with host buffers (batched + learned)
+    # e2e through the C ABI from pinned host memory (batched + learned)
     e2e = None
     if not args.no_e2e:
-        # one untimed step, then `steps` timed ones, each through a fresh context
-        for i in range(1 + args.steps):
+        n = reads.n
+        lmax = int(reads.lengths.max())
+        flags = np.zeros(n, np.uint8)
+        rows = np.zeros((n, lmax), np.uint8)
+        rt = torch.cuda.cudart()
+        pinned = []
+        for a in (reads.sequences, reads.offsets, flags, rows):
+            # page-lock the caller's buffers (untimed set-up), as a caller streaming reads would
+            if int(rt.cudaHostRegister(a.ctypes.data, a.nbytes, 0)) == 0:
+                pinned.append(a)
+        k = max(1, args.e2e_steps)
+        te = 0.0
+        for i in range(1 + k):
             barrier()
-            if i == 1:
-                t0 = time.perf_counter()
-            g2 = make_ctx("batched_learned")
-            g2.correct(0, n, flags, out)
+            t0 = time.perf_counter()
+            g2 = make_ctx(reads, cfg, "batched_learned")
+            g2.correct(0, n, flags, rows)
             g2.close()
-        barrier()
-        te = time.perf_counter() - t0
-        tt = torch.tensor([te], dtype=torch.float64, device="cuda")
-        if dist is not None:
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e = {"value": world * n * args.steps / float(tt.item()), "unit": UNIT, "steps": args.steps,
+            barrier()
+            if i >= 1:
+                te += time.perf_counter() - t0
+        for a in pinned:
+            rt.cudaHostUnregister(a.ctypes.data)
+        te = max_over_ranks(te)
+        e2e = {"value": world * n * k / te, "unit": UNIT, "steps": k, "seconds_per_step": te / k,
                "h2d_bytes_per_step": int(reads.sequences.nbytes + reads.offsets.nbytes + len(model)),
-               "d2h_bytes_per_step": int(flags.nbytes + out.nbytes),
+               "d2h_bytes_per_step": int(flags.nbytes + rows.nbytes), "pinned": len(pinned) == 4,
                "form": "batched_learned",
-               "includes": "append from host, device read-store + table build, classifier load, correction, "
-                           "results to host (launch shapes tuned in the warm-up)"}
+               "includes": "fresh context, append of every read from pinned host memory, device read-store and "
+                           "table build, classifier load, correction of every anchor, every result to pinned host "
+                           "memory, destroy"}
+        del flags, rows
+
+    secondary = None
+    if args.secondary and args.secondary != "none" and args.secondary != args.config:
+        cfg2 = sim.CONFIGS[args.secondary]
+        sec = run_workload(args.secondary, cfg2, args.steps, args.warmup, None, False)
+        secondary = {"config": workload_desc(args.secondary, cfg2), "forms": sec["forms"]}
+        del sec
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_arm(reads, capi.CareOptions.defaults(float(coverage), kmerlength=20), args.cpu_sample, threads)
+        cpu = cpu_baseline(reads, cfg, threads)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": dev_seconds / args.steps * 1e3, "higher_is_better": True,
+                "warmup": args.warmup, "ms_per_step": bl["dev"] / args.steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-                "config": config, "form": "batched_learned", "forms": forms, "e2e": e2e,
-                "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
-                "wall_seconds_timed": bl["wall"], "build_seconds": st1["seconds_build"],
-                "score": bl["score"], "stats": {k: st1[k] for k in ("raw_candidate_ids", "unique_candidates",
-                                                                    "aligned_candidates", "msa_candidates",
-                                                                    "msa_builds", "corrected_anchors", "hq_anchors", "table_keys",
-                                                                    "table_values", "learned_columns",
-                                                                    "learned_corrections")}}
+                "config": dict(workload_desc(args.config, cfg), window_anchors=args.window,
+                               step="one window of anchors against the tables of the whole read set"),
+                "form": "batched_learned", "forms": forms, "e2e": e2e, "gpu_launches": int(launches),
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "wall_seconds_timed": bl["wall"],
+                "build_seconds": bl["st1"]["seconds_build"], "score": bl["score"],
+                "stats": {k: bl["st1"][k] for k in ("raw_candidate_ids", "unique_candidates", "aligned_candidates",
+                                                   "msa_candidates", "msa_builds", "corrected_anchors",
+                                                   "hq_anchors", "table_keys", "table_values",
+                                                   "learned_columns", "learned_corrections")},
+                "secondary": secondary}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

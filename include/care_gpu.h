@@ -101,7 +101,30 @@ typedef struct cg_options {
      * plain 4-line FASTQ still take the host path), 1 = always parse and write
      * on the host; both give the same files */
     int32_t host_file_io;
-    int32_t reserved[3];
+    /* qualityScoreBits (8; 0 means 8): bits per quality score in the read
+     * store.  With 2 or 1 every score is stored binned -- 2 bits: Q <= 4 -> '$',
+     * <= 13 -> '(', <= 20 -> '1', else '9'; 1 bit: Q <= 13 -> '(', else '5' --
+     * and a row's positions past its read's end hold the first bin's score
+     * (reference: include/qualityscorecompression.hpp:25-73 and 74-140,
+     * applied by include/chunkedreadstorageconstruction.hpp:240-268, decoded
+     * by include/chunkedreadstorage.hpp:532-607).  Only the scores the
+     * correction reads change; output files keep the input's scores. */
+    int32_t quality_score_bits;
+    /* fixedNumberOfReads (0 = every read): only reads [0, n) are corrected as
+     * anchors -- cg_correct returns flags 0 for later reads -- while every read
+     * stays in the hash tables and can be a candidate (reference:
+     * include/options.hpp:126-133, src/correct_cpu.cpp:97-102).  Above the
+     * number of reads it means every read; even in paired mode. */
+    uint32_t fixed_number_of_reads;
+    int32_t reserved0;
+    /* memoryForHashtables (bytes; 0 = no limit).  The reference builds its
+     * maps in rounds of (limit / (12 bytes x reads)) - 2 under this limit
+     * (src/cpuminhasherconstruction.cpp:27-165, include/ordinaryminhasher.hpp:
+     * 350-372); when the first round cannot hold num_hash_functions maps, how
+     * many maps it ends with depends on the sizes of its compacted host tables,
+     * so cg_build_tables refuses the run with CG_ERR_UNSUPPORTED rather than
+     * correct with a different number of maps. */
+    uint64_t hashtable_memory_bytes;
 } cg_options;
 
 #define CG_DRIVER_PLAIN 0
@@ -149,6 +172,9 @@ typedef struct cg_stats {
     uint64_t learned_overflow;        /* columns beyond the per-batch records (fallback decision) */
     /* candidate correction (correct_candidates) */
     uint64_t candidate_corrections;   /* candidates corrected by HQ anchors, accumulated */
+    /* learned decision: classifier blocks that gave up waiting for their
+     * tensor-core MMAs, accumulated (each such call returned CG_ERR_TIMEOUT) */
+    uint64_t classifier_timeouts;
 } cg_stats;
 
 /* Fill *o with the reference defaults. */
@@ -167,6 +193,25 @@ void cg_destroy(cg_ctx* ctx);
  * die with the reset.  No counterpart in the reference (its CPU path keeps no
  * device memory). */
 int cg_release_cached_memory(int device);
+
+/* Fault injection for tests of the out-of-memory path (no counterpart in
+ * the reference): after `after` more requests for context device memory
+ * succeed, every later request fails as if the device were full -- the
+ * per-process block cache is emptied first, as on a real failure -- and the
+ * call that made it returns CG_ERR_OUT_OF_MEMORY.  after < 0 switches it off.
+ * Process-wide. */
+int cg_set_allocation_fault(int64_t after);
+
+/* Polls (mbarrier try-waits) a learned-decision inference block spends on
+ * each of its tensor-core MMAs before it gives up on its remaining columns,
+ * on `device`; polls < 0 restores the default (1 << 20, far above what an
+ * MMA needs).  A block that gives up leaves its columns to the fallback
+ * decision, drains its MMAs and releases its tensor memory; the call that ran
+ * it (cg_correct, cg_correct_files, cg_classifier_logits) returns
+ * CG_ERR_TIMEOUT and cg_stats.classifier_timeouts counts it.  A diagnostic
+ * hook (e.g. polls = 0 makes every such wait give up); no counterpart in the
+ * reference. */
+int cg_set_classifier_wait_limit(int device, int64_t polls);
 
 /* Message of the last failing call on this context (never NULL). */
 const char* cg_last_error(const cg_ctx* ctx);
@@ -275,7 +320,8 @@ int cg_get_candidates(cg_ctx* ctx, uint64_t anchor, uint32_t* out, uint32_t capa
  * scratch is a fixed 33 KiB device array inside the library, held by every
  * GPU that loads it until the process exits, shared by all calls and left
  * holding the last call's data; so calls must not overlap on the GPU.  The
- * first call on a device looks the array up (do it before any stream capture).
+ * first call on a device looks the array up (do it before any stream capture);
+ * cg_release_cached_memory(device) makes the next call look it up again.
  * An anchor with more than 8192 raw bucket hits is rejected with
  * CG_ERR_INVALID_ARGUMENT (cg_get_candidates handles it).
  */

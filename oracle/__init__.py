@@ -37,10 +37,18 @@ def build(force: bool = False) -> str:
     return LIB
 
 
-def build_reference(ref_dir: str = "/root/reference", jobs: int = 8) -> bool:
+def reference_dir() -> str:
+    """Where the reference (RabbitQCPlus) source tree is looked for: the
+    CARE_REFERENCE_DIR environment variable, else a directory named
+    `reference` beside this repository."""
+    return os.environ.get("CARE_REFERENCE_DIR") or os.path.join(os.path.dirname(REPO_DIR), "reference")
+
+
+def build_reference(ref_dir: str | None = None, jobs: int = 8) -> bool:
     """Compile the reference's own CARE sources into oracle/_ref (only where the
     reference tree exists; returns False otherwise)."""
-    if not os.path.isdir(ref_dir):
+    ref_dir = ref_dir or reference_dir()
+    if not os.path.isdir(os.path.join(ref_dir, "src")):
         return False
     cmd = ["make", "-f", os.path.join("oracle", "ref.mk"), f"REF={ref_dir}", f"-j{jobs}"]
     r = subprocess.run(cmd, cwd=REPO_DIR, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)

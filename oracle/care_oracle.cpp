@@ -123,7 +123,8 @@ struct Tables {
     std::vector<std::vector<uint32_t>> begin;
     std::vector<std::vector<uint32_t>> count;
     std::vector<std::vector<uint32_t>> values;
-    std::vector<uint64_t> sigs;  // n * nmaps (read-major)
+    // signatures are not kept: a query recomputes its anchor's, as the
+    // reference's query does (include/ordinaryminhasher.hpp:155-169)
 };
 
 // reference: include/forest.hpp:21-67 (node layout, preorder file format)
@@ -160,11 +161,12 @@ struct Oracle {
 // reference: include/cpusequencehasher.hpp:86-125 (hashInto) with the canonical
 // k-mer walk of include/sequencehelpers.hpp:842-930: for each hash function h,
 // the minimum over canonical k-mers of murmur64(kmer + h), masked to 2k bits.
-// Reads shorter than k keep the all-ones value (masked).
-void signature(const uint32_t* enc, int len, int k, int nmaps, uint64_t* out) {
+// Reads shorter than k keep the all-ones value (masked).  Maps [h0, h1) only;
+// out[h - h0].
+void signatureMaps(const uint32_t* enc, int len, int k, int h0, int h1, uint64_t* out) {
     const uint64_t kmask = k == 32 ? ~0ull : ((1ull << (2 * k)) - 1);
     uint64_t mins[CG_MAX_HASHMAPS];
-    for (int h = 0; h < nmaps; h++) mins[h] = ~0ull;
+    for (int h = h0; h < h1; h++) mins[h - h0] = ~0ull;
     if (len >= k) {
         uint64_t fwd = 0, rc = 0;
         for (int i = 0; i < len; i++) {
@@ -173,11 +175,16 @@ void signature(const uint32_t* enc, int len, int k, int nmaps, uint64_t* out) {
             rc = (rc >> 2) | ((3ull - b) << (2 * (k - 1)));
             if (i >= k - 1) {
                 const uint64_t canon = std::min(fwd, rc);
-                for (int h = 0; h < nmaps; h++) mins[h] = std::min(mins[h], murmur64(canon + uint64_t(h)));
+                for (int h = h0; h < h1; h++)
+                    mins[h - h0] = std::min(mins[h - h0], murmur64(canon + uint64_t(h)));
             }
         }
     }
-    for (int h = 0; h < nmaps; h++) out[h] = mins[h] & kmask;
+    for (int h = h0; h < h1; h++) out[h - h0] = mins[h - h0] & kmask;
+}
+
+void signature(const uint32_t* enc, int len, int k, int nmaps, uint64_t* out) {
+    signatureMaps(enc, len, k, 0, nmaps, out);
 }
 
 // reference: include/chunkedreadstorageconstruction.hpp:67-92 (preprocessSequence),
@@ -218,6 +225,29 @@ void buildStore(Oracle& O, const char* seqs, const uint64_t* offs, const char* q
         encode2bit(&s.enc[i * s.pitch], tmp.data(), L);
         if (s.hasQual) std::memcpy(&s.qual[i * size_t(s.Lmax)], quals + offs[i], L);
     }
+    // reference: include/qualityscorecompression.hpp:25-140 (QualityCompressorConfig<1|2>,
+    // encodeQualityString: the first bin whose boundary is >= Q, Q = int(char) - 33;
+    // decodeQualityToString: the bin's score) as include/chunkedreadstorage.hpp:532-607
+    // decodes a whole Lmax row, so positions past a read's end (zero bits in
+    // the reference's row) decode to the first bin's score.
+    const int bits = O.o.quality_score_bits == 0 ? 8 : O.o.quality_score_bits;
+    if (s.hasQual && (bits == 1 || bits == 2)) {
+        static const int bound1[2] = {13, 256}, bound2[4] = {4, 13, 20, 256};
+        static const char score1[2] = {'(', '5'}, score2[4] = {'$', '(', '1', '9'};
+        const int* bound = bits == 1 ? bound1 : bound2;
+        const char* score = bits == 1 ? score1 : score2;
+        for (uint64_t i = 0; i < n; i++) {
+            char* row = &s.qual[i * size_t(s.Lmax)];
+            for (int p = 0; p < s.Lmax; p++) {
+                int bin = 0;
+                if (p < s.len[i]) {
+                    const int Q = int(int8_t(row[p])) - 33;
+                    while (Q > bound[bin]) bin++;
+                }
+                row[p] = score[bin];
+            }
+        }
+    }
 }
 
 // reference: src/cpuminhasherconstruction.cpp:27-165 with
@@ -240,32 +270,47 @@ void buildTables(Oracle& O, int threads) {
         r = std::max(10, r);
         t.maxValuesPerKey = r;
     }
-    t.sigs.resize(s.n * t.nmaps);
-#pragma omp parallel for num_threads(threads) schedule(dynamic, 1024)
-    for (int64_t i = 0; i < int64_t(s.n); i++) {
-        signature(&s.enc[i * s.pitch], s.len[i], t.k, t.nmaps, &t.sigs[i * t.nmaps]);
-    }
     t.keys.assign(t.nmaps, {});
     t.begin.assign(t.nmaps, {});
     t.count.assign(t.nmaps, {});
     t.values.assign(t.nmaps, {});
+    // maps in waves of up to 8: the (key, read id) pairs of a wave's maps are
+    // the only per-read data held (16 bytes per read and map)
+    const int wave = std::max(1, std::min(8, t.nmaps));
+    const uint32_t upper = uint32_t(std::min(t.maxValuesPerKey, 65535));
+    for (int h0 = 0; h0 < t.nmaps; h0 += wave) {
+        const int h1 = std::min(t.nmaps, h0 + wave);
+        const int w = h1 - h0;
+        std::vector<std::vector<std::pair<uint64_t, uint32_t>>> kv(w);
+        for (auto& v : kv) v.resize(s.n);
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1024)
+        for (int64_t i = 0; i < int64_t(s.n); i++) {
+            uint64_t sig[CG_MAX_HASHMAPS];
+            signatureMaps(&s.enc[i * s.pitch], s.len[i], t.k, h0, h1, sig);
+            for (int j = 0; j < w; j++) kv[j][i] = {sig[j], uint32_t(i)};
+        }
 #pragma omp parallel for num_threads(threads) schedule(dynamic, 1)
-    for (int h = 0; h < t.nmaps; h++) {
-        std::vector<std::pair<uint64_t, uint32_t>> kv(s.n);
-        for (uint64_t i = 0; i < s.n; i++) kv[i] = {t.sigs[i * t.nmaps + h], uint32_t(i)};
-        std::sort(kv.begin(), kv.end());
-        const uint32_t upper = uint32_t(std::min(t.maxValuesPerKey, 65535));
-        for (uint64_t a = 0; a < kv.size();) {
-            uint64_t b = a;
-            while (b < kv.size() && kv[b].first == kv[a].first) b++;
-            const uint64_t num = b - a;
-            if (num >= 2 && num <= upper) {
-                t.keys[h].push_back(kv[a].first);
-                t.begin[h].push_back(uint32_t(t.values[h].size()));
-                t.count[h].push_back(uint32_t(num));
-                for (uint64_t j = a; j < b; j++) t.values[h].push_back(kv[j].second);
+        for (int j = 0; j < w; j++) {
+            const int h = h0 + j;
+            auto& v = kv[j];
+            std::sort(v.begin(), v.end());
+            for (uint64_t a = 0; a < v.size();) {
+                uint64_t b = a;
+                while (b < v.size() && v[b].first == v[a].first) b++;
+                const uint64_t num = b - a;
+                if (num >= 2 && num <= upper) {
+                    t.keys[h].push_back(v[a].first);
+                    t.begin[h].push_back(uint32_t(t.values[h].size()));
+                    t.count[h].push_back(uint32_t(num));
+                    for (uint64_t q = a; q < b; q++) t.values[h].push_back(v[q].second);
+                }
+                a = b;
             }
-            a = b;
+            std::vector<std::pair<uint64_t, uint32_t>>().swap(v);
+            t.keys[h].shrink_to_fit();
+            t.begin[h].shrink_to_fit();
+            t.count[h].shrink_to_fit();
+            t.values[h].shrink_to_fit();
         }
     }
 }
@@ -600,7 +645,8 @@ void candidates(const Oracle& O, uint64_t anchor, std::vector<uint32_t>& out, ui
     out.clear();
     if (O.o.exclude_ambiguous_reads && s.ambig[anchor]) return;
     if (s.len[anchor] >= t.k) {
-        const uint64_t* sig = &t.sigs[anchor * t.nmaps];
+        uint64_t sig[CG_MAX_HASHMAPS];
+        signature(&s.enc[anchor * s.pitch], s.len[anchor], t.k, t.nmaps, sig);
         for (int h = 0; h < t.nmaps; h++) {
             const auto& ks = t.keys[h];
             auto it = std::lower_bound(ks.begin(), ks.end(), sig[h]);
@@ -964,7 +1010,8 @@ int orc_info(void* h, uint64_t* nreads, int* lmax, int* k, int* nmaps, double* b
 int orc_signatures(void* h, uint64_t first, uint64_t n, uint64_t* out) {
     const Oracle* O = static_cast<Oracle*>(h);
     if (first + n > O->s.n) return CG_ERR_INVALID_ARGUMENT;
-    std::memcpy(out, &O->t.sigs[first * O->t.nmaps], n * O->t.nmaps * sizeof(uint64_t));
+    for (uint64_t i = first; i < first + n; i++)
+        signature(&O->s.enc[i * O->s.pitch], O->s.len[i], O->t.k, O->t.nmaps, out + (i - first) * O->t.nmaps);
     return 0;
 }
 
@@ -993,6 +1040,10 @@ int orc_correct(void* h, uint64_t first, uint64_t count, uint8_t* flags, char* o
     Counters total;
     std::vector<CandRec> allRecs;
     const int64_t units = int64_t(pe ? count / 2 : count);
+    // reference: include/options.hpp:126-133 (getNumReadsToProcess) with
+    // src/correct_cpu.cpp:97-102: only anchors below fixedNumberOfReads run
+    const uint64_t limit = O->o.fixed_number_of_reads ? std::min<uint64_t>(O->o.fixed_number_of_reads, O->s.n)
+                                                      : O->s.n;
 #pragma omp parallel num_threads(threads)
     {
         Counters cnt;
@@ -1004,12 +1055,20 @@ int orc_correct(void* h, uint64_t first, uint64_t count, uint8_t* flags, char* o
         for (int64_t u = 0; u < units; u++) {
             if (!pe) {
                 const uint64_t a = first + uint64_t(u);
+                if (a >= limit) {
+                    flags[a - first] = 0;
+                    continue;
+                }
                 candidates(*O, a, c1, &cnt.raw);
                 const uint8_t f = correctOne(*O, a, c1, none, corr, cnt, recs);
                 flags[a - first] = f;
                 if (f & CG_RESULT_CORRECTED) std::memcpy(out + (a - first) * pitch, corr.data(), corr.size());
             } else {
                 const uint64_t a = first + 2 * uint64_t(u);
+                if (a >= limit) {
+                    flags[a - first] = flags[a + 1 - first] = 0;
+                    continue;
+                }
                 candidates(*O, a, c1, &cnt.raw);
                 candidates(*O, a + 1, c2, &cnt.raw);
                 pairFlags(c1, c2, f1, f2);

@@ -2,13 +2,16 @@
 # where they lie (never copied into this repository) plus this directory's
 # drivers, writing every output under oracle/_ref/.  Usage:
 #     make -f oracle/ref.mk REF=/path/to/RabbitQCPlus -j8
+# (REF has no default: oracle.build_reference passes it.)
 # The reference's own Makefile is not used: these are the few translation
 # units that care::performCorrection needs, built with the reference's own
 # language/optimisation flags (ISO C++17, so floating-point contraction is off,
 # -O3, OpenMP, thrust on its OpenMP backend).  No -march=native: the SIMD block
 # guarded by Vec512 in src/cpu_alignment.cpp is unused by the selected path.
 
-REF ?= /root/reference
+ifndef REF
+$(error REF (the reference source tree) is not set)
+endif
 OUT := oracle/_ref
 OBJ := $(OUT)/obj
 CXX ?= g++
@@ -50,3 +53,25 @@ $(OUT)/ref_stages: $(filter-out $(OBJ)/dispatch_care_correct_cpu.o,$(REF_OBJS)) 
 	$(CXX) $^ -o $@ $(LIBS)
 
 .PHONY: all
+
+# The drop-in check: RabbitQCPlus's own caller (main_correction,
+# src/main_correct_cpu.cpp) and CARE objects, with dispatch_care_correct_cpu.o
+# replaced by the GB300 shim, linked against libcaregpu.so; the driver is
+# tests/shim_consumer.cpp.  Needs rabbitqcplus_gb300/lib/libcaregpu.so built.
+SHIM := rabbitqcplus_gb300/csrc/host/dispatch_care_correct_gpu.cpp
+GPULIB := rabbitqcplus_gb300/lib
+
+$(OBJ)/dispatch_care_correct_gpu.o: $(SHIM) rabbitqcplus_gb300/csrc/host/care_host.h include/care_gpu.h
+	@mkdir -p $(OBJ)
+	$(CXX) -c $< -o $@ $(CXXFLAGS) -Iinclude -Irabbitqcplus_gb300/csrc/host
+
+$(OBJ)/shim_consumer.o: tests/shim_consumer.cpp rabbitqcplus_gb300/csrc/host/care_host.h
+	@mkdir -p $(OBJ)
+	$(CXX) -c $< -o $@ $(CXXFLAGS) -I$(REF)/src -Iinclude -Irabbitqcplus_gb300/csrc/host
+
+$(OUT)/care_gpu_dropin: $(filter-out $(OBJ)/dispatch_care_correct_cpu.o,$(REF_OBJS)) $(OBJ)/main_correct_cpu.o \
+                        $(OBJ)/dispatch_care_correct_gpu.o $(OBJ)/shim_consumer.o $(GPULIB)/libcaregpu.so
+	$(CXX) $(filter %.o,$^) -o $@ $(LIBS) -L$(GPULIB) -lcaregpu -Wl,-rpath,$(abspath $(GPULIB))
+
+.PHONY: dropin
+dropin: $(OUT)/care_gpu_dropin

@@ -26,7 +26,8 @@ static void usage() {
     std::fprintf(stderr,
                  "ref_driver -i in1 [-i in2] -o out1 [-o out2] -d outdir -c cov "
                  "[-k 20] [-h 48] [-t threads] [--pe] [-q] [--candidates] "
-                 "[--exclude-ambiguous] [--forest file] [--print] [--labels] [--new-columns n] [--tempdir dir]\n");
+                 "[--exclude-ambiguous] [--forest file] [--print] [--labels] [--new-columns n] [--tempdir dir] "
+                 "[--quality-bits 1|2|8] [--fixed-reads n]\n");
 }
 
 int main(int argc, char** argv) {
@@ -72,6 +73,8 @@ int main(int argc, char** argv) {
         else if (a == "--labels") o.outputCorrectionQualityLabels = true;
         else if (a == "--new-columns") o.new_columns_to_correct = std::stoi(next());
         else if (a == "--tempdir") o.tempdirectory = next();
+        else if (a == "--quality-bits") o.qualityScoreBits = std::stoi(next());
+        else if (a == "--fixed-reads") o.fixedNumberOfReads = std::stoull(next());
         else { usage(); return 2; }
     }
     if (o.inputfiles.empty() || o.outputfilenames.size() != o.inputfiles.size() ||

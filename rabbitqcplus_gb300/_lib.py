@@ -143,6 +143,8 @@ def sim() -> ctypes.CDLL:
         lib.cgsim_write_fastq.restype = ctypes.c_int
         lib.cgsim_write_fastq.argtypes = [P, ctypes.c_char_p, ctypes.c_char_p]
         lib.cgsim_score.argtypes = [P, ctypes.c_char_p] + [ctypes.POINTER(ctypes.c_uint64)] * 4
+        lib.cgsim_score_results.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, P, P, ctypes.c_uint64] + \
+            [ctypes.POINTER(ctypes.c_uint64)] * 4
         lib._typed = True
     return lib
 

@@ -14,6 +14,8 @@ import numpy as np
 from . import _lib
 
 CG_OK = 0
+CG_ERR_INVALID_ARGUMENT, CG_ERR_UNSUPPORTED, CG_ERR_CUDA, CG_ERR_OUT_OF_MEMORY = 1, 2, 3, 4
+CG_ERR_STATE, CG_ERR_IO, CG_ERR_TIMEOUT = 5, 6, 7
 CG_ERRORS = {1: "invalid argument", 2: "unsupported", 3: "CUDA error", 4: "out of memory", 5: "bad state",
              6: "I/O error", 7: "timeout"}
 CG_MAX_HASHMAPS = 48
@@ -49,7 +51,10 @@ class CareOptions(ctypes.Structure):
         ("msa_warps", ctypes.c_int32),
         ("streams", ctypes.c_int32),
         ("host_file_io", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 3),
+        ("quality_score_bits", ctypes.c_int32),
+        ("fixed_number_of_reads", ctypes.c_uint32),
+        ("reserved0", ctypes.c_int32),
+        ("hashtable_memory_bytes", ctypes.c_uint64),
     ]
 
     @classmethod
@@ -72,6 +77,7 @@ class CareOptions(ctypes.Structure):
         o.pair_mode = CG_PAIR_SE
         o.correction_type = CG_CORR_CLASSIC
         o.threshold_anchor = 0.5
+        o.quality_score_bits = 8
         o.device = 0
         o.batch_anchors = 0
         for k, v in kw.items():
@@ -91,7 +97,7 @@ class CgStats(ctypes.Structure):
         ("msa_warps", ctypes.c_int32), ("streams", ctypes.c_int32), ("seconds_tune", ctypes.c_double),
         ("graph_replays", ctypes.c_uint64), ("learned_columns", ctypes.c_uint64),
         ("learned_corrections", ctypes.c_uint64), ("learned_overflow", ctypes.c_uint64),
-        ("candidate_corrections", ctypes.c_uint64)]
+        ("candidate_corrections", ctypes.c_uint64), ("classifier_timeouts", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
@@ -103,7 +109,7 @@ EXPORTED = ["cg_default_options", "cg_create", "cg_destroy", "cg_last_error", "c
             "cg_get_candidates", "cg_correct_files", "cg_load_forest", "cg_get_candidates_noalloc",
             "cg_classifier_size", "cg_load_classifier", "cg_get_columns", "cg_default_train_options",
             "cg_train_classifier", "cg_classifier_gradients", "cg_classifier_logits", "cg_release_cached_memory",
-            "cg_combine_results"]
+            "cg_combine_results", "cg_set_classifier_wait_limit", "cg_set_allocation_fault"]
 CLASSIFIER_FEATURES = 32
 CLASSIFIER_PARAMS = 6337  # w1 64x32, w2 64x64, w3 64, b1 64, b2 64, b3
 
@@ -165,6 +171,8 @@ def gpu_lib() -> ctypes.CDLL:
                                               ctypes.POINTER(ctypes.c_float)]
         L.cg_classifier_logits.argtypes = [ctypes.c_int, P, ctypes.c_size_t, P, ctypes.c_uint64, P]
         L.cg_release_cached_memory.argtypes = [ctypes.c_int]
+        L.cg_set_classifier_wait_limit.argtypes = [ctypes.c_int, ctypes.c_int64]
+        L.cg_set_allocation_fault.argtypes = [ctypes.c_int64]
         for f in EXPORTED:
             if f not in ("cg_destroy", "cg_default_options", "cg_last_error", "cg_classifier_size",
                          "cg_default_train_options"):
@@ -175,6 +183,24 @@ def gpu_lib() -> ctypes.CDLL:
 
 class CareError(RuntimeError):
     pass
+
+
+def set_allocation_fault(after: int) -> None:
+    """Every device-memory request after the next `after` fails as out of memory (< 0: off)."""
+    gpu_lib().cg_set_allocation_fault(after)
+
+
+def release_cached_memory(device: int = -1) -> None:
+    rc = gpu_lib().cg_release_cached_memory(device)
+    if rc != CG_OK:
+        raise CareError(f"cg_release_cached_memory: {CG_ERRORS.get(rc, rc)}")
+
+
+def set_classifier_wait_limit(polls: int, device: int = 0) -> None:
+    """Polls of the classifier's per-tile MMA waits on `device` (< 0: the default)."""
+    rc = gpu_lib().cg_set_classifier_wait_limit(device, polls)
+    if rc != CG_OK:
+        raise CareError(f"cg_set_classifier_wait_limit: {CG_ERRORS.get(rc, rc)}")
 
 
 class CareGpu:

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -36,11 +37,29 @@ namespace {
 // without cudaMalloc and frees without cudaFree.  A block is cached only after
 // the device has finished every queued kernel (the release synchronises, as
 // cudaFree would), and the cache is emptied before an allocation fails.
+// Simulated device out-of-memory (cg_set_allocation_fault): requests left
+// before every request fails; < 0 = off.
+std::atomic<long long> g_allocFault{-1};
+
+bool simulated_out_of_memory() {
+    long long v = g_allocFault.load();
+    while (v >= 0) {
+        if (v == 0) return true;
+        if (g_allocFault.compare_exchange_weak(v, v - 1)) return false;
+    }
+    return false;
+}
+
 class BlockCache {
 public:
     cudaError_t alloc(void** p, size_t n, size_t* got) {
         int dev = 0;
         cudaGetDevice(&dev);
+        if (simulated_out_of_memory()) {
+            // as a real failure: the cache is emptied before the request fails
+            trim(dev);
+            return cudaErrorMemoryAllocation;
+        }
         {
             std::lock_guard<std::mutex> lock(mu_);
             // the smallest cached block of this device that holds n bytes, if
@@ -199,6 +218,10 @@ struct Plan {
 
 constexpr int kMaxSets = 2;
 
+// Drops the cached device address of the no-allocation lookup's scratch array
+// for `device` (every device if < 0); defined with that entry point below.
+void forget_noalloc_scratch(int device);
+
 }  // namespace
 
 struct cg_ctx {
@@ -254,6 +277,7 @@ struct cg_ctx {
     bool haveMlp = false;
     bool collecting = false;  // cg_get_columns: record the columns, do not score them
     float minLogit = 0.0f;    // logit of threshold_anchor
+    unsigned long long timeoutsSeen = 0;  // classifier blocks whose MMA wait ran out, already reported
 
     // forest classifier (CG_CORR_FOREST)
     DevBuf forestNodes, treeOffsets;
@@ -457,6 +481,11 @@ int build_store(cg_ctx* c) {
     }
     c->chunks.clear();
     StoreArg st = store_arg(c);
+    const int qbits = c->o.quality_score_bits == 0 ? 8 : c->o.quality_score_bits;
+    if (q && qbits != 8) {
+        CG_CUDA(c, launch_quality_bins(c->qual.as<uint8_t>(), c->len.as<uint16_t>(), n, c->lmax, qbits, c->stream));
+        c->stats.kernel_launches += 1;
+    }
     CG_CUDA(c, launch_hilo(st, c->hilo.as<uint32_t>(), c->stream));
     // shortest and longest read (read back once the build has finished)
     CG_CUDA(c, c->lenRange.ensure(2 * sizeof(unsigned int)));
@@ -998,6 +1027,25 @@ int join_sets(cg_ctx* c, int S, cudaStream_t to) {
     return CG_OK;
 }
 
+// A learned-decision call whose classifier blocks gave up waiting for their
+// MMAs (counters[kCounterTimeouts] grew) left those blocks' columns to the
+// fallback decision: the call reports CG_ERR_TIMEOUT instead of CG_OK.
+int check_classifier_timeouts(cg_ctx* c) {
+    if (c->params.correctionType != CG_CORR_LEARNED || c->collecting) return CG_OK;
+    unsigned long long n = 0;
+    CG_CUDA(c, cudaMemcpy(&n, c->counters.as<unsigned long long>() + kCounterTimeouts, sizeof(n),
+                          cudaMemcpyDeviceToHost));
+    if (n > c->timeoutsSeen) {
+        const unsigned long long grew = n - c->timeoutsSeen;
+        c->timeoutsSeen = n;
+        return fail(c, CG_ERR_TIMEOUT,
+                    "%llu classifier block(s) timed out waiting for the tensor cores; their columns kept the "
+                    "fallback decision",
+                    grew);
+    }
+    return CG_OK;
+}
+
 // ---- autotuner
 //
 // The batch size, the persistent grids and the number of pipelines change
@@ -1210,7 +1258,7 @@ int correct_batched(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* out_flags,
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     c->stats.seconds_correct = ms / 1000.0;
     c->stats.num_anchors_processed += num;
-    return CG_OK;
+    return check_classifier_timeouts(c);
 }
 
 }  // namespace
@@ -1233,6 +1281,7 @@ void cg_default_options(cg_options* o) {
     o->pair_mode = CG_PAIR_SE;
     o->correction_type = CG_CORR_CLASSIC;
     o->threshold_anchor = 0.5f;
+    o->quality_score_bits = 8;
 }
 
 int cg_create(const cg_options* o, cg_ctx** out) {
@@ -1249,6 +1298,10 @@ int cg_create(const cg_options* o, cg_ctx** out) {
     if (o->correction_type == CG_CORR_LEARNED && !(o->threshold_anchor > 0.0f && o->threshold_anchor < 1.0f))
         return CG_ERR_INVALID_ARGUMENT;
     if (o->driver != CG_DRIVER_PLAIN && o->driver != CG_DRIVER_BATCHED) return CG_ERR_INVALID_ARGUMENT;
+    if (o->quality_score_bits != 0 && o->quality_score_bits != 1 && o->quality_score_bits != 2 &&
+        o->quality_score_bits != 8)
+        return CG_ERR_UNSUPPORTED;  // the reference's QualityCompressorWrapper knows 1, 2 and 8
+    if (o->pair_mode == CG_PAIR_PE && (o->fixed_number_of_reads & 1u)) return CG_ERR_INVALID_ARGUMENT;
     if (o->batch_anchors < 0 || o->align_blocks < 0 || o->msa_warps < 0 || o->msa_warps > 8 || o->streams < 0 ||
         o->streams > kMaxSets)
         return CG_ERR_INVALID_ARGUMENT;
@@ -1259,7 +1312,8 @@ int cg_create(const cg_options* o, cg_ctx** out) {
         c->minLogit = (float)std::log((double)o->threshold_anchor / (1.0 - (double)o->threshold_anchor));
     c->device = o->device;
     auto bail = [&](cudaError_t e) {
-        delete c;
+        cudaGetLastError();
+        cg_destroy(c);  // streams, events and blocks made so far
         return e == cudaErrorMemoryAllocation ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA;
     };
     cudaError_t e = cudaSetDevice(c->device);
@@ -1280,7 +1334,26 @@ int cg_create(const cg_options* o, cg_ctx** out) {
 
 int cg_release_cached_memory(int device) {
     block_cache().trim(device);
+    forget_noalloc_scratch(device);
     return cudaGetLastError() == cudaSuccess ? CG_OK : CG_ERR_CUDA;
+}
+
+int cg_set_allocation_fault(int64_t after) {
+    g_allocFault.store(after < 0 ? -1 : (long long)after);
+    return CG_OK;
+}
+
+int cg_set_classifier_wait_limit(int device, int64_t polls) {
+    int cur = 0;
+    if (cudaGetDevice(&cur) != cudaSuccess) return CG_ERR_CUDA;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return CG_ERR_INVALID_ARGUMENT;
+    }
+    const uint32_t p = polls < 0 ? (1u << 20) : (uint32_t)std::min<int64_t>(polls, 0xffffffffll);
+    const cudaError_t e = set_classifier_wait_limit(p);
+    cudaSetDevice(cur);
+    return e == cudaSuccess ? CG_OK : CG_ERR_CUDA;
 }
 
 void cg_destroy(cg_ctx* c) {
@@ -1361,6 +1434,18 @@ int cg_build_tables(cg_ctx* c) {
     if (c->appended == 0) return fail(c, CG_ERR_STATE, "no reads appended");
     if (c->o.pair_mode == CG_PAIR_PE && (c->appended & 1))
         return fail(c, CG_ERR_INVALID_ARGUMENT, "paired mode needs an even number of reads");
+    if (c->o.hashtable_memory_bytes) {
+        // reference: include/ordinaryminhasher.hpp:350-372 -- maps of the first
+        // construction round: limit / ((sizeof key + sizeof read id) x reads) - 2
+        const long long fit = (long long)(c->o.hashtable_memory_bytes / (12ull * c->appended)) - 2;
+        if (fit < c->o.num_hash_functions)
+            return fail(c, CG_ERR_UNSUPPORTED,
+                        "memoryForHashtables %llu bytes holds %lld maps of %llu reads in the reference's first "
+                        "construction round, fewer than the %d requested; the reference's final map count would "
+                        "depend on its host tables' sizes",
+                        (unsigned long long)c->o.hashtable_memory_bytes, fit, (unsigned long long)c->appended,
+                        c->o.num_hash_functions);
+    }
     CG_CUDA(c, cudaSetDevice(c->device));
     CG_CUDA(c, cudaEventRecord(c->ev0, c->stream));
     int rc = build_store(c);
@@ -1414,6 +1499,24 @@ int cg_correct(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* out_flags, char
     if (c->o.correction_type == CG_CORR_LEARNED && c->lmax > 256)
         return fail(c, CG_ERR_UNSUPPORTED, "learned correction supports reads up to 256 bp (longest is %d)", c->lmax);
     CG_CUDA(c, cudaSetDevice(c->device));
+    {
+        // fixedNumberOfReads: anchors past the limit are not corrected
+        const uint64_t limit =
+            c->o.fixed_number_of_reads ? std::min<uint64_t>(c->o.fixed_number_of_reads, c->n) : c->n;
+        const uint64_t run = first >= limit ? 0 : std::min(num, limit - first);
+        if (run < num) {
+            if (c->outKind == cudaMemcpyDeviceToDevice)
+                CG_CUDA(c, cudaMemsetAsync(out_flags + run, 0, num - run, c->stream));
+            else
+                std::memset(out_flags + run, 0, num - run);
+        }
+        if (run == 0) {
+            CG_CUDA(c, cudaStreamSynchronize(c->stream));
+            c->stats.seconds_correct = 0.0;
+            return CG_OK;
+        }
+        num = run;
+    }
     if (c->params.candidates) {
         const int rc = mark_pass(c, first, num);
         if (rc != CG_OK) return rc;
@@ -1433,7 +1536,7 @@ int cg_correct(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* out_flags, char
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     c->stats.seconds_correct = ms / 1000.0;
     c->stats.num_anchors_processed += num;
-    return CG_OK;
+    return check_classifier_timeouts(c);
 }
 
 int cg_combine_results(cg_ctx* c, uint64_t first, uint64_t num, uint8_t* flags, uint64_t* num_candidate_records) {
@@ -1473,6 +1576,7 @@ int cg_get_stats(const cg_ctx* c, cg_stats* out) {
     s.learned_corrections = cnt[kCounterLearnedTaken];
     s.learned_overflow = cnt[kCounterColumnOverflow];
     s.candidate_corrections = cnt[kCounterCandidateVotes];
+    s.classifier_timeouts = cnt[kCounterTimeouts];
     *out = s;
     return CG_OK;
 }
@@ -1696,6 +1800,9 @@ constexpr size_t kNoallocNcand = 576;      // uint32_t
 constexpr size_t kNoallocCounters = 640;   // unsigned long long[kNumCounters]
 constexpr size_t kNoallocCand = 1024;      // uint32_t[kNoallocMaxRaw]
 constexpr size_t kNoallocBytes = kNoallocCand + sizeof(uint32_t) * kNoallocMaxRaw;
+static_assert(kNoallocQrange + sizeof(uint2) * CG_MAX_HASHMAPS <= kNoallocRaw, "scratch layout: bucket ranges");
+static_assert(kNoallocRaw + 4 * sizeof(uint32_t) <= kNoallocNcand, "scratch layout: raw counts");
+static_assert(kNoallocNcand + sizeof(uint32_t) <= kNoallocCounters, "scratch layout: unique count");
 static_assert(kNoallocCounters + sizeof(unsigned long long) * kNumCounters <= kNoallocCand, "scratch layout");
 
 static __device__ __align__(256) unsigned char g_noallocScratch[kNoallocBytes];
@@ -1704,7 +1811,14 @@ constexpr int kNoallocMaxDevices = 64;
 std::mutex g_noallocMutex;
 unsigned char* g_noallocPtr[kNoallocMaxDevices] = {nullptr};
 
-// Device address of the scratch array on the current device (set up once per device).
+void forget_noalloc_scratch(int device) {
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    for (int d = 0; d < kNoallocMaxDevices; d++)
+        if (device < 0 || d == device) g_noallocPtr[d] = nullptr;
+}
+
+// Device address of the scratch array on the current device (set up once per
+// device; cg_release_cached_memory forgets it, as a device reset moves it).
 int noalloc_scratch(cg_ctx* c, unsigned char** out) {
     int dev = 0;
     CG_CUDA(c, cudaGetDevice(&dev));

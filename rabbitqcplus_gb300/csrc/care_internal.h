@@ -137,6 +137,9 @@ cudaError_t launch_hilo(StoreArg st, uint32_t* hilo, cudaStream_t s);
 cudaError_t launch_signatures(StoreArg st, int k, int nmaps, unsigned long long* sig, cudaStream_t s);
 // out[0] = shortest, out[1] = longest read of the store (out preset to {~0, 0})
 cudaError_t launch_len_range(const uint16_t* len, uint64_t n, unsigned int* out, cudaStream_t s);
+// qualityScoreBits 1 or 2: bins the stored scores of reads [0, n) in place
+// (rows of lmax bytes) and fills each row past its read's end with the first bin
+cudaError_t launch_quality_bins(uint8_t* qual, const uint16_t* len, uint64_t n, int lmax, int bits, cudaStream_t s);
 
 // hash tables
 cudaError_t launch_table_init(Slot* t, uint64_t cap, cudaStream_t s);

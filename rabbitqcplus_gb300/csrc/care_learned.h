@@ -53,6 +53,10 @@ cudaError_t launch_mlp_infer(const unsigned char* model, const __nv_bfloat16* fe
                              const unsigned int* countPtr, unsigned int count, unsigned int cap, float minLogit,
                              char* out, int outPitch, float* logits, unsigned long long* counters, int blocks,
                              cudaStream_t s);
+// Polls of the inference kernel's per-tile MMA waits on the current device
+// (default 1 << 20); a block whose wait runs out counts in
+// counters[kCounterTimeouts] and leaves its columns to the fallback decision.
+cudaError_t set_classifier_wait_limit(uint32_t polls);
 // Partial gradients of the mean binary cross-entropy over `rows` rows of a
 // minibatch: rows perm[step * rows + r] of feat/label (perm may be null; step
 // = *stepPtr % stepsPerEpoch, or 0 without stepPtr).

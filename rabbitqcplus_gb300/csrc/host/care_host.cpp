@@ -42,7 +42,28 @@ cg_options toCgOptions(const ProgramOptions& o) {
     c.threshold_anchor = o.thresholdAnchor;
     c.device = o.deviceIds.empty() ? 0 : o.deviceIds[0];
     c.driver = o.gpuBatched ? CG_DRIVER_BATCHED : CG_DRIVER_PLAIN;
+    c.quality_score_bits = o.qualityScoreBits;
+    c.fixed_number_of_reads = (uint32_t)std::min<std::size_t>(o.fixedNumberOfReads, 0xffffffffu);
+    std::size_t mem = o.memoryForHashtables;
+    if (o.memoryTotalLimit && (!mem || o.memoryTotalLimit < mem)) mem = o.memoryTotalLimit;  // src/options.cpp:296
+    c.hashtable_memory_bytes = mem;
     return c;
+}
+
+void validateOptions(const ProgramOptions& o) {
+    if (o.correctionType == CorrectionType::Print || o.correctionTypeCands == CorrectionType::Print)
+        // the reference then writes classifier features instead of an output
+        // file (src/dispatch_care_correct_cpu.cpp:180)
+        throw std::runtime_error("correction type Print is not supported");
+    if (o.correctCandidates && o.correctionTypeCands != CorrectionType::Classic)
+        throw std::runtime_error("candidate correction supports correctionTypeCands Classic only");
+    if (o.qualityScoreBits != 1 && o.qualityScoreBits != 2 && o.qualityScoreBits != 8)
+        throw std::runtime_error("qualityScoreBits must be 1, 2 or 8");
+    if (o.fixedNumberOfReads > 0xffffffffull)
+        throw std::runtime_error("fixedNumberOfReads above 2^32-1");
+    if (!o.save_binary_reads_to.empty() || !o.load_binary_reads_from.empty() || !o.save_hashtables_to.empty() ||
+        !o.load_hashtables_from.empty())
+        throw std::runtime_error("saving or loading preprocessed reads or hash tables is not supported");
 }
 
 namespace {
@@ -95,9 +116,7 @@ struct Corrected {
 
 Corrected runCorrection(const ProgramOptions& o) {
     if (o.inputfiles.empty()) throw std::runtime_error("no input files");
-    if (o.correctionType == CorrectionType::Print) throw std::runtime_error("correction type Print is not supported");
-    if (o.correctCandidates && o.correctionTypeCands != CorrectionType::Classic)
-        throw std::runtime_error("candidate correction supports correctionTypeCands Classic only");
+    validateOptions(o);
     Corrected r;
     std::vector<uint64_t> groupStarts;  // one device append call per input group
     if (o.pairType == SequencePairType::PairedEnd && o.inputfiles.size() == 2) {
@@ -331,6 +350,7 @@ private:
 }  // namespace
 
 RunReport performCorrection(const ProgramOptions& o) {
+    validateOptions(o);
     if (!o.outputfilenames.empty() && !o.inputfiles.empty()) {
         cg::FastqRun dr;
         RangeWriter out(o, outputFormat(o));
@@ -371,6 +391,7 @@ RunReport performCorrection(const ProgramOptions& o) {
 
 RunReport performCorrectionToSink(const ProgramOptions& o, const std::function<void(int)>& onStart,
                                   const ChunkSink& sink) {
+    validateOptions(o);
     {
         cg::FastqRun dr;
         dr.queueChunkBytes = 1u << 20;  // the queue protocol's chunks (src/correctionresultoutput.cpp:733-745)
@@ -474,6 +495,9 @@ extern "C" int cg_correct_files(const cg_options* options, const char* const* in
     o.deviceIds = {options->device};
     o.gpuBatched = options->driver == CG_DRIVER_BATCHED;
     o.deviceFileIO = options->host_file_io == 0;
+    o.qualityScoreBits = options->quality_score_bits == 0 ? 8 : options->quality_score_bits;
+    o.fixedNumberOfReads = options->fixed_number_of_reads;
+    o.memoryForHashtables = options->hashtable_memory_bytes;
     o.outputCorrectionQualityLabels = quality_labels != 0;
     o.gzoutput = gz_output != 0;
     o.outputdirectory = output_directory;

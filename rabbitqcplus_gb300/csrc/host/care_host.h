@@ -14,6 +14,7 @@
 #define CARE_HOST_H
 
 #include <atomic>
+#include <cstddef>
 #include <cstdint>
 #include <functional>
 #include <string>
@@ -64,7 +65,26 @@ struct ProgramOptions {
     bool showProgress = false;
     int threads = 1;
     std::vector<int> deviceIds;
-    int qualityScoreBits = 8;
+    int qualityScoreBits = 8;             // 8, 2 or 1: lossy quality store (cg_options.quality_score_bits)
+    std::size_t fixedNumberOfReads = 0;   // only reads [0, n) are corrected as anchors (0 = all)
+    // Host memory limits of the reference's table construction: the smaller
+    // one goes to cg_options.hashtable_memory_bytes, where a limit that would
+    // make the reference build its maps in several rounds is refused
+    // (CG_ERR_UNSUPPORTED).  0 = no limit (the device holds the tables).
+    std::size_t memoryForHashtables = 0;
+    std::size_t memoryTotalLimit = 0;
+    bool mustUseAllHashfunctions = false;  // the reference aborts when fewer maps than requested were built
+    // candidate classifier (only with correctCandidates; Forest/Print are refused)
+    float thresholdCands = .5f;
+    uint32_t maxForestTreesCands = 0xffffffffu;
+    std::string mlForestfileCands = "";
+    // binary read-store / hash-table files of the reference's checkpointing
+    // (--save_preprocessedreads_to, --load_preprocessedreads_from,
+    // --save_hashtables_to, --load_hashtables_from): not supported, refused
+    std::string save_binary_reads_to = "";
+    std::string load_binary_reads_from = "";
+    std::string save_hashtables_to = "";
+    std::string load_hashtables_from = "";
     SequencePairType pairType = SequencePairType::SingleEnd;
     std::string outputdirectory = "";
     std::string tempdirectory = "";
@@ -73,6 +93,13 @@ struct ProgramOptions {
 };
 
 cg_options toCgOptions(const ProgramOptions& o);
+
+// Throws std::runtime_error for options this engine refuses rather than
+// silently computing something else: Print correction (either type), a Forest
+// candidate classifier with candidate correction, the checkpoint files, and a
+// quality bit count other than 1, 2 or 8.  The hash-table memory limit is
+// checked by cg_build_tables once the number of reads is known.
+void validateOptions(const ProgramOptions& o);
 
 // One output chunk: `data` (allocated with new char[]) holds whole FASTQ
 // records of output file `file`; ownership passes to the sink.

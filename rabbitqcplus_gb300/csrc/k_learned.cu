@@ -154,6 +154,12 @@ constexpr int kTcRows = 128;
 constexpr uint32_t kTmemCols = 128;
 constexpr uint32_t kWaitSpins = 1u << 20;  // mbarrier polls before a wait is declared failed
 
+// Polls of the per-tile MMA waits (the waits whose failure ends a block);
+// set from the host by set_classifier_wait_limit.  The wait that drains a
+// failed block's MMAs before its tensor memory is released always uses
+// kWaitSpins.
+__device__ uint32_t g_tileWaitSpins = kWaitSpins;
+
 // byte offset of element (row, k) of a K-major tile with kdim columns
 __device__ __forceinline__ uint32_t core_offset(int row, int k, int kdim) {
     return (uint32_t)((((row >> 3) * (kdim >> 3) + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1));
@@ -190,9 +196,9 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// bounded wait for the completion of mbarrier phase `parity`
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitSpins; i++) {
+// bounded wait (at most `polls` polls) for the completion of mbarrier phase `parity`
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint32_t polls) {
+    for (uint32_t i = 0; i < polls; i++) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -280,6 +286,7 @@ __global__ void __launch_bounds__(kTcRows) mlp_infer_kernel(const unsigned char*
     uint32_t phase = 0;
     unsigned int taken = 0;
     bool failed = false;
+    const uint32_t tilePolls = g_tileWaitSpins;
     for (unsigned int t0 = blockIdx.x * kTcRows; t0 < n; t0 += gridDim.x * kTcRows) {
         const unsigned int row = t0 + (unsigned int)tid;
         uint4 f[4];
@@ -303,7 +310,7 @@ __global__ void __launch_bounds__(kTcRows) mlp_infer_kernel(const unsigned char*
                        idesc, k > 0);
             tc_commit(mb);
         }
-        bool ok = mbar_wait(mb, phase);
+        bool ok = mbar_wait(mb, phase, tilePolls);
         phase ^= 1u;
         if (__syncthreads_or(!ok)) {
             failed = true;
@@ -339,7 +346,7 @@ __global__ void __launch_bounds__(kTcRows) mlp_infer_kernel(const unsigned char*
                        smem_desc(smem_u32(b2) + 256u * k, 128, 1024), idesc, k > 0);
             tc_commit(mb);
         }
-        ok = mbar_wait(mb, phase);
+        ok = mbar_wait(mb, phase, tilePolls);
         phase ^= 1u;
         if (__syncthreads_or(!ok)) {
             failed = true;
@@ -372,7 +379,7 @@ __global__ void __launch_bounds__(kTcRows) mlp_infer_kernel(const unsigned char*
     }
     if (failed) {
         if (tid == 0 && counters) atomicAdd(&counters[kCounterTimeouts], 1ull);
-        mbar_wait(mb, phase ^ 1u);  // the MMAs in flight, bounded again
+        mbar_wait(mb, phase ^ 1u, kWaitSpins);  // the MMAs in flight, bounded again at the full limit
     }
     __syncthreads();
     tc_fence_after();
@@ -652,6 +659,10 @@ cudaError_t launch_mlp_infer(const unsigned char* model, const __nv_bfloat16* fe
     mlp_infer_kernel<<<blocks, kTcRows, 0, s>>>(model, feat, meta, countPtr, count, cap, minLogit, out, outPitch,
                                                  logits, counters);
     return cudaGetLastError();
+}
+
+cudaError_t set_classifier_wait_limit(uint32_t polls) {
+    return cudaMemcpyToSymbol(g_tileWaitSpins, &polls, sizeof(polls));
 }
 
 cudaError_t launch_mlp_grad(const unsigned char* model, const __nv_bfloat16* feat, const float* label,

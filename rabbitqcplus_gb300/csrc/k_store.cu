@@ -294,6 +294,39 @@ __global__ void len_range_kernel(const uint16_t* __restrict__ len, uint64_t n, u
 }
 }  // namespace
 
+namespace {
+// Lossy quality store (qualityScoreBits 1 or 2): the binned score of every
+// base, and the first bin's score past the read's end, where the reference's
+// zero-filled encoded row decodes to bin 0 (include/qualityscorecompression.hpp:
+// 25-140; scores are read as signed chars, as the reference's `int(quality[p])`
+// on x86-64).  Four bytes per thread, rows of lmax bytes.
+__global__ void quality_bin_kernel(uint8_t* __restrict__ qual, const uint16_t* __restrict__ len, uint64_t n,
+                                   int lmax, int bits) {
+    const uint64_t total = n * (uint64_t)lmax;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = i / (uint64_t)lmax;
+        const int p = (int)(i - r * (uint64_t)lmax);
+        const int q = (int)(int8_t)qual[i] - 33;
+        uint8_t b;
+        if (bits == 1) {
+            b = (p >= len[r] || q <= 13) ? '(' : '5';
+        } else {
+            b = (p >= len[r] || q <= 4) ? '$' : q <= 13 ? '(' : q <= 20 ? '1' : '9';
+        }
+        qual[i] = b;
+    }
+}
+}  // namespace
+
+cudaError_t launch_quality_bins(uint8_t* qual, const uint16_t* len, uint64_t n, int lmax, int bits, cudaStream_t s) {
+    if (n == 0 || (bits != 1 && bits != 2)) return cudaSuccess;
+    const uint64_t total = n * (uint64_t)lmax;
+    const unsigned blocks = (unsigned)std::min<uint64_t>((total + 255) / 256, 152 * 16);
+    quality_bin_kernel<<<blocks, 256, 0, s>>>(qual, len, n, lmax, bits);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_len_range(const uint16_t* len, uint64_t n, unsigned int* out, cudaStream_t s) {
     len_range_kernel<<<(unsigned)std::min<uint64_t>((n + 255) / 256, 1216), 256, 0, s>>>(len, n, out);
     return cudaGetLastError();

@@ -377,4 +377,32 @@ void cgsim_score(void* h, const char* corrected, uint64_t* tp, uint64_t* fp, uin
     *tp = TP; *fp = FP; *fn = FN; *reads_scored = R;
 }
 
+// The same score for reads [first, first + count) straight from correction
+// results: read first + j is row j of `rows` (pitch bytes) when flags[j] has
+// bit 1 (corrected) and not bit 8 (rejected by the combine step), else its
+// input sequence.
+void cgsim_score_results(void* h, uint64_t first, uint64_t count, const uint8_t* flags, const char* rows,
+                         uint64_t pitch, uint64_t* tp, uint64_t* fp, uint64_t* fn, uint64_t* reads_scored) {
+    SimData* d = static_cast<SimData*>(h);
+    uint64_t TP = 0, FP = 0, FN = 0, R = 0;
+#pragma omp parallel for reduction(+ : TP, FP, FN, R) schedule(static, 4096)
+    for (int64_t j = 0; j < (int64_t)count; j++) {
+        const uint64_t i = first + (uint64_t)j;
+        if (d->has_indel[i]) continue;
+        R++;
+        const bool use = (flags[j] & 1u) && !(flags[j] & 8u);
+        const char* row = rows + (uint64_t)j * pitch;
+        for (uint64_t p = d->offsets[i]; p < d->offsets[i + 1]; p++) {
+            const char o = d->seq[p], t = d->truth[p], c = use ? row[p - d->offsets[i]] : o;
+            if (o != t) {
+                if (c == t) TP++;
+                else FN++;
+            } else if (c != t) {
+                FP++;
+            }
+        }
+    }
+    *tp = TP; *fp = FP; *fn = FN; *reads_scored = R;
+}
+
 }  // extern "C"

@@ -47,6 +47,8 @@ const char* cgsim_truth(void* h);
 const uint8_t* cgsim_indel_flags(void* h);
 int cgsim_write_fastq(void* h, const char* path1, const char* path2);
 void cgsim_score(void* h, const char* corrected, uint64_t* tp, uint64_t* fp, uint64_t* fn, uint64_t* reads_scored);
+void cgsim_score_results(void* h, uint64_t first, uint64_t count, const uint8_t* flags, const char* rows,
+                         uint64_t pitch, uint64_t* tp, uint64_t* fp, uint64_t* fn, uint64_t* reads_scored);
 
 #ifdef __cplusplus
 }

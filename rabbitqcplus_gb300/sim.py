@@ -183,6 +183,18 @@ class SimReads:
                               ctypes.byref(fp), ctypes.byref(fn), ctypes.byref(r))
         return {"tp": tp.value, "fp": fp.value, "fn": fn.value, "reads_scored": r.value}
 
+    def score_results(self, first: int, flags: np.ndarray, rows: np.ndarray) -> dict:
+        """score() of reads [first, first + len(flags)) from correction results:
+        rows[j] is read first + j's corrected sequence where flags[j] says it
+        was corrected (and not rejected by the combine step)."""
+        flags = np.ascontiguousarray(flags, dtype=np.uint8)
+        assert rows.ndim == 2 and rows.shape[0] >= len(flags) and rows.strides[1] == 1
+        tp, fp, fn, r = (ctypes.c_uint64() for _ in range(4))
+        self._lib.cgsim_score_results(self._h, first, len(flags), flags.ctypes.data, rows.ctypes.data,
+                                      rows.strides[0], ctypes.byref(tp), ctypes.byref(fp), ctypes.byref(fn),
+                                      ctypes.byref(r))
+        return {"tp": tp.value, "fp": fp.value, "fn": fn.value, "reads_scored": r.value}
+
     def read(self, i: int) -> str:
         return self.sequences[self.offsets[i]:self.offsets[i + 1]].tobytes().decode()
 

@@ -36,7 +36,9 @@ def options_for(entry: dict) -> capi.CareOptions:
         pair_mode=capi.CG_PAIR_PE if o.get("paired") else capi.CG_PAIR_SE,
         correction_type=capi.CG_CORR_FOREST if o.get("forest") else capi.CG_CORR_CLASSIC,
         correct_candidates=int(bool(o.get("candidates"))),
-        new_columns_to_correct=int(o.get("new_columns", 15)))
+        new_columns_to_correct=int(o.get("new_columns", 15)),
+        quality_score_bits=int(o.get("quality_bits", 8)),
+        fixed_number_of_reads=int(o.get("fixed_reads", 0)))
 
 
 def forest_bytes(entry: dict) -> bytes | None:

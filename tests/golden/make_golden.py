@@ -2,7 +2,9 @@
 
 Run from the repository root, in a container where the reference tree exists:
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref PATH_TO_RABBITQCPLUS]
+
+(default: $CARE_REFERENCE_DIR, else a `reference` directory beside this repository)
 
 For every case in CASES it
   1. generates the seeded synthetic reads (rabbitqcplus_gb300.sim),
@@ -107,6 +109,29 @@ CASES = {
                       {"coverage": 30, "k": 20, "exclude_ambiguous": True}, 0),
     "se_candidates_tail": (sim.SimConfig(seed=118, genome_length=40_000, num_reads=8_000, n_read_fraction=0.3),
                            {"coverage": 30, "k": 20, "exclude_ambiguous": True, "candidates": True}, 0),
+    # lossy quality store (--qualityScoreBits): binned scores; with reads of
+    # several lengths a reverse-complement candidate's reversed row starts
+    # with the first bin's score
+    "se_quality_bits2": (sim.SimConfig(seed=120, genome_length=50_000, num_reads=10_000, repeat_families=3,
+                                       repeat_copies=3, sub_rate_5p=0.004, sub_rate_3p=0.03),
+                         {"coverage": 30, "k": 20, "quality": True, "quality_bits": 2}, 0),
+    "se_varlen_quality_bits1": (sim.SimConfig(seed=121, genome_length=60_000, repeat_families=4, repeat_copies=4,
+                                              num_reads=12_000, read_len_min=60, read_len_max=240,
+                                              sub_rate_5p=0.004, sub_rate_3p=0.03),
+                                {"coverage": 30, "k": 20, "quality": True, "quality_bits": 1}, 0),
+    "pe_varlen_quality_bits2": (sim.SimConfig(seed=122, genome_length=50_000, num_reads=10_000, paired=True,
+                                              repeat_families=3, repeat_copies=3, read_len_min=100,
+                                              read_len_max=150),
+                                {"coverage": 25, "k": 20, "paired": True, "quality": True, "quality_bits": 2}, 0),
+    # --fixedNumberOfReads: only the first reads are corrected as anchors,
+    # every read is a candidate
+    "se_fixed_reads": (sim.SimConfig(seed=123, genome_length=50_000, num_reads=10_000, repeat_families=3,
+                                     repeat_copies=3, sub_rate_5p=0.002, sub_rate_3p=0.02),
+                       {"coverage": 30, "k": 20, "fixed_reads": 6_001}, 0),
+    "pe_fixed_reads_candidates": (sim.SimConfig(seed=124, genome_length=50_000, num_reads=10_000, paired=True,
+                                                repeat_families=3, repeat_copies=3),
+                                  {"coverage": 30, "k": 20, "paired": True, "candidates": True,
+                                   "fixed_reads": 4_000}, 0),
 }
 
 
@@ -149,6 +174,10 @@ def run_case(name: str, cfg: sim.SimConfig, opts: dict, stage_anchors: int, work
         cmd.append("--candidates")
     if "new_columns" in opts:
         cmd += ["--new-columns", str(opts["new_columns"])]
+    if "quality_bits" in opts:
+        cmd += ["--quality-bits", str(opts["quality_bits"])]
+    if "fixed_reads" in opts:
+        cmd += ["--fixed-reads", str(opts["fixed_reads"])]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"reference failed on {name}:\n{r.stdout[-3000:]}")
@@ -222,13 +251,13 @@ def run_case(name: str, cfg: sim.SimConfig, opts: dict, stage_anchors: int, work
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None)
     ap.add_argument("--threads", type=int, default=os.cpu_count() or 4)
     ap.add_argument("--only", nargs="*")
     args = ap.parse_args()
     import oracle
     if not oracle.build_reference(args.ref):
-        sys.exit(f"reference tree not found at {args.ref}")
+        sys.exit(f"reference tree not found at {args.ref or oracle.reference_dir()}")
     manifest_path = os.path.join(HERE, "manifest.json")
     manifest = json.load(open(manifest_path)) if os.path.exists(manifest_path) else {}
     with tempfile.TemporaryDirectory() as work:

@@ -130,3 +130,24 @@ def test_apply_corrections_only_touches_corrected_reads():
     corr = np.frombuffer(b"TTTTTTTTACGA", np.uint8).reshape(3, 4)
     out = capi.apply_corrections(seqs, offs, flags, corr)
     assert out.tobytes() == b"AAAATTTTACGA"
+
+
+def test_file_errors_are_reported_before_any_device_work(tmp_path):
+    """cg_correct_files opens its outputs and parses host-path inputs before it
+    touches the GPU: an output directory that cannot exist and a truncated
+    FASTQ record both return CG_ERR_IO (runs without a GPU)."""
+    r = sim.SimReads(sim.SimConfig(seed=74, genome_length=20_000, num_reads=2_000))
+    fq = str(tmp_path / "in.fq")
+    r.write_fastq(fq)
+    blocker = tmp_path / "file"
+    blocker.write_text("x")
+    o = capi.CareOptions.defaults(30.0)
+    with pytest.raises(capi.CareError, match="I/O"):
+        capi.correct_files(o, [fq], str(blocker / "sub"), ["o.fq"])
+    data = open(fq, "rb").read()
+    with open(fq, "wb") as f:
+        f.write(data[:data.rfind(b"\n+\n") + 3])  # the last record loses its quality line
+    os.makedirs(tmp_path / "out")
+    o.host_file_io = 1
+    with pytest.raises(capi.CareError, match="I/O"):
+        capi.correct_files(o, [fq], str(tmp_path / "out"), ["o.fq"])
