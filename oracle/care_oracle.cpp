@@ -88,18 +88,6 @@ void decode2bit(char* out, const uint32_t* enc, int len) {
     for (int i = 0; i < len; i++) out[i] = kBase[get2bit(enc, i)];
 }
 
-// reference: include/sequencehelpers.hpp:645-691 (convert2BitTo2BitHiLo):
-// hi plane = high bit of each base code, lo plane = low bit, 32 bases per
-// word, first base in the most significant bit.
-void toHiLo(uint32_t* hi, uint32_t* lo, const uint32_t* enc, int len, int wordsPerPlane) {
-    for (int w = 0; w < wordsPerPlane; w++) hi[w] = lo[w] = 0;
-    for (int i = 0; i < len; i++) {
-        const uint32_t b = get2bit(enc, i);
-        hi[i / 32] |= (b >> 1) << (31 - (i % 32));
-        lo[i / 32] |= (b & 1u) << (31 - (i % 32));
-    }
-}
-
 // ---------------------------------------------------------------- read store
 
 struct Store {
@@ -111,6 +99,15 @@ struct Store {
     std::vector<char> qual;  // n * Lmax
     std::vector<uint8_t> ambig;
     bool hasQual = false;
+    // hi/lo planes of every read, forward then reverse complement, W words per
+    // plane (reference: include/sequencehelpers.hpp:264-324 and 645-691,
+    // reverseComplementSequence2Bit and convert2BitTo2BitHiLo: hi plane = high
+    // bit of each base code, lo plane = low bit, 32 bases per word, first base
+    // in the most significant bit).  The reference converts them per call
+    // (include/corrector.hpp:880-922); kept here once per read: same bits.
+    int W = 0;
+    std::vector<uint32_t> hilo;  // n * 4 * W: fwd hi, fwd lo, rc hi, rc lo
+    const uint32_t* planes(uint64_t id, bool rc) const { return &hilo[(id * 4 + (rc ? 2 : 0)) * size_t(W)]; }
 };
 
 struct Tables {
@@ -118,10 +115,14 @@ struct Tables {
     int nmaps = 48;
     int maxValuesPerKey = 75;
     uint64_t kmask = 0;
-    // per map: sorted unique kept keys, their value ranges, and the values
-    std::vector<std::vector<uint64_t>> keys;
-    std::vector<std::vector<uint32_t>> begin;
-    std::vector<std::vector<uint32_t>> count;
+    // per map: the kept keys in an open-addressing lookup (reference:
+    // include/cpuhashtable.hpp:30-292, AoSCpuSingleValueHashTable: murmur64 of
+    // the key, linear probing) to the range of their read ids in `values`
+    struct Slot {
+        uint64_t key;
+        uint32_t begin, count;  // count 0: empty slot (kept keys have 2 or more ids)
+    };
+    std::vector<std::vector<Slot>> slots;
     std::vector<std::vector<uint32_t>> values;
     // signatures are not kept: a query recomputes its anchor's, as the
     // reference's query does (include/ordinaryminhasher.hpp:155-169)
@@ -225,6 +226,26 @@ void buildStore(Oracle& O, const char* seqs, const uint64_t* offs, const char* q
         encode2bit(&s.enc[i * s.pitch], tmp.data(), L);
         if (s.hasQual) std::memcpy(&s.qual[i * size_t(s.Lmax)], quals + offs[i], L);
     }
+    s.W = sdiv(std::max(s.Lmax, 1), 32) + 1;
+    s.hilo.assign(n * 4 * size_t(s.W), 0);
+#pragma omp parallel for schedule(static, 4096)
+    for (int64_t i = 0; i < int64_t(n); i++) {
+        const int L = s.len[i];
+        const uint32_t* enc = &s.enc[i * s.pitch];
+        uint32_t* fh = &s.hilo[uint64_t(i) * 4 * s.W];
+        uint32_t* fl = fh + s.W;
+        uint32_t* rh = fl + s.W;
+        uint32_t* rl = rh + s.W;
+        for (int p = 0; p < L; p++) {
+            const uint32_t b = get2bit(enc, p);
+            const uint32_t c = 3u - b;  // complement; reverse-complement position L-1-p
+            const int q = L - 1 - p;
+            fh[p / 32] |= (b >> 1) << (31 - (p % 32));
+            fl[p / 32] |= (b & 1u) << (31 - (p % 32));
+            rh[q / 32] |= (c >> 1) << (31 - (q % 32));
+            rl[q / 32] |= (c & 1u) << (31 - (q % 32));
+        }
+    }
     // reference: include/qualityscorecompression.hpp:25-140 (QualityCompressorConfig<1|2>,
     // encodeQualityString: the first bin whose boundary is >= Q, Q = int(char) - 33;
     // decodeQualityToString: the bin's score) as include/chunkedreadstorage.hpp:532-607
@@ -270,9 +291,7 @@ void buildTables(Oracle& O, int threads) {
         r = std::max(10, r);
         t.maxValuesPerKey = r;
     }
-    t.keys.assign(t.nmaps, {});
-    t.begin.assign(t.nmaps, {});
-    t.count.assign(t.nmaps, {});
+    t.slots.assign(t.nmaps, {});
     t.values.assign(t.nmaps, {});
     // maps in waves of up to 8: the (key, read id) pairs of a wave's maps are
     // the only per-read data held (16 bytes per read and map)
@@ -294,22 +313,30 @@ void buildTables(Oracle& O, int threads) {
             const int h = h0 + j;
             auto& v = kv[j];
             std::sort(v.begin(), v.end());
+            uint64_t kept = 0;
+            for (uint64_t a = 0; a < v.size();) {
+                uint64_t b = a;
+                while (b < v.size() && v[b].first == v[a].first) b++;
+                if (b - a >= 2 && b - a <= upper) kept++;
+                a = b;
+            }
+            uint64_t cap = 16;
+            while (cap < 2 * kept) cap <<= 1;
+            auto& sl = t.slots[h];
+            sl.assign(cap, Tables::Slot{0, 0, 0});
             for (uint64_t a = 0; a < v.size();) {
                 uint64_t b = a;
                 while (b < v.size() && v[b].first == v[a].first) b++;
                 const uint64_t num = b - a;
                 if (num >= 2 && num <= upper) {
-                    t.keys[h].push_back(v[a].first);
-                    t.begin[h].push_back(uint32_t(t.values[h].size()));
-                    t.count[h].push_back(uint32_t(num));
+                    uint64_t i = murmur64(v[a].first) & (cap - 1);
+                    while (sl[i].count) i = (i + 1) & (cap - 1);
+                    sl[i] = Tables::Slot{v[a].first, uint32_t(t.values[h].size()), uint32_t(num)};
                     for (uint64_t q = a; q < b; q++) t.values[h].push_back(v[q].second);
                 }
                 a = b;
             }
             std::vector<std::pair<uint64_t, uint32_t>>().swap(v);
-            t.keys[h].shrink_to_fit();
-            t.begin[h].shrink_to_fit();
-            t.count[h].shrink_to_fit();
             t.values[h].shrink_to_fit();
         }
     }
@@ -648,13 +675,13 @@ void candidates(const Oracle& O, uint64_t anchor, std::vector<uint32_t>& out, ui
         uint64_t sig[CG_MAX_HASHMAPS];
         signature(&s.enc[anchor * s.pitch], s.len[anchor], t.k, t.nmaps, sig);
         for (int h = 0; h < t.nmaps; h++) {
-            const auto& ks = t.keys[h];
-            auto it = std::lower_bound(ks.begin(), ks.end(), sig[h]);
-            if (it != ks.end() && *it == sig[h]) {
-                const size_t j = it - ks.begin();
-                if (int(t.count[h][j]) > t.maxValuesPerKey) continue;
-                out.insert(out.end(), t.values[h].begin() + t.begin[h][j],
-                           t.values[h].begin() + t.begin[h][j] + t.count[h][j]);
+            const auto& sl = t.slots[h];
+            const uint64_t mask = sl.size() - 1;
+            for (uint64_t i = murmur64(sig[h]) & mask; sl[i].count; i = (i + 1) & mask) {
+                if (sl[i].key != sig[h]) continue;
+                out.insert(out.end(), t.values[h].begin() + sl[i].begin,
+                           t.values[h].begin() + sl[i].begin + sl[i].count);
+                break;
             }
         }
     }
@@ -749,28 +776,23 @@ uint8_t correctOne(const Oracle& O, uint64_t anchor, const std::vector<uint32_t>
     const Store& s = O.s;
     const cg_options& o = O.o;
     const int La = s.len[anchor];
-    const int W = sdiv(s.Lmax, 32) + 1;
     if (candIds.empty()) return 0;
     cnt.uniq += candIds.size();
-    std::vector<uint32_t> aHi(W), aLo(W), cHi(W), cLo(W), rHi(W), rLo(W);
-    toHiLo(aHi.data(), aLo.data(), &s.enc[anchor * s.pitch], La, W);
+    const uint32_t* aHi = s.planes(anchor, false);
+    const uint32_t* aLo = aHi + s.W;
     const std::string anchorStr = decodeRead(s, anchor);
     std::string anchorQ;
     if (o.use_quality_scores) anchorQ.assign(&s.qual[anchor * size_t(s.Lmax)], La);
-    std::vector<Cand> cs;
-    std::vector<uint32_t> rcEnc(s.pitch);
+    thread_local std::vector<Cand> cs, kept, next;  // reused across anchors
+    thread_local std::vector<char> remove;
+    cs.clear();
     for (size_t i = 0; i < candIds.size(); i++) {
         const uint32_t id = candIds[i];
         const int Lc = s.len[id];
-        const uint32_t* enc = &s.enc[id * s.pitch];
-        toHiLo(cHi.data(), cLo.data(), enc, Lc, W);
-        std::string fwd = decodeRead(s, id);
-        std::string rcs(Lc, 'A');
-        for (int p = 0; p < Lc; p++) rcs[p] = complementChar(fwd[Lc - 1 - p]);
-        encode2bit(rcEnc.data(), rcs.data(), Lc);
-        toHiLo(rHi.data(), rLo.data(), rcEnc.data(), Lc, W);
-        const Aln f = align(aHi.data(), aLo.data(), La, cHi.data(), cLo.data(), Lc, o.min_overlap, o.max_error_rate, o.min_overlap_ratio);
-        const Aln r = align(aHi.data(), aLo.data(), La, rHi.data(), rLo.data(), Lc, o.min_overlap, o.max_error_rate, o.min_overlap_ratio);
+        const uint32_t* cHi = s.planes(id, false);
+        const uint32_t* rHi = s.planes(id, true);
+        const Aln f = align(aHi, aLo, La, cHi, cHi + s.W, Lc, o.min_overlap, o.max_error_rate, o.min_overlap_ratio);
+        const Aln r = align(aHi, aLo, La, rHi, rHi + s.W, Lc, o.min_overlap, o.max_error_rate, o.min_overlap_ratio);
         const int ori = orientation(f, r, La, o.min_overlap_ratio, o.min_overlap, o.estimated_errorrate * 4.0f);
         if (ori == 3) continue;
         Cand c;
@@ -779,26 +801,12 @@ uint8_t correctOne(const Oracle& O, uint64_t anchor, const std::vector<uint32_t>
         c.orient = ori;
         c.aln = ori == 1 ? f : r;
         c.paired = paired.empty() ? false : paired[i] != 0;
-        c.seq = ori == 1 ? fwd : rcs;
-        if (o.use_quality_scores) {
-            // include/corrector.hpp:1214-1239: rows of Lmax qualities (zero past
-            // the read's end, include/chunkedreadstorage.hpp:532-610); a reverse-
-            // complement candidate's whole row is reversed, so a read shorter than
-            // Lmax takes zeros first
-            const char* row = &s.qual[id * size_t(s.Lmax)];
-            if (ori == 2) {
-                c.qual.assign(size_t(Lc), 0);
-                for (int i = 0; i < Lc; i++) c.qual[i] = row[s.Lmax - 1 - i];
-            } else {
-                c.qual.assign(row, Lc);
-            }
-        }
         cs.push_back(std::move(c));
     }
     cnt.aligned += cs.size();
     if (cs.empty()) return 0;
     // mismatch ratio filter: include/corrector.hpp:1053-1149 (SE), 1151-1211 (PE)
-    std::vector<Cand> kept;
+    kept.clear();
     if (o.pair_mode == CG_PAIR_PE) {
         for (auto& c : cs) {
             if (c.paired) kept.push_back(std::move(c));
@@ -827,15 +835,35 @@ uint8_t correctOne(const Oracle& O, uint64_t anchor, const std::vector<uint32_t>
     if (kept.empty()) return 0;
     // overlap weights: include/corrector.hpp:1260-1280, include/hostdevicefunctions.cuh:93-95
     for (auto& c : kept) c.weight = 1.0f - std::sqrt(c.aln.nOps / (c.aln.overlap * o.max_error_rate));
+    // candidate strings in aligned orientation (include/corrector.hpp:1242-1258)
+    // and their qualities (include/corrector.hpp:1214-1239: rows of Lmax
+    // qualities, zero -- or the first bin with lossy qualities -- past the
+    // read's end; a reverse-complement candidate's whole row is reversed, so a
+    // read shorter than Lmax takes the padding first)
+    for (auto& c : kept) {
+        c.seq = decodeRead(s, c.id);
+        if (c.orient == 2) {
+            std::reverse(c.seq.begin(), c.seq.end());
+            for (auto& ch : c.seq) ch = complementChar(ch);
+        }
+        if (o.use_quality_scores) {
+            const char* row = &s.qual[c.id * size_t(s.Lmax)];
+            if (c.orient == 2) {
+                c.qual.assign(size_t(c.len), 0);
+                for (int i = 0; i < c.len; i++) c.qual[i] = row[s.Lmax - 1 - i];
+            } else {
+                c.qual.assign(row, c.len);
+            }
+        }
+    }
     cnt.msaCands += kept.size();
-    Msa m;
+    thread_local Msa m;  // buffers reused across anchors
     buildMsa(m, anchorStr, anchorQ, kept, o.use_quality_scores != 0, O.qweight);
     cnt.msaBuilds++;
     // refinement: include/corrector.hpp:1307-1421
     for (int it = 0; it < 5; it++) {
-        std::vector<char> remove;
         if (!differentRegion(m, anchorStr, kept, int(o.estimated_coverage), remove)) break;
-        std::vector<Cand> next;
+        next.clear();
         for (size_t i = 0; i < kept.size(); i++)
             if (!remove[i]) next.push_back(std::move(kept[i]));
         const bool changed = next.size() != kept.size();

@@ -769,13 +769,14 @@ __device__ __forceinline__ int vote_candidate(const Params& p, int s, int len, b
 }
 
 // Quality score of position `pos` (aligned orientation) of a candidate row
-// (reference: include/corrector.hpp:1214-1239).  Rows hold Lmax scores, zero
-// past the read's end (include/chunkedreadstorage.hpp:532-610), and a reverse-
-// complement candidate's whole row is reversed, so a read shorter than Lmax
-// starts with the zero padding: its position pos reads score Lmax - 1 - pos.
-__device__ __forceinline__ uint8_t row_quality(const uint8_t* q, int lmax, int len, bool rc, int pos) {
-    const int qi = rc ? lmax - 1 - pos : pos;
-    return qi < len ? q[qi] : (uint8_t)0;
+// (reference: include/corrector.hpp:1214-1239).  Rows hold Lmax scores; past
+// the read's end the store holds what the reference's decoded row holds there
+// (zero, or the first bin's score with lossy qualities; include/
+// chunkedreadstorage.hpp:532-610), and a reverse-complement candidate's whole
+// row is reversed, so a read shorter than Lmax starts with that padding: its
+// position pos reads score Lmax - 1 - pos.
+__device__ __forceinline__ uint8_t row_quality(const uint8_t* q, int lmax, bool rc, int pos) {
+    return q[rc ? lmax - 1 - pos : pos];
 }
 
 __global__ void __launch_bounds__(1024) msa_correct_kernel(StoreArg st, Params p, BatchArg b,
@@ -902,7 +903,7 @@ __global__ void __launch_bounds__(1024) msa_correct_kernel(StoreArg st, Params p
                         uint32_t bb = get2bit(m.enc, sp);
                         if (m.rc) bb = 3u - bb;
                         float w = m.weight;
-                        if (p.useQuality) w = __fmul_rn(w, qw[row_quality(m.qual, st.lmax, (int)m.len, m.rc, pos)]);
+                        if (p.useQuality) w = __fmul_rn(w, qw[row_quality(m.qual, st.lmax, m.rc, pos)]);
                         add(k, bb, w);
                     }
                 }
@@ -1217,7 +1218,7 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
                 for (int wi = sp >> 4; c < c1; c += 32, wi += dwi, sp += dsp) {
                     const uint32_t bb = ((e[wi] >> sh) & 3u) ^ flip;
                     const int qi = sp + qd;
-                    const float wt = p.useQuality ? __fmul_rn(weight, qw[qi < len ? q[qi] : 0]) : weight;
+                    const float wt = p.useQuality ? __fmul_rn(weight, qw[q[qi]]) : weight;  // padding past the read's end as stored
                     uint2 v = wc[bb * lp + c];
                     if (add) {
                         v.x = __float_as_uint(__fadd_rn(__uint_as_float(v.x), wt));
@@ -1476,8 +1477,8 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
                                         (rc ? 3u : 0u);
                     float wt = __int_as_float(md.z);
                     if (p.useQuality)
-                        wt = __fmul_rn(wt, qw[row_quality(st.qual + (uint64_t)(uint32_t)md.w * st.lmax, st.lmax,
-                                                          len, rc, pos)]);
+                        wt = __fmul_rn(wt, qw[row_quality(st.qual + (uint64_t)(uint32_t)md.w * st.lmax, st.lmax, rc,
+                                                          pos)]);
 #pragma unroll
                     for (int q = 0; q < 4; q++)
                         if ((uint32_t)q == bb) w4[q] = __fadd_rn(w4[q], wt);

@@ -110,9 +110,6 @@ def main(argv=None):
     t.add_argument("--batch", type=int, default=4096)
     t.add_argument("--lr", type=float, default=2e-3)
     t.add_argument("--seed", type=int, default=1)
-    sy = sub.add_parser("train-synthetic", help="time the training kernels on random features")
-    sy.add_argument("--rows", type=int, default=1 << 20)
-    sy.add_argument("--epochs", type=int, default=1)
     e = sub.add_parser("evaluate")
     e.add_argument("--model", default=DEFAULT_MODEL)
     e.add_argument("--forest", default=None)
@@ -133,16 +130,6 @@ def main(argv=None):
         print(json.dumps({"columns": int(len(f)), "positive": float(y.mean()), "steps": int(len(losses)),
                           "epoch_loss": [float(losses[i * spe:(i + 1) * spe].mean()) for i in range(args.epochs)],
                           "collect_s": t1 - t0, "train_s": t2 - t1, "out": args.out}))
-    elif args.cmd == "train-synthetic":
-        rng = np.random.default_rng(1)
-        x = rng.uniform(0, 1, (args.rows, capi.CLASSIFIER_FEATURES)).astype(np.float32)
-        y = (x[:, 0] > 0.5).astype(np.uint8)
-        t0 = time.time()
-        model, losses = capi.train_classifier(x, y, capi.TrainOptions.defaults(epochs=args.epochs))
-        t1 = time.time()
-        z = capi.classifier_logits(model, x)
-        print(json.dumps({"rows": args.rows, "steps": int(len(losses)), "seconds": t1 - t0,
-                          "final_loss": float(losses[-1]), "accuracy": float(((z >= 0) == (y == 1)).mean())}))
     else:
         with open(args.model, "rb") as fh:
             model = fh.read()

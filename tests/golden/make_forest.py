@@ -16,6 +16,11 @@ way the reference's own workflow implies:
   4. run the reference in Forest mode (--correctionType 1 --ml-forestfile) on a
      separate test read set and store its output like the other fixtures.
 Outputs: forest_anchor.bin, forest_se.npz, and a "forest_se" manifest entry.
+
+`python tests/golden/make_forest.py workload` makes the workload-scale forest
+the learned classifier is compared with (forest_varlen.bin, described in
+forest_varlen.json): the same Print-mode features, from the reads the learned
+classifier is trained on, with the forest's size chosen on a held-out seed.
 """
 from __future__ import annotations
 
@@ -138,5 +143,83 @@ def main():
         print("forest", manifest["forest_se"]["score"], "classic", manifest["forest_se"]["classic_score"])
 
 
+def print_dump(reads: sim.SimReads, work: str, name: str):
+    """The reference's Print-mode features of a read set, labelled from the truth."""
+    fq = os.path.join(work, f"{name}.fq")
+    reads.write_fastq(fq)
+    d = os.path.join(work, name)
+    os.makedirs(d, exist_ok=True)
+    cov = round(reads.cfg.num_reads * (reads.cfg.read_len_min + reads.cfg.read_len_max) / 2 /
+                reads.cfg.genome_length)
+    ref("-i", fq, "-o", "out.fq", "-d", d, "-c", str(cov), "-k", "20", "-t", str(os.cpu_count() or 8), "--print",
+        cwd=d)
+    X = []
+    rid, pos, cons = [], [], []
+    with open(os.path.join(d, "anchorfeatures.txt")) as f:
+        header = f.readline().strip()
+        assert header == "13 extract_anchor_v3", header
+        for line in f:
+            t = line.split()
+            rid.append(int(t[0]))
+            pos.append(int(t[1]))
+            cons.append(ord(t[2]))
+            X.append([float(x) for x in t[3:16]])
+    rid = np.array(rid, np.int64)
+    idx = reads.offsets.astype(np.int64)[rid] + np.array(pos, np.int64)
+    y = (reads.truth[idx] == np.array(cons, np.uint8)).astype(np.int32)
+    return np.array(X, np.float32), y
+
+
+def workload_forest(seeds=(1001, 1002, 1003), validation_seed=1004, genome=10_000_000):
+    """The forest the learned decision is compared with: trained on the
+    reference's Print-mode features of the reads the learned classifier was
+    trained on (10 Mbp genome with repeats, reads U[50,250] at 30x, generator
+    seeds 1001-1003), its size chosen by the log-loss on a held-out seed.
+    Writes forest_varlen.bin and the "forest_varlen" manifest entry."""
+    from sklearn.ensemble import RandomForestClassifier
+    from sklearn.metrics import log_loss
+    import oracle
+    oracle.build_reference()
+    with tempfile.TemporaryDirectory() as work:
+        Xs, ys = [], []
+        for seed in seeds:
+            r = sim.SimReads(sim.scaled("c3_10mbp_varlen", genome, seed=seed))
+            X, y = print_dump(r, work, f"train{seed}")
+            print(f"seed {seed}: {len(y)} columns, {y.mean():.4f} positive", flush=True)
+            Xs.append(X)
+            ys.append(y)
+            r.close()
+        X, y = np.concatenate(Xs), np.concatenate(ys)
+        rv = sim.SimReads(sim.scaled("c3_10mbp_varlen", genome, seed=validation_seed))
+        Xv, yv = print_dump(rv, work, "validation")
+    rng = np.random.default_rng(5)
+    sub = rng.choice(len(y), size=min(len(y), 1_500_000), replace=False)
+    grid = []
+    for leaves in (256, 1024, 4096, 16384):
+        clf = RandomForestClassifier(n_estimators=32, max_leaf_nodes=leaves, random_state=7,
+                                     n_jobs=os.cpu_count() or 8)
+        clf.fit(X[sub], y[sub])
+        loss = float(log_loss(yv, np.clip(clf.predict_proba(Xv)[:, 1], 1e-6, 1 - 1e-6)))
+        grid.append({"trees": 32, "max_leaf_nodes": leaves, "validation_log_loss": loss})
+        print(grid[-1], flush=True)
+    best = min(grid, key=lambda g: g["validation_log_loss"])
+    clf = RandomForestClassifier(n_estimators=64, max_leaf_nodes=best["max_leaf_nodes"], random_state=7,
+                                 n_jobs=os.cpu_count() or 8)
+    clf.fit(X, y)
+    loss = float(log_loss(yv, np.clip(clf.predict_proba(Xv)[:, 1], 1e-6, 1 - 1e-6)))
+    fpath = os.path.join(HERE, "forest_varlen.bin")
+    serialize(clf, fpath)
+    mpath = os.path.join(HERE, "forest_varlen.json")
+    with open(mpath, "w") as f:
+        json.dump({"trees": 64, "max_leaf_nodes": best["max_leaf_nodes"], "training_rows": int(len(y)),
+                   "positive": float(y.mean()), "train_seeds": list(seeds), "validation_seed": validation_seed,
+                   "genome": genome, "grid": grid, "validation_log_loss": loss,
+                   "bytes": os.path.getsize(fpath)}, f, indent=1)
+    print("forest_varlen", best, loss, os.path.getsize(fpath), flush=True)
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "workload":
+        workload_forest()
+    else:
+        main()
