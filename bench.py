@@ -257,6 +257,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--forms", default="plain,batched,batched_learned,batched_candidates")
+    ap.add_argument("--sweep", default="c1_10mbp_repeats_se,c3_10mbp_varlen",
+                    help="workloads of the forest/learned threshold sweep ('none' to skip)")
     args = ap.parse_args()
     rank, world, local = env_rank()
     threads = os.cpu_count() or 1
@@ -286,7 +288,13 @@ def main():
         return float(t.item())
 
     model = open(learned.DEFAULT_MODEL, "rb").read()
-    forest = open(os.path.join(REPO, "tests", "golden", "forest_anchor.bin"), "rb").read()
+    # the forest the learned decision is compared with: trained on the reference's
+    # Print-mode features of the learned classifier's own training reads
+    # (tests/golden/make_forest.py workload); the fixture forest if it is absent
+    forest_path = os.path.join(REPO, "tests", "golden", "forest_varlen.bin")
+    if not os.path.exists(forest_path):
+        forest_path = os.path.join(REPO, "tests", "golden", "forest_anchor.bin")
+    forest = open(forest_path, "rb").read()
     hbm_peak, peak_kind = measured_peaks()
     forms_wanted = [f for f in args.forms.split(",") if f]
     if "batched_learned" not in forms_wanted:
@@ -526,6 +534,52 @@ def main():
                            "memory, destroy"}
         del flags, rows
 
+    def sweep_one(reads, cfg_, form, t):
+        o = form_options(cfg_, form)
+        o.driver = capi.CG_DRIVER_BATCHED
+        o.threshold_anchor = t
+        g = capi.CareGpu(o)
+        g.append_reads(reads.sequences, reads.offsets)
+        g.build_tables()
+        if form == "batched_learned":
+            g.load_classifier(model)
+        else:
+            g.load_forest(forest)
+        flags, rows = g.correct()
+        g.close()
+        sc = reads.score_results(0, flags, rows)
+        return {"threshold": t, "tp": sc["tp"], "fp": sc["fp"], "fn": sc["fn"]}
+
+    def matched(curve_a, curve_b):
+        """FP of curve_b at the TP of each point of curve_a (linear between
+        curve_b's neighbouring thresholds; None outside its TP range)."""
+        pts = sorted((p["tp"], p["fp"]) for p in curve_b)
+        out = []
+        for p in curve_a:
+            fp = None
+            for (t0, f0), (t1, f1) in zip(pts, pts[1:]):
+                if t0 <= p["tp"] <= t1:
+                    fp = f0 if t1 == t0 else f0 + (f1 - f0) * (p["tp"] - t0) / (t1 - t0)
+                    break
+            out.append({"tp": p["tp"], "fp_forest": p["fp"], "fp_learned_at_same_tp": fp,
+                        "forest_threshold": p["threshold"]})
+        return out
+
+    def threshold_sweep(name):
+        cfg_ = sim.CONFIGS[name]
+        reads_ = sim.SimReads(cfg_)
+        ts = (0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 0.95)
+        forest_curve = [sweep_one(reads_, cfg_, "forest", t) for t in ts]
+        learned_curve = [sweep_one(reads_, cfg_, "batched_learned", t) for t in ts]
+        reads_.close()
+        return {"forest": forest_curve, "learned": learned_curve, "learned_fp_at_forest_tp":
+                matched(forest_curve, learned_curve),
+                "forest_file": os.path.relpath(forest_path, REPO)}
+
+    sweeps = None
+    if args.sweep and args.sweep != "none":
+        sweeps = {name: threshold_sweep(name) for name in args.sweep.split(",") if name}
+
     secondary = None
     if args.secondary and args.secondary != "none" and args.secondary != args.config:
         cfg2 = sim.CONFIGS[args.secondary]
@@ -550,7 +604,7 @@ def main():
                                                    "msa_candidates", "msa_builds", "corrected_anchors",
                                                    "hq_anchors", "table_keys", "table_values",
                                                    "learned_columns", "learned_corrections")},
-                "secondary": secondary}
+                "secondary": secondary, "threshold_sweep": sweeps}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
