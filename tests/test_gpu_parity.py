@@ -4,6 +4,8 @@ All calls go through the C ABI (libcaregpu.so via ctypes).  Integer and
 order-fixed float work, so the bar is bit-exact: identical flags and
 identical corrected bases for every anchor.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -125,9 +127,12 @@ def test_gpu_paired_end_matches_oracle():
     g.close()
 
 
-def test_gpu_forest_matches_oracle_with_quality_and_tree_limit():
-    e = fx.manifest()["forest_se"]
-    forest = fx.forest_bytes(e)
+@pytest.mark.parametrize("forest_file", ["forest_anchor.bin", "forest_varlen.bin"])
+def test_gpu_forest_matches_oracle_with_quality_and_tree_limit(forest_file):
+    """The fixture forest (16 trees) and the workload forest the learned
+    decision is compared with (64 trees of up to 1024 leaves)."""
+    with open(os.path.join(fx.GOLDEN, forest_file), "rb") as f:
+        forest = f.read()
     cfg = sim.SimConfig(seed=45, genome_length=40_000, num_reads=8_000, repeat_families=3, repeat_copies=3,
                         read_len_min=100, read_len_max=150, sub_rate_5p=0.004, sub_rate_3p=0.03)
     r = sim.SimReads(cfg)
