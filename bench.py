@@ -71,10 +71,14 @@ UNIT = "reads/s"
 WINDOW = 4_194_304  # anchors per step
 # DRAM bytes (read + write) of align_lane_kernel per candidate and its warp
 # instructions per candidate, measured by ncu on one 65536-anchor launch of the
-# 150 bp workload with repeats at 2 Mbp (profiles/align_lane_kernel_c1_2mbp.md:
-# 92.92 MB and 1.28639e9 warp instructions for 3.777M candidates)
-ALIGN_DRAM_BYTES_PER_CANDIDATE = 92.92e6 / 3.777e6
-ALIGN_WARP_INST_PER_CANDIDATE = 1.28639e9 / 3.777e6
+# 100M-read workload's shape at 20 Mbp (profiles/top3_kernels_c4_shape_20mbp.md:
+# 632.2 MB and 1.15833e9 warp instructions for the launch's 3.3555M candidates,
+# the run's average from its own counters).  On the 2M-read workload with
+# repeats the instructions per candidate are the same (1.28639e9 for 3.777M,
+# profiles/align_lane_kernel_c1_2mbp.md) but the DRAM bytes far fewer (24.6 B:
+# candidates shared by the anchors of a batch hit in L2 there).
+ALIGN_DRAM_BYTES_PER_CANDIDATE = 632.2e6 / 3.3555e6
+ALIGN_WARP_INST_PER_CANDIDATE = 1.15833e9 / 3.3555e6
 # STEP2 speed of the oracle (the port) over the reference's own build, both on
 # 8 threads of an Intel Xeon @ 2.70 GHz, 2M-read 150 bp workload with repeats,
 # outputs byte-identical (python oracle/port_speed.py --threads 8): the port
@@ -470,9 +474,10 @@ def main():
                 "algorithmic_bytes_per_anchor": path_bytes / max(n_anchors, 1),
                 "kernel_bytes_per_launch": kbytes / launches, "avg_launch_ms": dur * 1e3,
                 "stage_seconds_per_step": {k: v / max(steps, 1) for k, v in stages.items()},
-                "note": "integer-issue bound, see `int`; the HBM fraction is low by construction and traffic "
-                        "(measured DRAM bytes, ncu per candidate x candidates per launch) is below the algorithmic "
-                        "bytes because the planes of candidates shared between anchors hit in L2"}
+                "note": "integer-issue bound, see `int`; the HBM fraction is low by construction.  traffic = "
+                        "measured DRAM bytes per candidate (ncu) x candidates per launch: the kernel reads each "
+                        "candidate's precomputed forward and reverse-complement hi/lo planes (96 B, in 32 B sectors) "
+                        "where the algorithmic count takes its 40 B 2-bit row"}
         if dom == "align":
             # warp instructions per candidate (ncu, committed profile) x the launch's candidates,
             # over the launch's CUDA-event time, against 152 SMs x 4 schedulers x 1 instruction per
@@ -484,7 +489,7 @@ def main():
                            "unit": "G warp-instructions/s", "frac": inst / dur / peak_i, "sm_mhz": mhz,
                            "warp_instructions_per_candidate": ALIGN_WARP_INST_PER_CANDIDATE,
                            "source": "smsp__inst_executed.sum per candidate from ncu "
-                                     "(profiles/align_lane_kernel_c1_2mbp.md) x candidates of an average launch"}
+                                     "(profiles/top3_kernels_c4_shape_20mbp.md) x candidates of an average launch"}
         return roof
 
     clk = ClockSampler(local, paused=True)
@@ -568,7 +573,7 @@ def main():
     def threshold_sweep(name):
         cfg_ = sim.CONFIGS[name]
         reads_ = sim.SimReads(cfg_)
-        ts = (0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 0.95)
+        ts = (0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 0.95)
         forest_curve = [sweep_one(reads_, cfg_, "forest", t) for t in ts]
         learned_curve = [sweep_one(reads_, cfg_, "batched_learned", t) for t in ts]
         reads_.close()

@@ -338,16 +338,21 @@ int cg_get_candidates_noalloc(cg_ctx* ctx, uint64_t anchor, uint32_t* out, uint3
  * takes the consensus base when the output reaches threshold_anchor (0.5),
  * otherwise the classic rule's decision (the fallback) stands.
  *
- * Features of a column c of an anchor of length L (in order): the four base
- * counts / coverage (A, C, G, T); the four base weights / column weight;
- * coverage / estimated coverage; column weight / estimated coverage; support
- * (consensus weight / column weight); anchor-base weight / column weight;
- * anchor-base count / coverage; consensus count / coverage; the anchor base
- * one-hot (4); the consensus base one-hot (4); c / L; min(c, L-1-c) / L; the
- * anchor's average support; its minimum support; its minimum coverage /
- * estimated coverage; its maximum coverage / estimated coverage; L / 256; the
- * anchor's number of differing columns / L; rows in the MSA / estimated
- * coverage; the quality weight of the anchor base (1 without quality scores).
+ * Features of a column c of an anchor of length L (in order; a ratio that
+ * lies near 1 enters as 1 - ratio, where BF16 keeps its digits): the four
+ * base counts / coverage (A, C, G, T); the four base weights / column weight;
+ * coverage / estimated coverage; column weight / estimated coverage;
+ * 1 - support (consensus weight / column weight); anchor-base weight / column
+ * weight; anchor-base count / coverage; 1 - consensus count / coverage;
+ * 1 - the mean weight of the anchor base's rows; 1 - the mean weight of the
+ * consensus base's rows; 1 - the mean weight of the column's rows; the second
+ * largest base weight / column weight; the consensus base one-hot (4); c / L;
+ * min(c, L-1-c) / L; 1 - the anchor's average support; 1 - its minimum
+ * support; its minimum coverage / estimated coverage; its maximum coverage /
+ * estimated coverage; L / 256; the anchor's number of differing columns / L;
+ * rows in the MSA / estimated coverage; the quality weight of the anchor base
+ * (1 without quality scores).  They include every feature of the reference's
+ * forest (extract_anchor_v3, include/classification.hpp:748-797).
  *
  * A serialized classifier is a 32-byte header {char magic[8] = "CGMLP001";
  * uint32 features = 32, hidden1 = 64, hidden2 = 64, payload bytes; uint32

@@ -1585,24 +1585,35 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
         const float cov = __fadd_rn(__fadd_rn(__fadd_rn(n4[0], n4[1]), n4[2]), n4[3]);
         const float icov = __fdiv_rn(1.0f, cov);
         const float icw = ci.colW > 0.0f ? __fdiv_rn(1.0f, ci.colW) : 0.0f;
+        // Ratios that sit near 1 enter as 1 - ratio: BF16 keeps about three
+        // significant digits, so 0.983 and 0.987 would be the same value but
+        // 0.017 and 0.013 are not.
+        const float na = pick(n4, ab), nc = pick(n4, (uint32_t)cb);
+        float second = 0.0f;  // the second largest base weight
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (q != cb) second = fmaxf(second, w4[q]);
         float f[kLearnedFeatures];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             f[q] = __fmul_rn(n4[q], icov);                 // base counts / coverage
             f[4 + q] = __fmul_rn(w4[q], icw);              // weights / column weight
-            f[14 + q] = (uint32_t)q == ab ? 1.0f : 0.0f;   // anchor base
             f[18 + q] = q == cb ? 1.0f : 0.0f;             // consensus base
         }
         f[8] = __fdiv_rn(cov, ec);
         f[9] = __fdiv_rn(ci.colW, ec);
-        f[10] = sup[c];
+        f[10] = __fsub_rn(1.0f, sup[c]);
         f[11] = __fmul_rn(pick(w4, ab), icw);
-        f[12] = __fmul_rn(pick(n4, ab), icov);
-        f[13] = __fmul_rn(pick(n4, (uint32_t)cb), icov);
+        f[12] = __fmul_rn(na, icov);
+        f[13] = __fsub_rn(1.0f, __fmul_rn(nc, icov));
+        f[14] = __fsub_rn(1.0f, __fdiv_rn(pick(w4, ab), na));                   // mean weight of the anchor base's rows
+        f[15] = nc > 0.0f ? __fsub_rn(1.0f, __fdiv_rn(ci.consW, nc)) : 1.0f;   // ... of the consensus base's rows
+        f[16] = __fsub_rn(1.0f, __fmul_rn(ci.colW, icov));                      // ... of all rows
+        f[17] = __fmul_rn(second, icw);                                          // runner-up weight / column weight
         f[22] = __fmul_rn((float)c, invLa);
         f[23] = __fmul_rn((float)min(c, La - 1 - c), invLa);
-        f[24] = avg;
-        f[25] = mins;
+        f[24] = __fsub_rn(1.0f, avg);
+        f[25] = __fsub_rn(1.0f, mins);
         f[26] = __fdiv_rn((float)minc, ec);
         f[27] = __fdiv_rn((float)maxc, ec);
         f[28] = __fmul_rn((float)La, 1.0f / 256.0f);

@@ -99,6 +99,37 @@ def evaluate(reads: sim.SimReads, model: bytes, forest: bytes | None = None, **k
     return res
 
 
+def log_loss(model: bytes, f: np.ndarray, y: np.ndarray) -> float:
+    """Mean binary cross-entropy of a classifier's outputs (the inference kernel's logits)."""
+    z = capi.classifier_logits(model, f).astype(np.float64)
+    return float(np.mean(np.logaddexp(0.0, z) - y * z))
+
+
+def score_threshold(reads: sim.SimReads, correction_type: int, t: float, model: bytes | None = None,
+                    forest: bytes | None = None) -> dict:
+    """TP/FP/FN of a decision at threshold_anchor t (batched driver)."""
+    g = capi.CareGpu(options(reads, correction_type, threshold_anchor=t, driver=capi.CG_DRIVER_BATCHED))
+    g.append_reads(reads.sequences, reads.offsets)
+    g.build_tables()
+    if model is not None:
+        g.load_classifier(model)
+    if forest is not None:
+        g.load_forest(forest)
+    flags, rows = g.correct()
+    g.close()
+    sc = reads.score_results(0, flags, rows)
+    return {"threshold": t, "tp": sc["tp"], "fp": sc["fp"], "fn": sc["fn"]}
+
+
+def fp_at_tp(curve: list, tp: int):
+    """FP of a (tp, fp) curve at `tp`, linear between its points; None outside."""
+    pts = sorted((p["tp"], p["fp"]) for p in curve)
+    for (t0, f0), (t1, f1) in zip(pts, pts[1:]):
+        if t0 <= tp <= t1:
+            return f0 if t1 == t0 else f0 + (f1 - f0) * (tp - t0) / (t1 - t0)
+    return None
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -106,30 +137,63 @@ def main(argv=None):
     t.add_argument("--out", default=DEFAULT_MODEL)
     t.add_argument("--columns", type=int, default=5_000_000)
     t.add_argument("--genome", type=int, default=10_000_000)
-    t.add_argument("--epochs", type=int, default=4)
+    t.add_argument("--grid", default="4:2e-3,8:1e-3,16:1e-3,16:5e-4",
+                   help="epochs:learning-rate pairs; the one with the lowest validation loss is kept")
     t.add_argument("--batch", type=int, default=4096)
-    t.add_argument("--lr", type=float, default=2e-3)
     t.add_argument("--seed", type=int, default=1)
+    t.add_argument("--validation-seed", type=int, default=1004)
     e = sub.add_parser("evaluate")
     e.add_argument("--model", default=DEFAULT_MODEL)
     e.add_argument("--forest", default=None)
     e.add_argument("--genome", type=int, default=10_000_000)
+    w = sub.add_parser("sweep", help="TP/FP of the learned decision and a forest over thresholds")
+    w.add_argument("--model", default=DEFAULT_MODEL)
+    w.add_argument("--forest", required=True)
+    w.add_argument("--workloads", default="c1_10mbp_repeats_se,c3_10mbp_varlen")
     args = ap.parse_args(argv)
     if args.cmd == "train":
         t0 = time.time()
         f, y = training_set(args.columns, args.genome)
+        rv = sim.SimReads(sim.scaled("c3_10mbp_varlen", args.genome, seed=args.validation_seed))
+        fv, yv = collect(rv)
+        rv.close()
         t1 = time.time()
-        o = capi.TrainOptions.defaults(epochs=args.epochs, batch_rows=args.batch, learning_rate=args.lr,
-                                       seed=args.seed)
-        model, losses = capi.train_classifier(f, y, o)
+        runs = []
+        best = None
+        for item in args.grid.split(","):
+            ep, lr = item.split(":")
+            o = capi.TrainOptions.defaults(epochs=int(ep), batch_rows=args.batch, learning_rate=float(lr),
+                                           seed=args.seed)
+            model, losses = capi.train_classifier(f, y, o)
+            vl = log_loss(model, fv, yv)
+            runs.append({"epochs": int(ep), "learning_rate": float(lr), "steps": int(len(losses)),
+                         "train_loss_last_epoch": float(losses[-max(len(losses) // int(ep), 1):].mean()),
+                         "validation_loss": vl})
+            if best is None or vl < best[0]:
+                best = (vl, model, runs[-1])
         t2 = time.time()
         os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
         with open(args.out, "wb") as fh:
-            fh.write(model)
-        spe = max(len(losses) // args.epochs, 1)
-        print(json.dumps({"columns": int(len(f)), "positive": float(y.mean()), "steps": int(len(losses)),
-                          "epoch_loss": [float(losses[i * spe:(i + 1) * spe].mean()) for i in range(args.epochs)],
+            fh.write(best[1])
+        print(json.dumps({"columns": int(len(f)), "positive": float(y.mean()), "validation_columns": int(len(fv)),
+                          "validation_seed": args.validation_seed, "grid": runs, "chosen": best[2],
                           "collect_s": t1 - t0, "train_s": t2 - t1, "out": args.out}))
+    elif args.cmd == "sweep":
+        with open(args.model, "rb") as fh:
+            model = fh.read()
+        with open(args.forest, "rb") as fh:
+            forest = fh.read()
+        ts = (0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 0.95)
+        out = {}
+        for name in args.workloads.split(","):
+            r = sim.SimReads(sim.CONFIGS[name])
+            fc = [score_threshold(r, capi.CG_CORR_FOREST, x, forest=forest) for x in ts]
+            lc = [score_threshold(r, capi.CG_CORR_LEARNED, x, model=model) for x in ts]
+            r.close()
+            out[name] = {"forest": fc, "learned": lc,
+                         "learned_fp_at_forest_tp": [{"tp": p["tp"], "fp_forest": p["fp"],
+                                                      "fp_learned": fp_at_tp(lc, p["tp"])} for p in fc]}
+        print(json.dumps(out))
     else:
         with open(args.model, "rb") as fh:
             model = fh.read()
