@@ -64,7 +64,7 @@ sys.path.insert(0, REPO)
 
 import numpy as np  # noqa: E402
 
-from rabbitqcplus_gb300 import capi, learned, sim  # noqa: E402
+from rabbitqcplus_gb300 import capi, learned, shard, sim  # noqa: E402
 
 METRIC = "corrected reads/s on 1 GB300: plain vs batched+learned, at equal TP/FP vs truth"
 UNIT = "reads/s"
@@ -347,6 +347,9 @@ def main():
         """Untimed pass over every window; TP/FP/FN of the whole read set (and
         per-window checksums of the results)."""
         cand = bool(g.options.correct_candidates)
+        if cand:
+            # the combine step needs the pass over every read: every rank scores the whole set
+            wins = windows_of(reads.n, args.window, bool(reads.cfg.paired))
         wmax = max(c for _, c in wins)
         if cand:
             flags_all = np.zeros(reads.n, np.uint8)
@@ -366,6 +369,10 @@ def main():
                 tot[k] += sc[k]
             if digest:
                 digests.append(window_digest(flags[:c], rows[:c], reads.lengths[s:s + c]))
+        if dist is not None:  # the ranks' shards together cover every read
+            t = torch.tensor([tot[k] for k in ("tp", "fp", "fn", "reads_scored")], dtype=torch.int64, device="cuda")
+            dist.all_reduce(t)
+            tot = dict(zip(("tp", "fp", "fn", "reads_scored"), (int(x) for x in t.tolist())))
         return tot, (digests if digest else None)
 
     def run_form(reads, cfg_, form, wins, steps, warmup, clk=None, digest=False):
@@ -412,7 +419,10 @@ def main():
 
     def run_workload(name, cfg_, steps, warmup, clk, with_roofline):
         reads = sim.SimReads(cfg_)
-        wins = windows_of(reads.n, args.window, bool(cfg_.paired))
+        # replicas: every rank holds the whole read store and tables and
+        # corrects its own contiguous shard of anchors, window by window
+        first, count = shard.shard_range(reads.n, rank, world, bool(cfg_.paired))
+        wins = [(first + s0, c) for s0, c in windows_of(count, args.window, bool(cfg_.paired))]
         runs = {}
         for form in forms_wanted:
             runs[form] = run_form(reads, cfg_, form, wins, steps, warmup, clk, digest=form in ("plain", "batched"))
@@ -423,8 +433,12 @@ def main():
                            "fn": forest_run["score"]["fn"], "driver": "plain", "timed": False}
         if "plain" in runs and "batched" in runs:
             # every flag and corrected base of every read, compared window by window
-            forms["batched_bit_exact_with_plain"] = runs["plain"]["res"] == runs["batched"]["res"] and \
-                runs["plain"]["score"] == runs["batched"]["score"]
+            same = runs["plain"]["res"] == runs["batched"]["res"] and runs["plain"]["score"] == runs["batched"]["score"]
+            if dist is not None:
+                t = torch.tensor([int(same)], dtype=torch.int64, device="cuda")
+                dist.all_reduce(t, op=dist.ReduceOp.MIN)
+                same = bool(t.item())
+            forms["batched_bit_exact_with_plain"] = same
         bl = runs["batched_learned"]
         forms["batched_shape"] = {k: bl["st1"][k] for k in ("batch_anchors", "align_blocks", "msa_warps",
                                                           "streams", "seconds_tune")}
@@ -518,11 +532,12 @@ def main():
                 pinned.append(a)
         k = max(1, args.e2e_steps)
         te = 0.0
+        sf, sc = shard.shard_range(n, rank, world, bool(cfg.paired))  # this replica's anchors
         for i in range(1 + k):
             barrier()
             t0 = time.perf_counter()
             g2 = make_ctx(reads, cfg, "batched_learned")
-            g2.correct(0, n, flags, rows)
+            g2.correct(sf, sc, flags[sf:sf + sc], rows[sf:sf + sc])
             g2.close()
             barrier()
             if i >= 1:
@@ -530,13 +545,14 @@ def main():
         for a in pinned:
             rt.cudaHostUnregister(a.ctypes.data)
         te = max_over_ranks(te)
-        e2e = {"value": world * n * k / te, "unit": UNIT, "steps": k, "seconds_per_step": te / k,
+        e2e = {"value": n * k / te, "unit": UNIT, "steps": k, "seconds_per_step": te / k,
                "h2d_bytes_per_step": int(reads.sequences.nbytes + reads.offsets.nbytes + len(model)),
-               "d2h_bytes_per_step": int(flags.nbytes + rows.nbytes), "pinned": len(pinned) == 4,
+               "d2h_bytes_per_step": int(flags[sf:sf + sc].nbytes + rows[sf:sf + sc].nbytes),
+               "pinned": len(pinned) == 4,
                "form": "batched_learned",
                "includes": "fresh context, append of every read from pinned host memory, device read-store and "
-                           "table build, classifier load, correction of every anchor, every result to pinned host "
-                           "memory, destroy"}
+                           "table build, classifier load, correction of every anchor (each replica its shard), "
+                           "every result to pinned host memory, destroy"}
         del flags, rows
 
     def sweep_one(reads, cfg_, form, t):
