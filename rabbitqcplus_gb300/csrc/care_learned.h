@@ -43,8 +43,8 @@ struct MlpAdam {
 };
 
 size_t mlp_grad_smem_bytes();
-// partial-gradient slots (warps) one minibatch of `rows` rows writes
-unsigned int mlp_grad_warps(unsigned int rows);
+// partial-gradient slots (128-row tiles) one minibatch of `rows` rows writes
+unsigned int mlp_grad_parts(unsigned int rows);
 
 // Inference over `count` (or *countPtr, at most cap) columns: logits to
 // `logits`, or the consensus base into out[meta.x][meta.y & 0xffff] for every
@@ -58,14 +58,17 @@ cudaError_t launch_mlp_infer(const unsigned char* model, const __nv_bfloat16* fe
 // counters[kCounterTimeouts] and leaves its columns to the fallback decision.
 cudaError_t set_classifier_wait_limit(uint32_t polls);
 // Partial gradients of the mean binary cross-entropy over `rows` rows of a
-// minibatch: rows perm[step * rows + r] of feat/label (perm may be null; step
-// = *stepPtr % stepsPerEpoch, or 0 without stepPtr).
+// minibatch, one slot per 128-row tile (tcgen05 products): rows
+// perm[step * rows + r] of feat/label (perm may be null; step = *stepPtr %
+// stepsPerEpoch, or 0 without stepPtr).  A tile whose MMA wait runs out
+// writes zeros and counts in *failed.
 cudaError_t launch_mlp_grad(const unsigned char* model, const __nv_bfloat16* feat, const float* label,
                             const uint32_t* perm, const unsigned long long* stepPtr, unsigned int stepsPerEpoch,
-                            unsigned int rows, float invTotal, float* part, cudaStream_t s);
+                            unsigned int rows, float invTotal, float* part, unsigned long long* failed,
+                            cudaStream_t s);
 // Sum of the partials (-> grad, loss -> lossOut[*stepPtr or 0]); with `state`
 // an Adam step that rewrites `model`; with stepPtr the step counter advances.
-cudaError_t launch_mlp_reduce(const float* part, unsigned int warps, float* grad, float* lossOut, MlpAdam* state,
+cudaError_t launch_mlp_reduce(const float* part, unsigned int parts, float* grad, float* lossOut, MlpAdam* state,
                               unsigned char* model, unsigned long long* stepPtr, cudaStream_t s);
 cudaError_t launch_to_bf16(const float* in, uint64_t n, __nv_bfloat16* out, cudaStream_t s);
 

@@ -176,7 +176,7 @@ int cg_train_classifier(const cg_train_options* o, const float* features, const 
     Stream st;
     TRY(cudaStreamCreateWithFlags(&st.s, cudaStreamNonBlocking));
     cudaStream_t s = st.s;
-    Dev f32, bf, lab, perm, model, part, adam, step, loss;
+    Dev f32, bf, lab, perm, model, part, adam, step, loss, failed;
     int rc = upload_features(features, n, f32, bf, s);
     if (rc != CG_OK) return rc;
     std::vector<float> hl(n);
@@ -186,9 +186,11 @@ int cg_train_classifier(const cg_train_options* o, const float* features, const 
     TRY(perm.alloc(n * sizeof(uint32_t)));
     TRY(model.alloc(kMlpBytes));
     TRY(cudaMemcpyAsync(model.p, blob.data(), kMlpBytes, cudaMemcpyHostToDevice, s));
-    const unsigned warps = mlp_grad_warps((unsigned)B);
-    TRY(part.alloc((size_t)warps * kMlpParams * sizeof(float)));
-    TRY(cudaMemsetAsync(part.p, 0, (size_t)warps * kMlpParams * sizeof(float), s));
+    const unsigned parts = mlp_grad_parts((unsigned)B);
+    TRY(part.alloc((size_t)parts * kMlpParams * sizeof(float)));
+    TRY(cudaMemsetAsync(part.p, 0, (size_t)parts * kMlpParams * sizeof(float), s));
+    TRY(failed.alloc(sizeof(unsigned long long)));
+    TRY(cudaMemsetAsync(failed.p, 0, sizeof(unsigned long long), s));
     // optimiser state: master weights from the initial model
     auto hs = std::make_unique<MlpAdam>();
     std::memset(hs.get(), 0, sizeof(MlpAdam));
@@ -213,9 +215,9 @@ int cg_train_classifier(const cg_train_options* o, const float* features, const 
     TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = launch_mlp_grad(model.as<unsigned char>(), bf.as<__nv_bfloat16>(), lab.as<float>(),
                                     perm.as<uint32_t>(), step.as<unsigned long long>(), stepsPerEpoch, (unsigned)B,
-                                    1.0f / (float)B, part.as<float>(), s);
+                                    1.0f / (float)B, part.as<float>(), failed.as<unsigned long long>(), s);
     if (e == cudaSuccess)
-        e = launch_mlp_reduce(part.as<float>(), warps, nullptr, loss.as<float>(), adam.as<MlpAdam>(),
+        e = launch_mlp_reduce(part.as<float>(), parts, nullptr, loss.as<float>(), adam.as<MlpAdam>(),
                               model.as<unsigned char>(), step.as<unsigned long long>(), s);
     const cudaError_t e2 = cudaStreamEndCapture(s, &graph);
     if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -238,6 +240,9 @@ int cg_train_classifier(const cg_train_options* o, const float* features, const 
         for (uint32_t k = 0; k < stepsPerEpoch && rc == CG_OK; k++) rc = cuda_status(cudaGraphLaunch(exec, s));
     }
     if (rc == CG_OK) rc = cuda_status(cudaStreamSynchronize(s));
+    unsigned long long nFailed = 0;
+    if (rc == CG_OK) rc = cuda_status(cudaMemcpy(&nFailed, failed.p, sizeof(nFailed), cudaMemcpyDeviceToHost));
+    if (rc == CG_OK && nFailed) rc = CG_ERR_TIMEOUT;  // a tile gave up waiting for its tensor-core products
     if (rc == CG_OK) rc = cuda_status(cudaMemcpy(blob.data(), model.p, kMlpBytes, cudaMemcpyDeviceToHost));
     if (rc == CG_OK && losses && loss_capacity) {
         const uint64_t k = std::min<uint64_t>(loss_capacity, totalSteps);
@@ -259,7 +264,7 @@ int cg_classifier_gradients(int device, const void* model_data, size_t model_siz
     Stream st;
     TRY(cudaStreamCreateWithFlags(&st.s, cudaStreamNonBlocking));
     cudaStream_t s = st.s;
-    Dev f32, bf, lab, model, part, grad;
+    Dev f32, bf, lab, model, part, grad, failed;
     int rc = upload_features(features, n, f32, bf, s);
     if (rc != CG_OK) return rc;
     std::vector<float> hl(n);
@@ -268,16 +273,21 @@ int cg_classifier_gradients(int device, const void* model_data, size_t model_siz
     TRY(cudaMemcpyAsync(lab.p, hl.data(), n * sizeof(float), cudaMemcpyHostToDevice, s));
     TRY(model.alloc(kMlpBytes));
     TRY(cudaMemcpyAsync(model.p, blob.data(), kMlpBytes, cudaMemcpyHostToDevice, s));
-    const unsigned warps = mlp_grad_warps(n);
-    TRY(part.alloc((size_t)warps * kMlpParams * sizeof(float)));
-    TRY(cudaMemsetAsync(part.p, 0, (size_t)warps * kMlpParams * sizeof(float), s));
+    const unsigned parts = mlp_grad_parts(n);
+    TRY(part.alloc((size_t)parts * kMlpParams * sizeof(float)));
+    TRY(cudaMemsetAsync(part.p, 0, (size_t)parts * kMlpParams * sizeof(float), s));
     TRY(grad.alloc(kMlpParams * sizeof(float)));
+    TRY(failed.alloc(sizeof(unsigned long long)));
+    TRY(cudaMemsetAsync(failed.p, 0, sizeof(unsigned long long), s));
     TRY(launch_mlp_grad(model.as<unsigned char>(), bf.as<__nv_bfloat16>(), lab.as<float>(), nullptr, nullptr, 1, n,
-                        1.0f / (float)n, part.as<float>(), s));
-    TRY(launch_mlp_reduce(part.as<float>(), warps, grad.as<float>(), nullptr, nullptr, nullptr, nullptr, s));
+                        1.0f / (float)n, part.as<float>(), failed.as<unsigned long long>(), s));
+    TRY(launch_mlp_reduce(part.as<float>(), parts, grad.as<float>(), nullptr, nullptr, nullptr, nullptr, s));
     std::vector<float> g(kMlpParams);
+    unsigned long long nFailed = 0;
     TRY(cudaMemcpyAsync(g.data(), grad.p, kMlpParams * sizeof(float), cudaMemcpyDeviceToHost, s));
+    TRY(cudaMemcpyAsync(&nFailed, failed.p, sizeof(nFailed), cudaMemcpyDeviceToHost, s));
     TRY(cudaStreamSynchronize(s));
+    if (nFailed) return CG_ERR_TIMEOUT;
     std::memcpy(grads, g.data(), (kMlpParams - 1) * sizeof(float));
     if (loss_out) *loss_out = g[kMlpParamLoss];
     return CG_OK;

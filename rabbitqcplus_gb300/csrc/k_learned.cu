@@ -6,14 +6,13 @@
 // include/corrector.hpp:1448-1472); the network, its features and its training
 // are this project's own.
 //
-// All three matrix products (forward, the two weight gradients and the hidden
-// gradient) run on the tensor cores with mma.sync.m16n8k16 (BF16 operands,
-// FP32 accumulators).  A warp owns 16 columns (rows of the product): the
-// first layer's accumulators become the second layer's A operand in registers,
-// and the transposed operands of the weight gradients are staged in shared
-// memory.  Training is deterministic: every warp writes its partial gradients
-// to its own slot and one kernel sums the slots in a fixed order before the
-// Adam update.
+// Every matrix product runs on the tcgen05 tensor cores (kind::f16: BF16
+// operands in shared memory, FP32 accumulators in tensor memory).  Inference
+// scores 128 columns per tile; training takes a 128-row tile of a minibatch
+// per block through the forward pass, the hidden gradient and both weight
+// gradients (one product over transposed tiles).  Training is deterministic:
+// every block writes its partial gradients to its own slot and one kernel sums
+// the slots in a fixed order before the Adam update.
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -32,111 +31,6 @@ constexpr unsigned kFull = 0xffffffffu;
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<const uint32_t*>(&v);
-}
-
-__device__ __forceinline__ uint32_t pack_raw(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
-}
-
-// D += A * B, A 16x16 (row), B 16x8 (col), BF16 in, FP32 accumulate
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// Weights staged in shared memory (BF16) with the biases (FP32).
-struct SmemMlp {
-    __nv_bfloat16 w1[kMlpHidden * kMlpFeatures];
-    __nv_bfloat16 w2[kMlpHidden * kMlpHidden];
-    __nv_bfloat16 w3[kMlpHidden];
-    float b1[kMlpHidden], b2[kMlpHidden], b3;
-};
-
-__device__ void stage_weights(SmemMlp& s, const unsigned char* model) {
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(model);
-    uint32_t* dst = reinterpret_cast<uint32_t*>(s.w1);
-    // w1, w2, w3 are contiguous in both layouts
-    constexpr int words = (kMlpHidden * kMlpFeatures + kMlpHidden * kMlpHidden + kMlpHidden) / 2;
-    for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
-    const float* bsrc = reinterpret_cast<const float*>(model + kMlpOffB1);
-    for (int i = threadIdx.x; i < kMlpHidden; i += blockDim.x) {
-        s.b1[i] = bsrc[i];
-        s.b2[i] = bsrc[kMlpHidden + i];
-    }
-    if (threadIdx.x == 0) s.b3 = bsrc[2 * kMlpHidden];
-}
-
-// Forward pass of 16 rows held by one warp.  x(r, f) gives feature f of local
-// row r (BF16).  On return h1/h2 hold the BF16-rounded post-ReLU activations
-// in accumulator layout (tile nt: rows g and g+8, columns nt*8 + 2t, +1) and
-// logit[0]/logit[1] the outputs of rows g and g+8 (the same in all four lanes
-// of a group).
-template <class XF>
-__device__ __forceinline__ void mlp_forward(const SmemMlp& s, XF x, float (&h1)[8][4], float (&h2)[8][4],
-                                            float (&logit)[2]) {
-    const int lane = (int)lane_id();
-    const int g = lane >> 2, t = lane & 3;
-    uint32_t ax[2][4];
-#pragma unroll
-    for (int kc = 0; kc < 2; kc++) {
-        const int c0 = kc * 16 + 2 * t;
-        ax[kc][0] = pack_raw(x(g, c0), x(g, c0 + 1));
-        ax[kc][1] = pack_raw(x(g + 8, c0), x(g + 8, c0 + 1));
-        ax[kc][2] = pack_raw(x(g, c0 + 8), x(g, c0 + 9));
-        ax[kc][3] = pack_raw(x(g + 8, c0 + 8), x(g + 8, c0 + 9));
-    }
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-        const int n = nt * 8 + 2 * t;
-        h1[nt][0] = h1[nt][2] = s.b1[n];
-        h1[nt][1] = h1[nt][3] = s.b1[n + 1];
-#pragma unroll
-        for (int kc = 0; kc < 2; kc++) {
-            const __nv_bfloat16* w = s.w1 + (nt * 8 + g) * kMlpFeatures + kc * 16 + 2 * t;
-            const uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(w), *reinterpret_cast<const uint32_t*>(w + 8)};
-            mma_bf16(h1[nt], ax[kc], b);
-        }
-#pragma unroll
-        for (int i = 0; i < 4; i++) h1[nt][i] = __bfloat162float(__float2bfloat16_rn(fmaxf(h1[nt][i], 0.0f)));
-    }
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-        const int n = nt * 8 + 2 * t;
-        h2[nt][0] = h2[nt][2] = s.b2[n];
-        h2[nt][1] = h2[nt][3] = s.b2[n + 1];
-    }
-#pragma unroll
-    for (int kc = 0; kc < 4; kc++) {
-        const uint32_t a[4] = {pack_bf16(h1[2 * kc][0], h1[2 * kc][1]), pack_bf16(h1[2 * kc][2], h1[2 * kc][3]),
-                               pack_bf16(h1[2 * kc + 1][0], h1[2 * kc + 1][1]),
-                               pack_bf16(h1[2 * kc + 1][2], h1[2 * kc + 1][3])};
-#pragma unroll
-        for (int nt = 0; nt < 8; nt++) {
-            const __nv_bfloat16* w = s.w2 + (nt * 8 + g) * kMlpHidden + kc * 16 + 2 * t;
-            const uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(w), *reinterpret_cast<const uint32_t*>(w + 8)};
-            mma_bf16(h2[nt], a, b);
-        }
-    }
-    float z0 = 0.0f, z1 = 0.0f;
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-#pragma unroll
-        for (int i = 0; i < 4; i++) h2[nt][i] = __bfloat162float(__float2bfloat16_rn(fmaxf(h2[nt][i], 0.0f)));
-        const int n = nt * 8 + 2 * t;
-        const float wa = __bfloat162float(s.w3[n]), wb = __bfloat162float(s.w3[n + 1]);
-        z0 = __fadd_rn(z0, __fadd_rn(__fmul_rn(h2[nt][0], wa), __fmul_rn(h2[nt][1], wb)));
-        z1 = __fadd_rn(z1, __fadd_rn(__fmul_rn(h2[nt][2], wa), __fmul_rn(h2[nt][3], wb)));
-    }
-    // the four lanes of a group hold disjoint columns of the same rows
-    z0 = __fadd_rn(z0, __shfl_xor_sync(kFull, z0, 1));
-    z1 = __fadd_rn(z1, __shfl_xor_sync(kFull, z1, 1));
-    z0 = __fadd_rn(z0, __shfl_xor_sync(kFull, z0, 2));
-    z1 = __fadd_rn(z1, __shfl_xor_sync(kFull, z1, 2));
-    logit[0] = __fadd_rn(z0, s.b3);
-    logit[1] = __fadd_rn(z1, s.b3);
 }
 
 // ---------------------------------------------------------------- inference (tcgen05)
@@ -391,226 +285,310 @@ __global__ void __launch_bounds__(kTcRows) mlp_infer_kernel(const unsigned char*
     }
 }
 
-// ---------------------------------------------------------------- training
+// ---------------------------------------------------------------- training (tcgen05)
+//
+// One block of 128 threads per 128-row tile of the minibatch (thread = row =
+// TMEM lane): the forward pass and every gradient of the mean loss over the
+// tile, as partial sums in part[tile][...] (parameter order of the model: w1,
+// w2, w3, b1, b2, b3, loss) that mlp_reduce_kernel adds in tile order.  The
+// matrix products run on tcgen05.mma (kind::f16, BF16 operands in shared
+// memory in the canonical K-major layout, FP32 accumulators in tensor memory):
+//   forward   D1 = X W1^T, D2 = H1 W2^T                (M = 128 rows)
+//   backward  dH1 = dH2 W2                              (M = 128 rows)
+//             [dW2; dW1] = [dH2^T; dH1^T] [H1^T | X^T]  (one M = 128, N = 96,
+//             K = 128 product: rows 0-63 x columns 0-63 are dW2, rows 64-127
+//             x columns 64-95 are dW1; the cross terms are not read)
+// BF16 rounding at the same points as the oracle (oracle/mlp.py): the
+// features, h1 and h2 after ReLU, dH2 before the products, dH1 before dW1;
+// FP32 elsewhere.  dW3 and the bias gradients are column sums over the tile's
+// rows (warp shuffles, then the four warps in order).
 
-constexpr int kTrainWarps = 4;
+constexpr int kTrainRows = 128;
+constexpr uint32_t kTrainTmemCols = 256;  // D1/D2 (0-127, later [dW2 dW1] at 0-95), dH1 (128-191)
+constexpr int kTrainOutCols = kMlpHidden + kMlpFeatures;  // N of the weight-gradient product
 
-struct TrainSmem {
-    SmemMlp w;
-    __nv_bfloat16 x[kTrainWarps][16][kMlpFeatures];
-    __nv_bfloat16 h1[kTrainWarps][16][kMlpHidden];
-    __nv_bfloat16 d2[kTrainWarps][16][kMlpHidden];
-    __nv_bfloat16 d1[kTrainWarps][16][kMlpHidden];
+// shared memory of one block (every operand tile 1024-byte aligned)
+struct TrainTc {
+    unsigned char xa[kTrainRows * kMlpFeatures * 2];        // A of D1: X [128][32]
+    unsigned char w1[kMlpHidden * kMlpFeatures * 2];        // B of D1: W1 [64][32]
+    unsigned char h1a[kTrainRows * kMlpHidden * 2];         // A of D2: H1 [128][64]
+    unsigned char w2[kMlpHidden * kMlpHidden * 2];          // B of D2: W2 [64 out][64 in]
+    unsigned char d2a[kTrainRows * kMlpHidden * 2];         // A of dH1: dH2 [128][64]
+    unsigned char w2t[kMlpHidden * kMlpHidden * 2];         // B of dH1: W2^T [64 in][64 out]
+    unsigned char gA[kTrainRows * kTrainRows * 2];          // A of [dW2; dW1]: [dH2^T; dH1^T] [128][128 rows]
+    unsigned char gB[kTrainOutCols * kTrainRows * 2];       // B of [dW2; dW1]: [H1^T | X^T] [96][128 rows]
+    float b1[kMlpHidden], b2[kMlpHidden], w3[kMlpHidden];
+    float red[4][3 * kMlpHidden + 2];                       // per-warp column sums: dW3, db2, db1, db3, loss
+    float b3;
+    unsigned long long mbar;
+    uint32_t tmemBase;
 };
 
-// softplus(z) - y*z, the binary cross-entropy of sigmoid(z) against y
-__device__ __forceinline__ float bce_logit(float z, float y) {
-    const float sp = fmaxf(z, 0.0f) + log1pf(expf(-fabsf(z)));
-    return sp - y * z;
-}
-
-// One warp = 16 rows of the minibatch: forward, loss and all gradients of the
-// mean loss over `total` rows; its partial sums go to part[globalWarp][...]
-// in the parameter order of the model (w1, w2, w3, b1, b2, b3, loss).
-// Rows index the feature matrix through `perm` (or directly when null).
-__global__ void __launch_bounds__(kTrainWarps * 32) mlp_grad_kernel(const unsigned char* __restrict__ model,
-                                                                    const __nv_bfloat16* __restrict__ feat,
-                                                                    const float* __restrict__ label,
-                                                                    const uint32_t* __restrict__ perm,
-                                                                    const unsigned long long* stepPtr,
-                                                                    unsigned int stepsPerEpoch, unsigned int rows,
-                                                                    float invTotal, float* __restrict__ part) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    TrainSmem& s = *reinterpret_cast<TrainSmem*>(smraw);
-    stage_weights(s.w, model);
-    const int wi = (int)(threadIdx.x >> 5);
-    const int lane = (int)lane_id();
-    const int g = lane >> 2, t = lane & 3;
-    // first row of this minibatch
+__global__ void __launch_bounds__(kTrainRows, 1) mlp_grad_kernel(const unsigned char* __restrict__ model,
+                                                                 const __nv_bfloat16* __restrict__ feat,
+                                                                 const float* __restrict__ label,
+                                                                 const uint32_t* __restrict__ perm,
+                                                                 const unsigned long long* stepPtr,
+                                                                 unsigned int stepsPerEpoch, unsigned int rows,
+                                                                 float invTotal, float* __restrict__ part,
+                                                                 unsigned long long* failed) {
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    TrainTc& s = *reinterpret_cast<TrainTc*>(smraw);
+    const int tid = (int)threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const __nv_bfloat16* w1g = reinterpret_cast<const __nv_bfloat16*>(model + kMlpOffW1);
+    const __nv_bfloat16* w2g = reinterpret_cast<const __nv_bfloat16*>(model + kMlpOffW2);
+    const __nv_bfloat16* w3g = reinterpret_cast<const __nv_bfloat16*>(model + kMlpOffW3);
+    for (int i = tid; i < kMlpHidden * kMlpFeatures; i += kTrainRows)
+        *reinterpret_cast<__nv_bfloat16*>(s.w1 + core_offset(i / kMlpFeatures, i % kMlpFeatures, kMlpFeatures)) =
+            w1g[i];
+    for (int i = tid; i < kMlpHidden * kMlpHidden; i += kTrainRows) {
+        const int o = i / kMlpHidden, in = i % kMlpHidden;
+        *reinterpret_cast<__nv_bfloat16*>(s.w2 + core_offset(o, in, kMlpHidden)) = w2g[i];
+        *reinterpret_cast<__nv_bfloat16*>(s.w2t + core_offset(in, o, kMlpHidden)) = w2g[i];
+    }
+    const float* bsrc = reinterpret_cast<const float*>(model + kMlpOffB1);
+    if (tid < kMlpHidden) {
+        s.b1[tid] = bsrc[tid];
+        s.b2[tid] = bsrc[kMlpHidden + tid];
+        s.w3[tid] = __bfloat162float(w3g[tid]);
+    }
+    if (tid == 0) {
+        s.b3 = bsrc[2 * kMlpHidden];
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s.mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s.tmemBase)),
+                     "r"(kTrainTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    // this thread's row of the minibatch (zero features past the end)
     const uint64_t base = stepPtr ? (*stepPtr % stepsPerEpoch) * (uint64_t)rows : 0;
-    const unsigned gw = blockIdx.x * kTrainWarps + wi;
-    const unsigned r0 = gw * 16;
-    // stage this warp's 16 rows (zero past the end)
-    for (int i = lane; i < 16 * kMlpFeatures; i += 32) {
-        const int r = i / kMlpFeatures, f = i % kMlpFeatures;
-        const unsigned row = r0 + (unsigned)r;
-        __nv_bfloat16 v = __float2bfloat16_rn(0.0f);
-        if (row < rows) {
-            const uint64_t src = perm ? perm[base + row] : base + row;
-            v = feat[src * kMlpFeatures + f];
+    const unsigned row = blockIdx.x * kTrainRows + (unsigned)tid;
+    const bool valid = row < rows;
+    const uint64_t src = valid ? (perm ? perm[base + row] : base + row) : 0;
+    {
+        uint4 f[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) f[j] = make_uint4(0, 0, 0, 0);
+        if (valid) {
+            const uint4* x = reinterpret_cast<const uint4*>(feat + src * kMlpFeatures);
+#pragma unroll
+            for (int j = 0; j < 4; j++) f[j] = x[j];
         }
-        s.x[wi][r][f] = v;
+#pragma unroll
+        for (int j = 0; j < 4; j++) *reinterpret_cast<uint4*>(s.xa + core_offset(tid, 8 * j, kMlpFeatures)) = f[j];
+        // X^T into rows 64-95 of the weight-gradient B operand (column = this row)
+        const __nv_bfloat16* fv = reinterpret_cast<const __nv_bfloat16*>(f);
+#pragma unroll
+        for (int k = 0; k < kMlpFeatures; k++)
+            *reinterpret_cast<__nv_bfloat16*>(s.gB + core_offset(kMlpHidden + k, tid, kTrainRows)) = fv[k];
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = s.tmemBase;
+    const uint32_t laneAddr = tbase + ((uint32_t)(warp * 32) << 16);
+    const uint32_t mb = smem_u32(&s.mbar);
+    uint32_t phase = 0;
+    bool ok = true;
+    auto wait_mma = [&]() {
+        if (!mbar_wait(mb, phase, kWaitSpins)) ok = false;
+        phase ^= 1u;
+        ok = !__syncthreads_or(!ok);
+        tc_fence_after();
+    };
+    // ---- D1 = X W1^T (TMEM columns 0-63)
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < kMlpFeatures / 16; k++)
+            tc_mma(tbase, smem_desc(smem_u32(s.xa) + 256u * k, 128, 512), smem_desc(smem_u32(s.w1) + 256u * k, 128, 512),
+                   instr_desc(kTrainRows, kMlpHidden), k > 0);
+        tc_commit(mb);
+    }
+    wait_mma();
+    uint64_t h1pos = 0, h2pos = 0;  // ReLU masks of this row
+    if (ok) {
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            float v[32];
+            tc_ld32(laneAddr + 32u * half, v);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                uint32_t w[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int c = 32 * half + 8 * j + 2 * q;
+                    const float a = fmaxf(__fadd_rn(v[8 * j + 2 * q], s.b1[c]), 0.0f);
+                    const float b = fmaxf(__fadd_rn(v[8 * j + 2 * q + 1], s.b1[c + 1]), 0.0f);
+                    h1pos |= (uint64_t)(a > 0.0f) << c;
+                    h1pos |= (uint64_t)(b > 0.0f) << (c + 1);
+                    w[q] = pack_bf16(a, b);
+                }
+                *reinterpret_cast<uint4*>(s.h1a + core_offset(tid, 32 * half + 8 * j, kMlpHidden)) =
+                    make_uint4(w[0], w[1], w[2], w[3]);
+#pragma unroll
+                for (int q = 0; q < 4; q++) {  // H1^T into rows 0-63 of the weight-gradient B operand
+                    const int c = 32 * half + 8 * j + 2 * q;
+                    *reinterpret_cast<uint16_t*>(s.gB + core_offset(c, tid, kTrainRows)) = (uint16_t)(w[q] & 0xffffu);
+                    *reinterpret_cast<uint16_t*>(s.gB + core_offset(c + 1, tid, kTrainRows)) = (uint16_t)(w[q] >> 16);
+                }
+            }
+        }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    // ---- D2 = H1 W2^T (TMEM columns 64-127)
+    if (ok && tid == 0) {
+#pragma unroll
+        for (int k = 0; k < kMlpHidden / 16; k++)
+            tc_mma(tbase + kMlpHidden, smem_desc(smem_u32(s.h1a) + 256u * k, 128, 1024),
+                   smem_desc(smem_u32(s.w2) + 256u * k, 128, 1024), instr_desc(kTrainRows, kMlpHidden), k > 0);
+        tc_commit(mb);
+    }
+    if (ok) wait_mma();
+    // output layer, loss, dH2
+    float h2[kMlpHidden];
+    float dz = 0.0f, loss = 0.0f;
+    if (ok) {
+        float z = 0.0f;
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            float v[32];
+            tc_ld32(laneAddr + (uint32_t)kMlpHidden + 32u * half, v);
+#pragma unroll
+            for (int i = 0; i < 32; i++) {
+                const int c = 32 * half + i;
+                const float r = fmaxf(__fadd_rn(v[i], s.b2[c]), 0.0f);
+                h2pos |= (uint64_t)(r > 0.0f) << c;
+                h2[c] = __bfloat162float(__float2bfloat16_rn(r));
+                z = __fadd_rn(z, __fmul_rn(h2[c], s.w3[c]));
+            }
+        }
+        z = __fadd_rn(z, s.b3);
+        if (valid) {
+            const float y = label[src];
+            const float pr = 1.0f / (1.0f + expf(-z));
+            dz = (pr - y) * invTotal;
+            const float sp = fmaxf(z, 0.0f) + log1pf(expf(-fabsf(z)));
+            loss = (sp - y * z) * invTotal;
+        }
+    }
+    // column sums over the block's rows: four warps' shuffle sums, then in warp order
+    auto colsum = [&](float v, int slot) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = __fadd_rn(v, __shfl_xor_sync(kFull, v, o));
+        if (lane == 0) s.red[warp][slot] = v;
+    };
+    if (ok) {
+#pragma unroll 4
+        for (int c = 0; c < kMlpHidden; c++) {
+            const float d2 = (h2pos >> c) & 1ull ? __fmul_rn(dz, s.w3[c]) : 0.0f;
+            colsum(__fmul_rn(dz, h2[c]), c);           // dW3
+            colsum(d2, kMlpHidden + c);                 // db2
+            const __nv_bfloat16 b = __float2bfloat16_rn(d2);
+            *reinterpret_cast<__nv_bfloat16*>(s.d2a + core_offset(tid, c, kMlpHidden)) = b;
+            *reinterpret_cast<__nv_bfloat16*>(s.gA + core_offset(c, tid, kTrainRows)) = b;  // dH2^T, rows 0-63
+        }
+        colsum(dz, 3 * kMlpHidden);      // db3
+        colsum(loss, 3 * kMlpHidden + 1);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    // ---- dH1 = dH2 W2 (TMEM columns 128-191)
+    if (ok && tid == 0) {
+#pragma unroll
+        for (int k = 0; k < kMlpHidden / 16; k++)
+            tc_mma(tbase + 2 * kMlpHidden, smem_desc(smem_u32(s.d2a) + 256u * k, 128, 1024),
+                   smem_desc(smem_u32(s.w2t) + 256u * k, 128, 1024), instr_desc(kTrainRows, kMlpHidden), k > 0);
+        tc_commit(mb);
+    }
+    if (ok) wait_mma();
+    if (ok) {
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            float v[32];
+            tc_ld32(laneAddr + 2u * kMlpHidden + 32u * half, v);
+#pragma unroll 4
+            for (int i = 0; i < 32; i++) {
+                const int c = 32 * half + i;
+                const float d1 = (h1pos >> c) & 1ull ? v[i] : 0.0f;
+                colsum(d1, 2 * kMlpHidden + c);  // db1
+                *reinterpret_cast<__nv_bfloat16*>(s.gA + core_offset(kMlpHidden + c, tid, kTrainRows)) =
+                    __float2bfloat16_rn(d1);  // dH1^T, rows 64-127
+            }
+        }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    // ---- [dW2; dW1] = [dH2^T; dH1^T] [H1^T | X^T] (TMEM columns 0-95; D1 and D2 were read)
+    if (ok && tid == 0) {
+#pragma unroll
+        for (int k = 0; k < kTrainRows / 16; k++)
+            tc_mma(tbase, smem_desc(smem_u32(s.gA) + 256u * k, 128, 2048), smem_desc(smem_u32(s.gB) + 256u * k, 128, 2048),
+                   instr_desc(kTrainRows, kTrainOutCols), k > 0);
+        tc_commit(mb);
+    }
+    if (ok) wait_mma();
+    float* out = part + (uint64_t)blockIdx.x * kMlpParams;
+    if (ok) {
+        if (tid < kMlpHidden) {  // row o of dW2: columns 0-63
+#pragma unroll
+            for (int half = 0; half < 2; half++) {
+                float v[32];
+                tc_ld32(laneAddr + 32u * half, v);
+#pragma unroll
+                for (int i = 0; i < 32; i++) out[kMlpOffW2 / 2 + tid * kMlpHidden + 32 * half + i] = v[i];
+            }
+        } else {  // row i of dW1: columns 64-95
+            float v[32];
+            tc_ld32(laneAddr + (uint32_t)kMlpHidden, v);
+#pragma unroll
+            for (int f = 0; f < kMlpFeatures; f++) out[kMlpOffW1 / 2 + (tid - kMlpHidden) * kMlpFeatures + f] = v[f];
+        }
     }
     __syncthreads();
-    auto x = [&](int r, int f) -> __nv_bfloat16 { return s.x[wi][r][f]; };
-    float h1[8][4], h2[8][4], z[2];
-    mlp_forward(s.w, x, h1, h2, z);
-
-    float dz[2] = {0.0f, 0.0f}, loss = 0.0f;
-#pragma unroll
-    for (int half = 0; half < 2; half++) {
-        const unsigned row = r0 + (unsigned)(g + 8 * half);
-        if (row < rows) {
-            const uint64_t src = perm ? perm[base + row] : base + row;
-            const float y = label[src];
-            const float p = 1.0f / (1.0f + expf(-z[half]));
-            dz[half] = (p - y) * invTotal;
-            if (t == 0) loss += bce_logit(z[half], y) * invTotal;
+    if (ok) {
+        for (int i = tid; i < 3 * kMlpHidden + 2; i += kTrainRows) {
+            const float v = __fadd_rn(__fadd_rn(__fadd_rn(s.red[0][i], s.red[1][i]), s.red[2][i]), s.red[3][i]);
+            int dst;
+            if (i < kMlpHidden) dst = kMlpOffW3 / 2 + i;
+            else if (i < 2 * kMlpHidden) dst = kMlpParamB2 + (i - kMlpHidden);
+            else if (i < 3 * kMlpHidden) dst = kMlpParamB1 + (i - 2 * kMlpHidden);
+            else if (i == 3 * kMlpHidden) dst = kMlpParamB3;
+            else dst = kMlpParamLoss;
+            out[dst] = v;
         }
+    } else {
+        for (int i = tid; i < kMlpParams; i += kTrainRows) out[i] = 0.0f;
+        if (tid == 0 && failed) atomicAdd(failed, 1ull);
+        mbar_wait(mb, phase ^ 1u, kWaitSpins);  // the MMAs in flight, bounded again
     }
-    float* out = part + (uint64_t)gw * kMlpParams;
-    // output layer: dW3, db3; hidden 2 gradient dH2 = dz * w3 * relu'(h2)
-    float d2[8][4];
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-        const int n = nt * 8 + 2 * t;
-        const float wa = __bfloat162float(s.w.w3[n]), wb = __bfloat162float(s.w.w3[n + 1]);
-        float ga = __fadd_rn(__fmul_rn(dz[0], h2[nt][0]), __fmul_rn(dz[1], h2[nt][2]));
-        float gb = __fadd_rn(__fmul_rn(dz[0], h2[nt][1]), __fmul_rn(dz[1], h2[nt][3]));
-        // sum over the 8 groups (lanes with the same t)
-#pragma unroll
-        for (int o = 4; o < 32; o <<= 1) {
-            ga = __fadd_rn(ga, __shfl_xor_sync(kFull, ga, o));
-            gb = __fadd_rn(gb, __shfl_xor_sync(kFull, gb, o));
-        }
-        if (g == 0) {
-            out[kMlpOffW3 / 2 + n] = ga;
-            out[kMlpOffW3 / 2 + n + 1] = gb;
-        }
-        d2[nt][0] = h2[nt][0] > 0.0f ? __fmul_rn(dz[0], wa) : 0.0f;
-        d2[nt][1] = h2[nt][1] > 0.0f ? __fmul_rn(dz[0], wb) : 0.0f;
-        d2[nt][2] = h2[nt][2] > 0.0f ? __fmul_rn(dz[1], wa) : 0.0f;
-        d2[nt][3] = h2[nt][3] > 0.0f ? __fmul_rn(dz[1], wb) : 0.0f;
-    }
-    {
-        float db3 = __fadd_rn(dz[0], dz[1]);
-        db3 = __fadd_rn(db3, __shfl_xor_sync(kFull, db3, 4));
-        db3 = __fadd_rn(db3, __shfl_xor_sync(kFull, db3, 8));
-        db3 = __fadd_rn(db3, __shfl_xor_sync(kFull, db3, 16));
-        float l = loss;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) l = __fadd_rn(l, __shfl_xor_sync(kFull, l, o));
-        if (lane == 0) {
-            out[kMlpParamB3] = db3;
-            out[kMlpParamLoss] = l;
-        }
-    }
-    // db2 = column sums of dH2 (FP32); stage BF16 dH2 and h1 for the transposed products
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-        const int n = nt * 8 + 2 * t;
-        float sa = __fadd_rn(d2[nt][0], d2[nt][2]), sb = __fadd_rn(d2[nt][1], d2[nt][3]);
-#pragma unroll
-        for (int o = 4; o < 32; o <<= 1) {
-            sa = __fadd_rn(sa, __shfl_xor_sync(kFull, sa, o));
-            sb = __fadd_rn(sb, __shfl_xor_sync(kFull, sb, o));
-        }
-        if (g == 0) {
-            out[kMlpParamB2 + n] = sa;
-            out[kMlpParamB2 + n + 1] = sb;
-        }
-        s.d2[wi][g][n] = __float2bfloat16_rn(d2[nt][0]);
-        s.d2[wi][g][n + 1] = __float2bfloat16_rn(d2[nt][1]);
-        s.d2[wi][g + 8][n] = __float2bfloat16_rn(d2[nt][2]);
-        s.d2[wi][g + 8][n + 1] = __float2bfloat16_rn(d2[nt][3]);
-        s.h1[wi][g][n] = __float2bfloat16_rn(h1[nt][0]);
-        s.h1[wi][g][n + 1] = __float2bfloat16_rn(h1[nt][1]);
-        s.h1[wi][g + 8][n] = __float2bfloat16_rn(h1[nt][2]);
-        s.h1[wi][g + 8][n + 1] = __float2bfloat16_rn(h1[nt][3]);
-    }
-    __syncwarp();
-    // dH1 = (dH2 W2) * relu'(h1): A = dH2 (16 x 64), B[k=j][n=i] = W2[j][i]
-    float d1[8][4];
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) d1[nt][0] = d1[nt][1] = d1[nt][2] = d1[nt][3] = 0.0f;
-#pragma unroll
-    for (int kc = 0; kc < 4; kc++) {
-        const int c0 = kc * 16 + 2 * t;
-        const uint32_t a[4] = {pack_raw(s.d2[wi][g][c0], s.d2[wi][g][c0 + 1]),
-                               pack_raw(s.d2[wi][g + 8][c0], s.d2[wi][g + 8][c0 + 1]),
-                               pack_raw(s.d2[wi][g][c0 + 8], s.d2[wi][g][c0 + 9]),
-                               pack_raw(s.d2[wi][g + 8][c0 + 8], s.d2[wi][g + 8][c0 + 9])};
-#pragma unroll
-        for (int nt = 0; nt < 8; nt++) {
-            const int col = nt * 8 + g;
-            const uint32_t b[2] = {pack_raw(s.w.w2[c0 * kMlpHidden + col], s.w.w2[(c0 + 1) * kMlpHidden + col]),
-                                   pack_raw(s.w.w2[(c0 + 8) * kMlpHidden + col], s.w.w2[(c0 + 9) * kMlpHidden + col])};
-            mma_bf16(d1[nt], a, b);
-        }
-    }
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-        const int n = nt * 8 + 2 * t;
-#pragma unroll
-        for (int i = 0; i < 4; i++) d1[nt][i] = h1[nt][i] > 0.0f ? d1[nt][i] : 0.0f;
-        float sa = __fadd_rn(d1[nt][0], d1[nt][2]), sb = __fadd_rn(d1[nt][1], d1[nt][3]);
-#pragma unroll
-        for (int o = 4; o < 32; o <<= 1) {
-            sa = __fadd_rn(sa, __shfl_xor_sync(kFull, sa, o));
-            sb = __fadd_rn(sb, __shfl_xor_sync(kFull, sb, o));
-        }
-        if (g == 0) {
-            out[kMlpParamB1 + n] = sa;
-            out[kMlpParamB1 + n + 1] = sb;
-        }
-        s.d1[wi][g][n] = __float2bfloat16_rn(d1[nt][0]);
-        s.d1[wi][g][n + 1] = __float2bfloat16_rn(d1[nt][1]);
-        s.d1[wi][g + 8][n] = __float2bfloat16_rn(d1[nt][2]);
-        s.d1[wi][g + 8][n + 1] = __float2bfloat16_rn(d1[nt][3]);
-    }
-    __syncwarp();
-    // dW2[j][i] = sum_r dH2[r][j] h1[r][i]: A[m=j][k=r] = dH2[r][j], B[k=r][n=i] = h1[r][i]
-    // dW1[i][f] = sum_r dH1[r][i] x[r][f]:  A[m=i][k=r] = dH1[r][i], B[k=r][n=f] = x[r][f]
-#pragma unroll
-    for (int mt = 0; mt < 4; mt++) {
-        const int m = mt * 16 + g;
-        const uint32_t a2[4] = {pack_raw(s.d2[wi][2 * t][m], s.d2[wi][2 * t + 1][m]),
-                                pack_raw(s.d2[wi][2 * t][m + 8], s.d2[wi][2 * t + 1][m + 8]),
-                                pack_raw(s.d2[wi][2 * t + 8][m], s.d2[wi][2 * t + 9][m]),
-                                pack_raw(s.d2[wi][2 * t + 8][m + 8], s.d2[wi][2 * t + 9][m + 8])};
-        const uint32_t a1[4] = {pack_raw(s.d1[wi][2 * t][m], s.d1[wi][2 * t + 1][m]),
-                                pack_raw(s.d1[wi][2 * t][m + 8], s.d1[wi][2 * t + 1][m + 8]),
-                                pack_raw(s.d1[wi][2 * t + 8][m], s.d1[wi][2 * t + 9][m]),
-                                pack_raw(s.d1[wi][2 * t + 8][m + 8], s.d1[wi][2 * t + 9][m + 8])};
-#pragma unroll
-        for (int nt = 0; nt < 8; nt++) {
-            const int col = nt * 8 + g;
-            const uint32_t b[2] = {pack_raw(s.h1[wi][2 * t][col], s.h1[wi][2 * t + 1][col]),
-                                   pack_raw(s.h1[wi][2 * t + 8][col], s.h1[wi][2 * t + 9][col])};
-            float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            mma_bf16(acc, a2, b);
-            const int n = nt * 8 + 2 * t;
-            out[kMlpOffW2 / 2 + m * kMlpHidden + n] = acc[0];
-            out[kMlpOffW2 / 2 + m * kMlpHidden + n + 1] = acc[1];
-            out[kMlpOffW2 / 2 + (m + 8) * kMlpHidden + n] = acc[2];
-            out[kMlpOffW2 / 2 + (m + 8) * kMlpHidden + n + 1] = acc[3];
-        }
-#pragma unroll
-        for (int nt = 0; nt < 4; nt++) {
-            const int col = nt * 8 + g;
-            const uint32_t b[2] = {pack_raw(s.x[wi][2 * t][col], s.x[wi][2 * t + 1][col]),
-                                   pack_raw(s.x[wi][2 * t + 8][col], s.x[wi][2 * t + 9][col])};
-            float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            mma_bf16(acc, a1, b);
-            const int n = nt * 8 + 2 * t;
-            out[kMlpOffW1 / 2 + m * kMlpFeatures + n] = acc[0];
-            out[kMlpOffW1 / 2 + m * kMlpFeatures + n + 1] = acc[1];
-            out[kMlpOffW1 / 2 + (m + 8) * kMlpFeatures + n] = acc[2];
-            out[kMlpOffW1 / 2 + (m + 8) * kMlpFeatures + n + 1] = acc[3];
-        }
-    }
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(kTrainTmemCols)
+                     : "memory");
 }
 
-// One thread per parameter: the sum of the warps' partials in warp order, then
+// One thread per parameter: the sum of the tiles' partials in tile order, then
 // (with `state`) an Adam step on the FP32 master copy and the BF16/FP32 model
 // the kernels read.  Thread kMlpParamLoss sums the loss into `lossOut`.
-__global__ void mlp_reduce_kernel(const float* __restrict__ part, unsigned int warps, float* __restrict__ grad,
+__global__ void mlp_reduce_kernel(const float* __restrict__ part, unsigned int parts, float* __restrict__ grad,
                                   float* lossOut, MlpAdam* state, unsigned char* model,
                                   unsigned long long* stepPtr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kMlpParams) return;
     float sum = 0.0f;
-    for (unsigned w = 0; w < warps; w++) sum = __fadd_rn(sum, part[(uint64_t)w * kMlpParams + i]);
+    for (unsigned w = 0; w < parts; w++) sum = __fadd_rn(sum, part[(uint64_t)w * kMlpParams + i]);
     if (grad) grad[i] = sum;
     if (i == kMlpParamLoss) {
         if (lossOut) lossOut[stepPtr ? *stepPtr : 0] = sum;
@@ -649,7 +627,7 @@ __global__ void to_bf16_kernel(const float* __restrict__ in, uint64_t n, __nv_bf
 
 }  // namespace
 
-size_t mlp_grad_smem_bytes() { return sizeof(TrainSmem); }
+size_t mlp_grad_smem_bytes() { return sizeof(TrainTc) + 1024; }
 
 cudaError_t launch_mlp_infer(const unsigned char* model, const __nv_bfloat16* feat, const uint2* meta,
                              const unsigned int* countPtr, unsigned int count, unsigned int cap, float minLogit,
@@ -667,25 +645,22 @@ cudaError_t set_classifier_wait_limit(uint32_t polls) {
 
 cudaError_t launch_mlp_grad(const unsigned char* model, const __nv_bfloat16* feat, const float* label,
                             const uint32_t* perm, const unsigned long long* stepPtr, unsigned int stepsPerEpoch,
-                            unsigned int rows, float invTotal, float* part, cudaStream_t s) {
-    const size_t smem = sizeof(TrainSmem);
+                            unsigned int rows, float invTotal, float* part, unsigned long long* failed,
+                            cudaStream_t s) {
+    const size_t smem = mlp_grad_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const unsigned warps = (rows + 15) / 16;
-    const unsigned blocks = (warps + kTrainWarps - 1) / kTrainWarps;
-    mlp_grad_kernel<<<blocks, kTrainWarps * 32, smem, s>>>(model, feat, label, perm, stepPtr,
-                                                           stepsPerEpoch ? stepsPerEpoch : 1u, rows, invTotal, part);
+    mlp_grad_kernel<<<mlp_grad_parts(rows), kTrainRows, smem, s>>>(model, feat, label, perm, stepPtr,
+                                                                   stepsPerEpoch ? stepsPerEpoch : 1u, rows, invTotal,
+                                                                   part, failed);
     return cudaGetLastError();
 }
 
-unsigned int mlp_grad_warps(unsigned int rows) {
-    const unsigned warps = (rows + 15) / 16;
-    return (warps + kTrainWarps - 1) / kTrainWarps * kTrainWarps;
-}
+unsigned int mlp_grad_parts(unsigned int rows) { return (rows + kTrainRows - 1) / kTrainRows; }
 
-cudaError_t launch_mlp_reduce(const float* part, unsigned int warps, float* grad, float* lossOut, MlpAdam* state,
+cudaError_t launch_mlp_reduce(const float* part, unsigned int parts, float* grad, float* lossOut, MlpAdam* state,
                               unsigned char* model, unsigned long long* stepPtr, cudaStream_t s) {
-    mlp_reduce_kernel<<<(kMlpParams + 255) / 256, 256, 0, s>>>(part, warps, grad, lossOut, state, model, stepPtr);
+    mlp_reduce_kernel<<<(kMlpParams + 255) / 256, 256, 0, s>>>(part, parts, grad, lossOut, state, model, stepPtr);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !stepPtr) return e;
     mlp_step_kernel<<<1, 1, 0, s>>>(state, stepPtr);

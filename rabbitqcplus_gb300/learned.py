@@ -137,8 +137,8 @@ def main(argv=None):
     t.add_argument("--out", default=DEFAULT_MODEL)
     t.add_argument("--columns", type=int, default=5_000_000)
     t.add_argument("--genome", type=int, default=10_000_000)
-    t.add_argument("--grid", default="4:2e-3,8:1e-3,16:1e-3,16:5e-4",
-                   help="epochs:learning-rate pairs; the one with the lowest validation loss is kept")
+    t.add_argument("--grid", default="4:2e-3,8:1e-3,16:1e-3,16:5e-4,24:1e-3,32:7e-4,16:1e-3:2,16:1e-3:3",
+                   help="epochs:learning-rate[:seed] settings; the one with the lowest validation loss is kept")
     t.add_argument("--batch", type=int, default=4096)
     t.add_argument("--seed", type=int, default=1)
     t.add_argument("--validation-seed", type=int, default=1004)
@@ -153,7 +153,7 @@ def main(argv=None):
     args = ap.parse_args(argv)
     if args.cmd == "train":
         t0 = time.time()
-        f, y = training_set(args.columns, args.genome)
+        f, y = training_set(args.columns, args.genome, log=lambda m: print(m, file=sys.stderr))
         rv = sim.SimReads(sim.scaled("c3_10mbp_varlen", args.genome, seed=args.validation_seed))
         fv, yv = collect(rv)
         rv.close()
@@ -161,13 +161,14 @@ def main(argv=None):
         runs = []
         best = None
         for item in args.grid.split(","):
-            ep, lr = item.split(":")
-            o = capi.TrainOptions.defaults(epochs=int(ep), batch_rows=args.batch, learning_rate=float(lr),
-                                           seed=args.seed)
+            parts = item.split(":")
+            ep, lr = int(parts[0]), float(parts[1])
+            seed = int(parts[2]) if len(parts) > 2 else args.seed
+            o = capi.TrainOptions.defaults(epochs=ep, batch_rows=args.batch, learning_rate=lr, seed=seed)
             model, losses = capi.train_classifier(f, y, o)
             vl = log_loss(model, fv, yv)
-            runs.append({"epochs": int(ep), "learning_rate": float(lr), "steps": int(len(losses)),
-                         "train_loss_last_epoch": float(losses[-max(len(losses) // int(ep), 1):].mean()),
+            runs.append({"epochs": ep, "learning_rate": lr, "seed": seed, "steps": int(len(losses)),
+                         "train_loss_last_epoch": float(losses[-max(len(losses) // ep, 1):].mean()),
                          "validation_loss": vl})
             if best is None or vl < best[0]:
                 best = (vl, model, runs[-1])
