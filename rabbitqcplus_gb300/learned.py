@@ -42,12 +42,18 @@ def options(reads: sim.SimReads, correction_type: int, **kw) -> capi.CareOptions
 
 
 def collect(reads: sim.SimReads, **kw):
-    """Columns of the learned decision with their truth labels."""
+    """Columns of the learned decision with their truth labels, in (anchor, position) order.
+
+    The device records columns in an unspecified order; sorting them makes a
+    training run (minibatch order drawn from its seed) reproducible.
+    """
     g = capi.CareGpu(options(reads, capi.CG_CORR_LEARNED, **kw))
     g.append_reads(reads.sequences, reads.offsets)
     g.build_tables()
     feats, anchors, pos, cons = g.columns()
     g.close()
+    order = np.lexsort((pos, anchors))
+    feats, anchors, pos, cons = feats[order], anchors[order], pos[order], cons[order]
     idx = reads.offsets.astype(np.int64)[anchors.astype(np.int64)] + pos.astype(np.int64)
     labels = (reads.truth[idx] == cons).astype(np.uint8)
     return feats, labels
