@@ -510,6 +510,12 @@ __device__ __forceinline__ void seq_scan_fast(uint32_t (&S)[2][MAXW + 1], const 
                 }
             }
         };
+        // The fast tests only mark the shifts that pass (bit bb of `pass`);
+        // the steps run after the group's tests, each lane's in shift order.
+        // The tests do not depend on the best score, so this is the
+        // reference's sequence of steps, and lanes that pass at different
+        // shifts take their steps together instead of one shift at a time.
+        uint32_t pass = 0u;
         // shifts where the lanes' tiers differ: each lane tests its own
         // (selected, not branched on, so the lanes stay together)
         auto mixed = [&](int e) {
@@ -517,7 +523,7 @@ __device__ __forceinline__ void seq_scan_fast(uint32_t (&S)[2][MAXW + 1], const 
                 const int sl = base + bb;
                 const bool two = sl <= slFast, one = sl <= slFast1;
                 const int m = __popc(diff(bb, 0)) + (two ? __popc(diff(bb, 1)) : 0);
-                if (m < (two ? tabMax : one ? tab63 : 0x7fffffff)) step(bb);
+                pass |= (uint32_t)(m < (two ? tabMax : one ? tab63 : 0x7fffffff)) << bb;
             }
         };
         {  // all lanes: two words
@@ -526,12 +532,10 @@ __device__ __forceinline__ void seq_scan_fast(uint32_t (&S)[2][MAXW + 1], const 
                 for (; bb + 1 < e; bb += 2) {
                     const int ma = __popc(diff(bb, 0)) + __popc(diff(bb, 1));
                     const int mb = __popc(diff(bb + 1, 0)) + __popc(diff(bb + 1, 1));
-                    if (ma < tabMax) step(bb);
-                    if (mb < tabMax) step(bb + 1);
+                    pass |= ((uint32_t)(ma < tabMax) | ((uint32_t)(mb < tabMax) << 1)) << bb;
                 }
             }
-            for (; bb < e; bb++)
-                if (__popc(diff(bb, 0)) + __popc(diff(bb, 1)) < tabMax) step(bb);
+            for (; bb < e; bb++) pass |= (uint32_t)(__popc(diff(bb, 0)) + __popc(diff(bb, 1)) < tabMax) << bb;
         }
         mixed(min(ge, max(bb, fastAny + 1 - base)));
         {  // all lanes: one word
@@ -539,14 +543,19 @@ __device__ __forceinline__ void seq_scan_fast(uint32_t (&S)[2][MAXW + 1], const 
             if (MAXW <= 5) {  // two shifts per iteration
                 for (; bb + 1 < e; bb += 2) {
                     const int ma = __popc(diff(bb, 0)), mb = __popc(diff(bb + 1, 0));
-                    if (ma < tab63) step(bb);
-                    if (mb < tab63) step(bb + 1);
+                    pass |= ((uint32_t)(ma < tab63) | ((uint32_t)(mb < tab63) << 1)) << bb;
                 }
             }
-            for (; bb < e; bb++)
-                if (__popc(diff(bb, 0)) < tab63) step(bb);
+            for (; bb < e; bb++) pass |= (uint32_t)(__popc(diff(bb, 0)) < tab63) << bb;
         }
         mixed(ge);
+        while (__any_sync(lanes, pass != 0u)) {
+            if (pass != 0u) {
+                const int q = __ffs(pass) - 1;
+                pass &= pass - 1u;
+                step(q);
+            }
+        }
 #pragma unroll
         for (int k = 0; k < MAXW; k++) {
             S[0][k] = S[0][k + 1];
