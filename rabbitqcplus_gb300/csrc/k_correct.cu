@@ -510,12 +510,15 @@ __device__ __forceinline__ void seq_scan_fast(uint32_t (&S)[2][MAXW + 1], const 
                 }
             }
         };
-        // The fast tests only mark the shifts that pass (bit bb of `pass`);
-        // the steps run after the group's tests, each lane's in shift order.
+        // The fast tests only record whether each shift passes (shifted into
+        // `pass` from the bottom, so the group's last shift is bit 0); the
+        // steps run after the group's tests, each lane's in shift order.
         // The tests do not depend on the best score, so this is the
         // reference's sequence of steps, and lanes that pass at different
         // shifts take their steps together instead of one shift at a time.
         uint32_t pass = 0u;
+        // x < 0: the shift passes (its sign bit moves into pass)
+        auto record = [&](int x) { pass = __funnelshift_l((uint32_t)x, pass, 1); };
         // shifts where the lanes' tiers differ: each lane tests its own
         // (selected, not branched on, so the lanes stay together)
         auto mixed = [&](int e) {
@@ -523,37 +526,39 @@ __device__ __forceinline__ void seq_scan_fast(uint32_t (&S)[2][MAXW + 1], const 
                 const int sl = base + bb;
                 const bool two = sl <= slFast, one = sl <= slFast1;
                 const int m = __popc(diff(bb, 0)) + (two ? __popc(diff(bb, 1)) : 0);
-                pass |= (uint32_t)(m < (two ? tabMax : one ? tab63 : 0x7fffffff)) << bb;
+                record(m - (two ? tabMax : one ? tab63 : 0x7fffffff));
             }
         };
         {  // all lanes: two words
             const int e = min(ge, fastAll + 1 - base);
             if (MAXW <= 5) {  // two shifts per iteration: independent tests, steps in order
                 for (; bb + 1 < e; bb += 2) {
-                    const int ma = __popc(diff(bb, 0)) + __popc(diff(bb, 1));
-                    const int mb = __popc(diff(bb + 1, 0)) + __popc(diff(bb + 1, 1));
-                    pass |= ((uint32_t)(ma < tabMax) | ((uint32_t)(mb < tabMax) << 1)) << bb;
+                    const int ma = __popc(diff(bb, 0)) + __popc(diff(bb, 1)) - tabMax;
+                    const int mb = __popc(diff(bb + 1, 0)) + __popc(diff(bb + 1, 1)) - tabMax;
+                    record(ma);
+                    record(mb);
                 }
             }
-            for (; bb < e; bb++) pass |= (uint32_t)(__popc(diff(bb, 0)) + __popc(diff(bb, 1)) < tabMax) << bb;
+            for (; bb < e; bb++) record(__popc(diff(bb, 0)) + __popc(diff(bb, 1)) - tabMax);
         }
         mixed(min(ge, max(bb, fastAny + 1 - base)));
         {  // all lanes: one word
             const int e = min(ge, fast1All + 1 - base);
             if (MAXW <= 5) {  // two shifts per iteration
                 for (; bb + 1 < e; bb += 2) {
-                    const int ma = __popc(diff(bb, 0)), mb = __popc(diff(bb + 1, 0));
-                    pass |= ((uint32_t)(ma < tab63) | ((uint32_t)(mb < tab63) << 1)) << bb;
+                    const int ma = __popc(diff(bb, 0)) - tab63, mb = __popc(diff(bb + 1, 0)) - tab63;
+                    record(ma);
+                    record(mb);
                 }
             }
-            for (; bb < e; bb++) pass |= (uint32_t)(__popc(diff(bb, 0)) < tab63) << bb;
+            for (; bb < e; bb++) record(__popc(diff(bb, 0)) - tab63);
         }
         mixed(ge);
         while (__any_sync(lanes, pass != 0u)) {
             if (pass != 0u) {
-                const int q = __ffs(pass) - 1;
-                pass &= pass - 1u;
-                step(q);
+                const int q = 31 - __clz(pass);  // the earliest shift left
+                pass ^= 1u << q;
+                step(ge - 1 - q);
             }
         }
 #pragma unroll
