@@ -69,16 +69,16 @@ from rabbitqcplus_gb300 import capi, learned, shard, sim  # noqa: E402
 METRIC = "corrected reads/s on 1 GB300: plain vs batched+learned, at equal TP/FP vs truth"
 UNIT = "reads/s"
 WINDOW = 4_194_304  # anchors per step
-# DRAM bytes (read + write) of align_lane_kernel per candidate and its warp
-# instructions per candidate, measured by ncu on one 65536-anchor launch of the
-# 100M-read workload's shape at 20 Mbp (profiles/top3_kernels_c4_shape_20mbp.md:
-# 632.2 MB and 1.15833e9 warp instructions for the launch's 3.3555M candidates,
-# the run's average from its own counters).  On the 2M-read workload with
-# repeats the instructions per candidate are the same (1.28639e9 for 3.777M,
-# profiles/align_lane_kernel_c1_2mbp.md) but the DRAM bytes far fewer (24.6 B:
-# candidates shared by the anchors of a batch hit in L2 there).
-ALIGN_DRAM_BYTES_PER_CANDIDATE = 632.2e6 / 3.3555e6
-ALIGN_WARP_INST_PER_CANDIDATE = 1.15833e9 / 3.3555e6
+# DRAM bytes (read + write) of align_lane_kernel per candidate, its warp
+# instructions per candidate and its ALU pipe activity, measured by ncu on one
+# 65536-anchor launch of the 100M-read workload's shape at 20 Mbp
+# (profiles/top3_kernels_c4_shape_20mbp.md: 624.8 MB and 9.08779e8 warp
+# instructions for the launch's 3.3555M candidates, ALU pipe 84.7% active).
+# On the 2M-read workload with repeats the DRAM bytes per candidate are far
+# fewer (candidates shared by the anchors of a batch hit in L2 there).
+ALIGN_DRAM_BYTES_PER_CANDIDATE = 624.8e6 / 3.3555e6
+ALIGN_WARP_INST_PER_CANDIDATE = 9.08779e8 / 3.3555e6
+ALIGN_ALU_PIPE_ACTIVE = 0.847
 # STEP2 speed of the oracle (the port) over the reference's own build, both on
 # 8 threads of an Intel Xeon @ 2.70 GHz, 2M-read 150 bp workload with repeats,
 # outputs byte-identical (python oracle/port_speed.py --threads 8): the port
@@ -502,6 +502,7 @@ def main():
             roof["int"] = {"bound": "int-issue", "achieved": inst / dur / 1e9, "peak": peak_i / 1e9,
                            "unit": "G warp-instructions/s", "frac": inst / dur / peak_i, "sm_mhz": mhz,
                            "warp_instructions_per_candidate": ALIGN_WARP_INST_PER_CANDIDATE,
+                           "alu_pipe_active_ncu": ALIGN_ALU_PIPE_ACTIVE,
                            "source": "smsp__inst_executed.sum per candidate from ncu "
                                      "(profiles/top3_kernels_c4_shape_20mbp.md) x candidates of an average launch"}
         return roof
