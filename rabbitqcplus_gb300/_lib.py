@@ -37,6 +37,7 @@ NVCCFLAGS = ["-O3", "-std=c++17", ARCH, "-lineinfo", "--fmad=false", "-prec-div=
 GPU_CU_SOURCES = [
     "k_store.cu",
     "k_tables.cu",
+    "k_sort.cu",
     "k_correct.cu",
     "k_learned.cu",
     "care_capi.cu",

@@ -312,17 +312,6 @@ int fail(cg_ctx* c, int code, const char* fmt, ...) {
         }                                                                                               \
     } while (0)
 
-// kernels one exclusive scan of n elements launches
-uint64_t scan_launches(uint64_t n) {
-    uint64_t k = 0;
-    while (true) {
-        const uint64_t tiles = (n + 4095) / 4096;
-        if (tiles <= 1) return k + 1;
-        k += 2;
-        n = tiles;
-    }
-}
-
 uint64_t pow2_at_least(uint64_t x) {
     uint64_t p = 1;
     while (p < x) p <<= 1;
@@ -500,18 +489,20 @@ int build_tables(cg_ctx* c) {
     CG_CUDA(c, c->sig.ensure(n * c->nmaps * sizeof(unsigned long long)));
     StoreArg st = store_arg(c);
     CG_CUDA(c, launch_signatures(st, c->k, c->nmaps, c->sig.as<unsigned long long>(), c->stream));
-    const uint64_t cap = pow2_at_least(std::max<uint64_t>(2 * n, 1024));
-    if (cap > 0x80000000ull) return fail(c, CG_ERR_UNSUPPORTED, "too many reads for one table (%llu)",
-                                         (unsigned long long)n);
+    if (n > 0x40000000ull) return fail(c, CG_ERR_UNSUPPORTED, "too many reads for one table (%llu)",
+                                       (unsigned long long)n);
     // The maps are built in waves of up to kTableStreams maps, one stream and
-    // one set of counting buffers per map of a wave (as many as a quarter of
-    // the free memory holds).  A wave counts its maps' keys and values, one
-    // synchronisation sizes one slab for the wave's slots and values, then the
-    // wave places and fills its maps; the next wave's counting follows on the
-    // same streams.
+    // one set of sorting buffers per map of a wave (as many as a quarter of the
+    // free memory holds).  A wave sorts its maps' (key, read id) pairs and
+    // marks their runs of equal keys; one synchronisation reads the run
+    // counts, a second the kept keys' and values' totals, which size one slab
+    // for the wave's slots and values; then the wave fills its maps.  The
+    // next wave's sorts follow on the same streams.
     constexpr int kTableStreams = 8;
-    const size_t perStream = cap * (sizeof(Slot) + sizeof(uint32_t)) + (cap + 1) * sizeof(unsigned long long) +
-                             scan_tmp_bytes(cap + 1);
+    const int bits = std::min(64, 2 * c->k);  // the signatures keep 2k bits
+    const size_t perStream = n * (2 * sizeof(unsigned long long) + 2 * sizeof(uint32_t)) +
+                             2 * (n + 1) * sizeof(uint32_t) + (n + 1) * sizeof(unsigned long long) +
+                             radix_sort_temp_bytes(n) + scan_tmp_bytes(n + 1);
     size_t freeB = 0, totalB = 0;
     CG_CUDA(c, cudaMemGetInfo(&freeB, &totalB));
     const int S = (int)std::max<size_t>(1, std::min<size_t>({(size_t)kTableStreams, (size_t)c->nmaps,
@@ -519,10 +510,10 @@ int build_tables(cg_ctx* c) {
     struct Lane {
         cudaStream_t stream = nullptr;
         cudaEvent_t done = nullptr;
-        DevBuf tmp, cursor, packed, scanTmp;
+        DevBuf keys, ids, keysAlt, idsAlt, runOf, start, packed, sortTmp, scanTmp;
     };
     std::vector<Lane> lanes(S);
-    unsigned long long* hTot = nullptr;
+    unsigned long long* hTot = nullptr;  // per map: (kept keys << 32) | values, then the runs (u32)
     release_tables(c);
     c->maps.resize(c->nmaps);
     c->stats.table_keys = 0;
@@ -535,36 +526,56 @@ int build_tables(cg_ctx* c) {
                       what, cudaGetErrorString(e));
         return rc == CG_OK;
     };
-    if (cuda(cudaMallocHost(&hTot, (size_t)c->nmaps * sizeof(unsigned long long)), "host totals") &&
+    if (cuda(cudaMallocHost(&hTot, 2 * (size_t)c->nmaps * sizeof(unsigned long long)), "host totals") &&
         cuda(cudaEventCreateWithFlags(&sigDone, cudaEventDisableTiming), "event") &&
         cuda(cudaEventRecord(sigDone, c->stream), "event")) {
         for (Lane& l : lanes) {
             if (!cuda(cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking), "stream") ||
                 !cuda(cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming), "event") ||
                 !cuda(cudaStreamWaitEvent(l.stream, sigDone, 0), "wait") ||
-                !cuda(l.tmp.ensure(cap * sizeof(Slot)), "counting table") ||
-                !cuda(l.cursor.ensure(cap * sizeof(uint32_t)), "cursors") ||
-                !cuda(l.packed.ensure((cap + 1) * sizeof(unsigned long long)), "counts") ||
-                !cuda(l.scanTmp.ensure(scan_tmp_bytes(cap + 1)), "scan"))
+                !cuda(l.keys.ensure(std::max<uint64_t>(n, 1) * sizeof(unsigned long long)), "sorted keys") ||
+                !cuda(l.ids.ensure(std::max<uint64_t>(n, 1) * sizeof(uint32_t)), "sorted ids") ||
+                !cuda(l.keysAlt.ensure(std::max<uint64_t>(n, 1) * sizeof(unsigned long long)), "sort keys") ||
+                !cuda(l.idsAlt.ensure(std::max<uint64_t>(n, 1) * sizeof(uint32_t)), "sort ids") ||
+                !cuda(l.runOf.ensure((n + 1) * sizeof(uint32_t)), "runs") ||
+                !cuda(l.start.ensure((n + 1) * sizeof(uint32_t)), "run starts") ||
+                !cuda(l.packed.ensure((n + 1) * sizeof(unsigned long long)), "run lengths") ||
+                !cuda(l.sortTmp.ensure(radix_sort_temp_bytes(n)), "sort") ||
+                !cuda(l.scanTmp.ensure(scan_tmp_bytes(n + 1)), "scan"))
                 break;
         }
     }
+    uint32_t* hRuns = reinterpret_cast<uint32_t*>(hTot + c->nmaps);
     for (int w0 = 0; w0 < c->nmaps && rc == CG_OK; w0 += S) {
         const int w1 = std::min(c->nmaps, w0 + S);
         for (int h = w0; h < w1 && rc == CG_OK; h++) {
             Lane& l = lanes[h - w0];
             const unsigned long long* keys = c->sig.as<unsigned long long>() + (uint64_t)h * n;
-            cudaError_t e = launch_table_init(l.tmp.as<Slot>(), cap, l.stream);
-            if (e == cudaSuccess) e = launch_table_count(keys, n, l.tmp.as<Slot>(), (uint32_t)(cap - 1), l.stream);
-            if (e == cudaSuccess) e = launch_table_mark(l.tmp.as<Slot>(), cap, c->maxValuesPerKey,
-                                                        l.packed.as<unsigned long long>(), l.stream);
-            if (e == cudaSuccess) e = scan_exclusive_u64(l.packed.as<unsigned long long>(), cap + 1, l.scanTmp.p,
-                                                         l.stream);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(hTot + h, l.packed.as<unsigned long long>() + cap,
-                                                      sizeof(unsigned long long), cudaMemcpyDeviceToHost, l.stream);
-            cuda(e, "count");
+            cudaError_t e = radix_sort_pairs(keys, n, bits, l.keys.as<unsigned long long>(), l.ids.as<uint32_t>(),
+                                             l.keysAlt.as<unsigned long long>(), l.idsAlt.as<uint32_t>(),
+                                             l.sortTmp.p, l.stream);
+            if (e == cudaSuccess) e = launch_run_heads(l.keys.as<unsigned long long>(), n, l.runOf.as<uint32_t>(),
+                                                       l.stream);
+            if (e == cudaSuccess) e = scan_exclusive_u32(l.runOf.as<uint32_t>(), n + 1, l.scanTmp.p, l.stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(hRuns + h, l.runOf.as<uint32_t>() + n, sizeof(uint32_t),
+                                                      cudaMemcpyDeviceToHost, l.stream);
+            cuda(e, "sort");
         }
-        for (int h = w0; h < w1 && rc == CG_OK; h++) cuda(cudaStreamSynchronize(lanes[h - w0].stream), "count");
+        for (int h = w0; h < w1 && rc == CG_OK; h++) cuda(cudaStreamSynchronize(lanes[h - w0].stream), "sort");
+        for (int h = w0; h < w1 && rc == CG_OK; h++) {
+            Lane& l = lanes[h - w0];
+            const uint32_t runs = hRuns[h];
+            cudaError_t e = launch_run_starts(l.keys.as<unsigned long long>(), n, l.runOf.as<uint32_t>(),
+                                              l.start.as<uint32_t>(), l.stream);
+            if (e == cudaSuccess) e = launch_run_pack(l.keys.as<unsigned long long>(), l.start.as<uint32_t>(), runs,
+                                                      c->maxValuesPerKey, l.packed.as<unsigned long long>(), l.stream);
+            if (e == cudaSuccess) e = scan_exclusive_u64(l.packed.as<unsigned long long>(), (size_t)runs + 1,
+                                                         l.scanTmp.p, l.stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(hTot + h, l.packed.as<unsigned long long>() + runs,
+                                                      sizeof(unsigned long long), cudaMemcpyDeviceToHost, l.stream);
+            cuda(e, "runs");
+        }
+        for (int h = w0; h < w1 && rc == CG_OK; h++) cuda(cudaStreamSynchronize(lanes[h - w0].stream), "runs");
         if (rc != CG_OK) break;
         uint64_t slotTotal = 0, valueTotal = 0;
         std::vector<uint64_t> valueOff(w1 - w0);
@@ -586,19 +597,16 @@ int build_tables(cg_ctx* c) {
         uint32_t* valueBase = reinterpret_cast<uint32_t*>(slotBase + slotTotal);
         for (int h = w0; h < w1 && rc == CG_OK; h++) {
             Lane& l = lanes[h - w0];
-            const unsigned long long* keys = c->sig.as<unsigned long long>() + (uint64_t)h * n;
             MapTable& mt = c->maps[h];
             mt.slots = slotBase;
             slotBase += mt.cap;
             mt.values = valueBase + valueOff[h - w0];
             cudaError_t e = launch_table_init(mt.slots, mt.cap, l.stream);
-            if (e == cudaSuccess) e = launch_table_place(l.tmp.as<Slot>(), cap, l.packed.as<unsigned long long>(),
-                                                         c->maxValuesPerKey, mt.slots, (uint32_t)(mt.cap - 1),
-                                                         nullptr, l.stream);
-            if (e == cudaSuccess) e = cudaMemsetAsync(l.cursor.p, 0, cap * sizeof(uint32_t), l.stream);
-            if (e == cudaSuccess) e = launch_table_fill(keys, n, l.tmp.as<Slot>(), (uint32_t)(cap - 1),
-                                                        l.cursor.as<uint32_t>(), mt.values, l.stream);
-            if (e == cudaSuccess) e = launch_table_sort(mt.slots, mt.cap, mt.values, l.stream);
+            if (e == cudaSuccess) e = launch_run_fill(l.keys.as<unsigned long long>(), l.ids.as<uint32_t>(), n,
+                                                      l.runOf.as<uint32_t>(), l.start.as<uint32_t>(),
+                                                      hRuns[h], l.packed.as<unsigned long long>(),
+                                                      c->maxValuesPerKey, mt.values, mt.slots,
+                                                      (uint32_t)(mt.cap - 1), l.stream);
             if (!cuda(e, "build")) break;
             c->stats.table_keys += mt.keys;
             c->stats.table_values += mt.nvalues;
@@ -615,10 +623,9 @@ int build_tables(cg_ctx* c) {
     cudaError_t e = cudaStreamSynchronize(c->stream);
     for (Lane& l : lanes) {
         if (l.stream) cudaStreamSynchronize(l.stream);
-        l.tmp.release();
-        l.cursor.release();
-        l.packed.release();
-        l.scanTmp.release();
+        for (DevBuf* d : {&l.keys, &l.ids, &l.keysAlt, &l.idsAlt, &l.runOf, &l.start, &l.packed, &l.sortTmp,
+                          &l.scanTmp})
+            d->release();
         if (l.done) cudaEventDestroy(l.done);
         if (l.stream) cudaStreamDestroy(l.stream);
     }

@@ -125,6 +125,8 @@ static_assert(sizeof(ForestNode) == 24, "forest node layout");
 size_t scan_tmp_bytes(size_t n);
 cudaError_t scan_exclusive_u32(uint32_t* data, size_t n, void* tmp, cudaStream_t s);
 cudaError_t scan_exclusive_u64(unsigned long long* data, size_t n, void* tmp, cudaStream_t s);
+// kernels one scan of n elements launches
+uint64_t scan_launches(uint64_t n);
 
 // read store
 cudaError_t launch_count_invalid(const char* chars, const uint64_t* offs, uint64_t n, uint32_t* invalid,
@@ -143,15 +145,26 @@ cudaError_t launch_quality_bins(uint8_t* qual, const uint16_t* len, uint64_t n, 
 
 // hash tables
 cudaError_t launch_table_init(Slot* t, uint64_t cap, cudaStream_t s);
-cudaError_t launch_table_count(const unsigned long long* keys, uint64_t n, Slot* tmp, uint32_t tmpMask,
-                               cudaStream_t s);
-cudaError_t launch_table_mark(const Slot* tmp, uint64_t cap, int maxValues, unsigned long long* packed,
+// one map's (key, read id) pairs sorted by key (read ids ascending within a
+// key) into keys/vals, from the first `bits` bits of keysIn's keys (values
+// 0 .. n - 1); keysAlt/valsAlt hold n pairs of scratch, temp
+// radix_sort_temp_bytes(n) bytes
+size_t radix_sort_temp_bytes(uint64_t n);
+cudaError_t radix_sort_pairs(const unsigned long long* keysIn, uint64_t n, int bits, unsigned long long* keys,
+                             uint32_t* vals, unsigned long long* keysAlt, uint32_t* valsAlt, void* temp,
+                             cudaStream_t s);
+// runs of equal keys in sorted pairs: runOf[0..n] (scanned in place by the
+// caller into run indices, runOf[n] = number of runs R), start[0..R],
+// packed[0..R] (scanned by the caller into value offsets and totals), then
+// the kept runs' ids into values and their keys into the final table
+cudaError_t launch_run_heads(const unsigned long long* keys, uint64_t n, uint32_t* runOf, cudaStream_t s);
+cudaError_t launch_run_starts(const unsigned long long* keys, uint64_t n, const uint32_t* runOf, uint32_t* start,
                               cudaStream_t s);
-cudaError_t launch_table_place(Slot* tmp, uint64_t cap, const unsigned long long* packedScan, int maxValues,
-                               Slot* fin, uint32_t finMask, uint32_t* cursor, cudaStream_t s);
-cudaError_t launch_table_fill(const unsigned long long* keys, uint64_t n, const Slot* tmp, uint32_t tmpMask,
-                              uint32_t* cursor, uint32_t* values, cudaStream_t s);
-cudaError_t launch_table_sort(const Slot* fin, uint64_t finCap, uint32_t* values, cudaStream_t s);
+cudaError_t launch_run_pack(const unsigned long long* keys, const uint32_t* start, uint32_t runs, int maxValues,
+                            unsigned long long* packed, cudaStream_t s);
+cudaError_t launch_run_fill(const unsigned long long* keys, const uint32_t* ids, uint64_t n, const uint32_t* runOf,
+                            const uint32_t* start, uint32_t runs, const unsigned long long* packedScan, int maxValues,
+                            uint32_t* values, Slot* fin, uint32_t finMask, cudaStream_t s);
 
 // correction batch
 struct BatchArg {

@@ -95,6 +95,16 @@ size_t scan_tmp_bytes(size_t n) {
     return (total + 16) * sizeof(unsigned long long);
 }
 
+uint64_t scan_launches(uint64_t n) {
+    uint64_t k = 0;
+    while (true) {
+        const uint64_t tiles = tiles_of(n);
+        if (tiles <= 1) return k + 1;
+        k += 2;
+        n = tiles;
+    }
+}
+
 cudaError_t scan_exclusive_u32(uint32_t* data, size_t n, void* tmp, cudaStream_t s) {
     return scan_impl<uint32_t>(data, n, static_cast<uint32_t*>(tmp), s);
 }

@@ -7,11 +7,12 @@
 // sorted, unique, self removed, optionally ambiguous reads removed) and
 // include/util.hpp:1005-1200 (pair flags of paired-end candidates).
 //
-// Build, per map, without a sort: (1) count every key in an open-addressing
-// table of 2N slots, (2) scan the kept keys' counts into value offsets,
-// (3) place kept keys into a compact final table, (4) scatter read ids into
-// their buckets, (5) sort each bucket (at most maxValuesPerKey ids).  The
-// bucket contents -- the only thing a query observes -- equal the reference's.
+// Build, per map: (1) sort the (key, read id) pairs by key, read ids
+// ascending within a key (k_sort.cu), (2) find the runs of equal keys,
+// (3) keep the keys with 2 to maxValuesPerKey ids and scan their lengths into
+// value offsets, (4) copy each kept run's read ids into its bucket and place
+// its key in a compact open-addressing table.  The bucket contents -- the only
+// thing a query observes -- equal the reference's.
 
 #include <algorithm>
 
@@ -31,130 +32,78 @@ __global__ void table_init_kernel(Slot* __restrict__ t, uint64_t cap) {
     }
 }
 
-__global__ void table_count_kernel(const unsigned long long* __restrict__ keys, uint64_t n, Slot* __restrict__ tmp,
-                                   uint32_t mask) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const unsigned long long key = keys[i];
-    if (key == kEmptyKey) return;  // only possible for k == 32; never queried
-    uint32_t s = slot_of(key, mask);
-    for (uint32_t probe = 0; probe <= mask; probe++) {
-        const unsigned long long old = atomicCAS(&tmp[s].key, kEmptyKey, key);
-        if (old == kEmptyKey || old == key) {
-            atomicAdd(&tmp[s].count, 1u);
-            return;
-        }
-        s = (s + 1) & mask;
-    }
+// ---------------------------------------------------------------- runs of sorted pairs
+//
+// keys/ids: one map's pairs sorted by key.  runOf[i] = 1 where element i
+// starts a run (runOf[n] = 0); after an exclusive scan over n + 1 entries,
+// runOf[i + 1] - 1 is element i's run and runOf[n] the number of runs R.
+// start[r] = first element of run r, start[R] = n.
+
+__device__ __forceinline__ bool run_kept(unsigned long long key, uint32_t len, int maxValues) {
+    const uint32_t upper = (uint32_t)min(maxValues, kMaxBucket);
+    return key != kEmptyKey && len >= 2u && len <= upper;
 }
 
-// packed[s] = (1 << 32) | count for a kept key, else 0; packed[cap] = 0
-__global__ void table_mark_kernel(const Slot* __restrict__ tmp, uint64_t cap, int maxValues,
-                                  unsigned long long* __restrict__ packed) {
-    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s > cap) return;
-    if (s == cap) {
-        packed[s] = 0;
+__global__ void run_head_kernel(const unsigned long long* __restrict__ keys, uint64_t n,
+                                uint32_t* __restrict__ runOf) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    runOf[i] = (i < n && (i == 0 || keys[i] != keys[i - 1])) ? 1u : 0u;
+}
+
+__global__ void run_start_kernel(const unsigned long long* __restrict__ keys, uint64_t n,
+                                 const uint32_t* __restrict__ runOf, uint32_t* __restrict__ start) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    if (i == n) start[runOf[n]] = (uint32_t)n;
+    else if (i == 0 || keys[i] != keys[i - 1]) start[runOf[i]] = (uint32_t)i;
+}
+
+// packed[r] = (1 << 32) | length for a kept run, else 0; packed[R] = 0
+__global__ void run_pack_kernel(const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ start,
+                                uint32_t runs, int maxValues, unsigned long long* __restrict__ packed) {
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > runs) return;
+    if (r == runs) {
+        packed[r] = 0;
         return;
     }
-    const Slot t = tmp[s];
-    const uint32_t upper = (uint32_t)min(maxValues, kMaxBucket);
-    const bool kept = t.key != kEmptyKey && t.count >= 2u && t.count <= upper;
-    packed[s] = kept ? ((1ull << 32) | t.count) : 0ull;
+    const uint32_t s0 = start[r], len = start[r + 1] - s0;
+    packed[r] = run_kept(keys[s0], len, maxValues) ? ((1ull << 32) | len) : 0ull;
 }
 
-__global__ void table_place_kernel(Slot* __restrict__ tmp, uint64_t cap, const unsigned long long* __restrict__ scan,
-                                   int maxValues, Slot* __restrict__ fin, uint32_t finMask) {
-    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= cap) return;
-    Slot t = tmp[s];
-    if (t.key == kEmptyKey) return;
-    const uint32_t upper = (uint32_t)min(maxValues, kMaxBucket);
-    const bool kept = t.count >= 2u && t.count <= upper;
-    const uint32_t off = (uint32_t)(scan[s] & 0xffffffffull);
-    tmp[s].offset = kept ? off : 0xffffffffu;
-    if (!kept) return;
-    uint32_t f = slot_of(t.key, finMask);
-    for (uint32_t probe = 0; probe <= finMask; probe++) {
-        const unsigned long long old = atomicCAS(&fin[f].key, kEmptyKey, t.key);
-        if (old == kEmptyKey) {
-            fin[f].offset = off;
-            fin[f].count = t.count;
-            return;
-        }
-        f = (f + 1) & finMask;
-    }
-}
-
-__global__ void table_fill_kernel(const unsigned long long* __restrict__ keys, uint64_t n,
-                                  const Slot* __restrict__ tmp, uint32_t mask, uint32_t* __restrict__ cursor,
+// packedScan = exclusive scan of run_pack_kernel's output: the read ids of
+// every kept run, in order, at its value offset
+__global__ void run_values_kernel(const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ ids,
+                                  uint64_t n, const uint32_t* __restrict__ runOf, const uint32_t* __restrict__ start,
+                                  const unsigned long long* __restrict__ packedScan, int maxValues,
                                   uint32_t* __restrict__ values) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const unsigned long long key = keys[i];
-    if (key == kEmptyKey) return;
-    uint32_t s = slot_of(key, mask);
-    for (uint32_t probe = 0; probe <= mask; probe++) {
-        const Slot t = tmp[s];
-        if (t.key == key) {
-            if (t.offset != 0xffffffffu) {
-                const uint32_t pos = atomicAdd(&cursor[s], 1u);
-                values[t.offset + pos] = (uint32_t)i;
-            }
-            return;
-        }
-        if (t.key == kEmptyKey) return;
-        s = (s + 1) & mask;
-    }
+    const uint32_t r = runOf[i + 1] - 1u;
+    const uint32_t s0 = start[r], len = start[r + 1] - s0;
+    if (!run_kept(keys[i], len, maxValues)) return;
+    values[(uint32_t)(packedScan[r] & 0xffffffffull) + ((uint32_t)i - s0)] = ids[i];
 }
 
-// One warp per 32 slots of the final table: the read ids of each occupied
-// slot's bucket in ascending order.  Buckets of up to 96 ids are ranked in
-// registers (the ids of a bucket are distinct: a read adds one id per map);
-// larger ones take an insertion sort by one lane.
-__global__ void table_sort_kernel(const Slot* __restrict__ fin, uint64_t cap, uint32_t* __restrict__ values) {
-    constexpr unsigned kFull = 0xffffffffu;
-    const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;  // blockDim: a multiple of 32
-    const int lane = (int)(threadIdx.x & 31u);
-    Slot t{};
-    bool occ = false;
-    if (s < cap) {
-        t = fin[s];
-        occ = t.key != kEmptyKey && t.count > 1;
-    }
-    for (unsigned m = __ballot_sync(kFull, occ); m; m &= m - 1) {
-        const int src = __ffs(m) - 1;
-        const uint32_t off = __shfl_sync(kFull, t.offset, src), cnt = __shfl_sync(kFull, t.count, src);
-        uint32_t* v = values + off;
-        if (cnt <= 96) {
-            uint32_t x[3], r[3] = {0u, 0u, 0u};
-#pragma unroll
-            for (int k = 0; k < 3; k++) x[k] = (uint32_t)(lane + 32 * k) < cnt ? v[lane + 32 * k] : 0xffffffffu;
-#pragma unroll
-            for (int k2 = 0; k2 < 3; k2++) {
-                if ((uint32_t)(32 * k2) >= cnt) break;
-                for (int j = 0; j < 32; j++) {
-                    const uint32_t y = __shfl_sync(kFull, x[k2], j);
-#pragma unroll
-                    for (int k = 0; k < 3; k++) r[k] += y < x[k];
-                }
-            }
-            __syncwarp();
-#pragma unroll
-            for (int k = 0; k < 3; k++)
-                if ((uint32_t)(lane + 32 * k) < cnt) v[r[k]] = x[k];
-        } else if (lane == src) {
-            for (uint32_t i = 1; i < cnt; i++) {
-                const uint32_t x = v[i];
-                int j = (int)i - 1;
-                while (j >= 0 && v[j] > x) {
-                    v[j + 1] = v[j];
-                    j--;
-                }
-                v[j + 1] = x;
-            }
+// every kept run's key into the final table with its value offset and length
+__global__ void run_place_kernel(const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ start,
+                                 uint32_t runs, const unsigned long long* __restrict__ packedScan, int maxValues,
+                                 Slot* __restrict__ fin, uint32_t finMask) {
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= runs) return;
+    const uint32_t s0 = start[r], len = start[r + 1] - s0;
+    const unsigned long long key = keys[s0];
+    if (!run_kept(key, len, maxValues)) return;
+    uint32_t f = slot_of(key, finMask);
+    for (uint32_t probe = 0; probe <= finMask; probe++) {
+        const unsigned long long old = atomicCAS(&fin[f].key, kEmptyKey, key);
+        if (old == kEmptyKey) {
+            fin[f].offset = (uint32_t)(packedScan[r] & 0xffffffffull);
+            fin[f].count = len;
+            return;
         }
-        __syncwarp();
+        f = (f + 1) & finMask;
     }
 }
 
@@ -560,36 +509,36 @@ __global__ void pair_flags_kernel(BatchArg b, const uint32_t* __restrict__ rawOf
 }  // namespace
 
 cudaError_t launch_table_init(Slot* t, uint64_t cap, cudaStream_t s) {
-    table_init_kernel<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(t, cap);
+    table_init_kernel<<<(unsigned)std::max<uint64_t>(1, (cap + 255) / 256), 256, 0, s>>>(t, cap);
     return cudaGetLastError();
 }
 
-cudaError_t launch_table_count(const unsigned long long* keys, uint64_t n, Slot* tmp, uint32_t tmpMask,
-                               cudaStream_t s) {
-    table_count_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(keys, n, tmp, tmpMask);
+unsigned grid_of(uint64_t threads) { return (unsigned)std::max<uint64_t>(1, (threads + 255) / 256); }
+
+cudaError_t launch_run_heads(const unsigned long long* keys, uint64_t n, uint32_t* runOf, cudaStream_t s) {
+    run_head_kernel<<<grid_of(n + 1), 256, 0, s>>>(keys, n, runOf);
     return cudaGetLastError();
 }
 
-cudaError_t launch_table_mark(const Slot* tmp, uint64_t cap, int maxValues, unsigned long long* packed,
+cudaError_t launch_run_starts(const unsigned long long* keys, uint64_t n, const uint32_t* runOf, uint32_t* start,
                               cudaStream_t s) {
-    table_mark_kernel<<<(unsigned)((cap + 1 + 255) / 256), 256, 0, s>>>(tmp, cap, maxValues, packed);
+    run_start_kernel<<<grid_of(n + 1), 256, 0, s>>>(keys, n, runOf, start);
     return cudaGetLastError();
 }
 
-cudaError_t launch_table_place(Slot* tmp, uint64_t cap, const unsigned long long* packedScan, int maxValues,
-                               Slot* fin, uint32_t finMask, uint32_t* /*cursor*/, cudaStream_t s) {
-    table_place_kernel<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(tmp, cap, packedScan, maxValues, fin, finMask);
+cudaError_t launch_run_pack(const unsigned long long* keys, const uint32_t* start, uint32_t runs, int maxValues,
+                            unsigned long long* packed, cudaStream_t s) {
+    run_pack_kernel<<<grid_of((uint64_t)runs + 1), 256, 0, s>>>(keys, start, runs, maxValues, packed);
     return cudaGetLastError();
 }
 
-cudaError_t launch_table_fill(const unsigned long long* keys, uint64_t n, const Slot* tmp, uint32_t tmpMask,
-                              uint32_t* cursor, uint32_t* values, cudaStream_t s) {
-    table_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(keys, n, tmp, tmpMask, cursor, values);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_table_sort(const Slot* fin, uint64_t finCap, uint32_t* values, cudaStream_t s) {
-    table_sort_kernel<<<(unsigned)((finCap + 255) / 256), 256, 0, s>>>(fin, finCap, values);
+cudaError_t launch_run_fill(const unsigned long long* keys, const uint32_t* ids, uint64_t n, const uint32_t* runOf,
+                            const uint32_t* start, uint32_t runs, const unsigned long long* packedScan, int maxValues,
+                            uint32_t* values, Slot* fin, uint32_t finMask, cudaStream_t s) {
+    run_values_kernel<<<grid_of(n), 256, 0, s>>>(keys, ids, n, runOf, start, packedScan, maxValues, values);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    run_place_kernel<<<grid_of(runs), 256, 0, s>>>(keys, start, runs, packedScan, maxValues, fin, finMask);
     return cudaGetLastError();
 }
 
