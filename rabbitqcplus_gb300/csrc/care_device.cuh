@@ -43,6 +43,16 @@ __device__ __forceinline__ bool fgeq(float l, float r) { return (l > r) || feq(l
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
+// One 4-byte word from global to shared memory without a register (cp.async,
+// L1-cached); complete and visible to the issuing thread after
+// cp_async_wait_all(), to the rest of its warp after a __syncwarp() that
+// follows.
+__device__ __forceinline__ void cp_async4(uint32_t* dst, const uint32_t* src) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // first anchor of the batch and anchor id of output row 0: kernel parameters,
 // or device memory in graph replays
 __device__ __forceinline__ uint64_t batch_first(const BatchArg& b) { return b.cursor ? b.cursor[0] : b.first; }

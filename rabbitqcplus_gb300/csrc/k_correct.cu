@@ -12,6 +12,8 @@
 // intrinsics (the library is also built with --fmad=false): every compare the
 // decision makes sees the same float values as the reference's host code.
 
+#include <type_traits>
+
 #include "care_device.cuh"
 #include "care_internal.h"
 
@@ -1158,9 +1160,17 @@ __device__ __forceinline__ ColInfo col_info(const uint2* wc, int cp, int c) {
 //
 // `sm` is the warp's own slice of shared memory (msa_warp_slice_bytes), `qw`
 // the block's quality weights.
+// Walk of the chunk staging loop: word i0 + lane of a chunk's rows is word
+// off of row r (r = (i0 + lane) / pitch); (r0, off0) at i0 = 0 and the step
+// (dr, doff) per 32 words, so that the loop divides nothing.
+struct StageWalk {
+    int r0, off0, dr, doff;
+};
+
+template <bool QUAL>
 __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params& p, const BatchArg& b,
                                              const uint32_t* __restrict__ rawOff, int lp, int a, uint64_t first,
-                                             unsigned char* sm, const float* qw) {
+                                             unsigned char* sm, const float* qw, const StageWalk sw) {
     const int lane = (int)lane_id();
     uint2* wc = reinterpret_cast<uint2*>(sm);                    // [4][lp]: weight bits, count
     float* sup = reinterpret_cast<float*>(wc + 4 * lp);          // [lp]
@@ -1178,13 +1188,16 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
     const int La = st.len[aid];
     const int pitch = st.pitch;
     const uint32_t* aenc = st.enc + aid * (uint64_t)pitch;
-    const uint8_t* aq = p.useQuality ? st.qual + aid * (uint64_t)st.lmax : nullptr;
+    const uint8_t* aq = QUAL ? st.qual + aid * (uint64_t)st.lmax : nullptr;
     constexpr uint8_t kRm = 0x80;
 
     // Rows are added (sign +1: every row still in the MSA, after the anchor
     // row) or taken out again (sign -1: the rows just removed, marked kNew).
+    // Returns the number of rows added or taken out.
     constexpr uint8_t kNew = 0x40;
-    auto rowsPass = [&](bool add) {
+    auto rowsPass = [&](auto addTag) -> int {
+        constexpr bool add = decltype(addTag)::value;
+        int selected = 0;
         for (uint32_t j0 = 0; j0 < nf; j0 += 32) {
             const uint32_t jr = j0 + lane;
             const int rows = (int)min(32u, nf - j0);
@@ -1201,15 +1214,28 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
             const bool sel = jr < nf && (add ? !(mo & kRm) : (mo & kNew) != 0);
             const unsigned selRows = __ballot_sync(kFull, sel);
             if (!selRows) continue;
+            selected += __popc(selRows);
             if (!add && sel) b.forient[base + jr] = (uint8_t)(mo & ~kNew);
-            for (int i0 = 0; i0 < rows * pitch; i0 += 32) {  // warp-uniform trip count
-                const int idx = i0 + lane;
-                const int r = min(idx / pitch, rows - 1);
-                const uint32_t rid = __shfl_sync(kFull, mid, r);
-                if (idx < rows * pitch && ((selRows >> r) & 1u))
-                    stage[idx] = st.enc[(uint64_t)rid * pitch + (idx - r * pitch)];
+            // the selected rows' 2-bit words, copied without a register round
+            // trip and waited for once
+            {
+                const int total = rows * pitch;
+                int r = sw.r0, off = sw.off0;
+                for (int i0 = 0; i0 < total; i0 += 32) {  // warp-uniform trip count
+                    const int rr = min(r, rows - 1);
+                    const uint32_t rid = __shfl_sync(kFull, mid, rr);
+                    if (i0 + lane < total && ((selRows >> rr) & 1u))
+                        cp_async4(stage + i0 + lane, st.enc + (uint64_t)rid * pitch + off);
+                    r += sw.dr;
+                    off += sw.doff;
+                    if (off >= pitch) {
+                        off -= pitch;
+                        r++;
+                    }
+                }
             }
             meta[lane] = make_int4(mshift, mlen | (int)((mo & 3u) << 16), __float_as_int(mw), (int)mid);
+            cp_async_wait_all();
             __syncwarp();
             for (int r = 0; r < rows; r++) {
                 if (!((selRows >> r) & 1u)) continue;
@@ -1218,8 +1244,7 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
                 const int shift = md.x, len = md.y & 0xffff;
                 const float weight = __int_as_float(md.z);
                 const uint32_t* e = stage + r * pitch;
-                const uint8_t* q = nullptr;
-                if (p.useQuality) q = st.qual + (uint64_t)(uint32_t)md.w * st.lmax;
+                const uint8_t* q = QUAL ? st.qual + (uint64_t)(uint32_t)md.w * st.lmax : nullptr;
                 const int c0 = max(shift, 0), c1 = min(La, shift + len);  // overlap with the anchor
                 int c = c0 + ((lane - c0) & 31);                           // this lane's first column
                 // the row position moves by 32 per column step of the lane, so
@@ -1229,11 +1254,9 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
                 const uint32_t sh = 30u - 2u * (uint32_t)(sp & 15), flip = rc ? 3u : 0u;
                 // quality index: sp, or for a reverse complement row Lmax - 1 - (c - shift)
                 const int qd = rc ? st.lmax - len : 0;
-                for (int wi = sp >> 4; c < c1; c += 32, wi += dwi, sp += dsp) {
-                    const uint32_t bb = ((e[wi] >> sh) & 3u) ^ flip;
-                    const int qi = sp + qd;
-                    const float wt = p.useQuality ? __fmul_rn(weight, qw[q[qi]]) : weight;  // padding past the read's end as stored
-                    uint2 v = wc[bb * lp + c];
+                // padding past the read's end is read as stored
+                auto wtAt = [&](int s) -> float { return QUAL ? __fmul_rn(weight, qw[q[s + qd]]) : weight; };
+                auto upd = [&](uint2& v, float wt) {
                     if (add) {
                         v.x = __float_as_uint(__fadd_rn(__uint_as_float(v.x), wt));
                         v.y++;
@@ -1241,18 +1264,42 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
                         v.x = __float_as_uint(__fsub_rn(__uint_as_float(v.x), wt));
                         v.y--;
                     }
-                    wc[bb * lp + c] = v;
+                };
+                int wi = sp >> 4;
+                // two of the lane's columns (c and c + 32) per iteration: both
+                // words and both entries are read before either is written
+                // (distinct columns, distinct entries)
+                for (; c + 32 < c1; c += 64, wi += 2 * dwi, sp += 2 * dsp) {
+                    const uint32_t b0 = ((e[wi] >> sh) & 3u) ^ flip;
+                    const uint32_t b1 = ((e[wi + dwi] >> sh) & 3u) ^ flip;
+                    const float w0 = wtAt(sp), w1 = wtAt(sp + dsp);
+                    uint2* p0 = wc + b0 * lp + c;
+                    uint2* p1 = wc + b1 * lp + (c + 32);
+                    uint2 v0 = *p0, v1 = *p1;
+                    upd(v0, w0);
+                    upd(v1, w1);
+                    *p0 = v0;
+                    *p1 = v1;
+                }
+                if (c < c1) {
+                    const uint32_t b0 = ((e[wi] >> sh) & 3u) ^ flip;
+                    uint2* p0 = wc + b0 * lp + c;
+                    uint2 v0 = *p0;
+                    upd(v0, wtAt(sp));
+                    *p0 = v0;
                 }
             }
             __syncwarp();  // the next chunk overwrites the staged rows
         }
+        return selected;
     };
     // The MSA of the rows still in it, built as the reference builds it: the
     // anchor row (weight 1 times the quality weight), then the rows in order.
-    auto build = [&]() {
+    // Returns the number of rows it holds besides the anchor.
+    auto build = [&]() -> int {
         for (int pos = lane; pos < La; pos += 32) {
             const uint32_t bb = get2bit(aenc, pos);
-            const float wt = p.useQuality ? __fmul_rn(1.0f, qw[aq[pos]]) : 1.0f;
+            const float wt = QUAL ? __fmul_rn(1.0f, qw[aq[pos]]) : 1.0f;
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 wc[q * lp + pos] = (uint32_t)q == bb ? make_uint2(__float_as_uint(__fadd_rn(0.0f, wt)), 1u)
@@ -1260,29 +1307,12 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
             }
         }
         __syncwarp();
-        rowsPass(true);
+        return rowsPass(std::true_type{});
     };
 
-    // Region refinement (src/msa.cpp:532-734 and the loop around it in
-    // include/corrector.hpp): up to five rounds, each removing the rows that
-    // differ from the anchor at one significant column and rebuilding.  A
-    // round here subtracts the removed rows instead of rebuilding: counts are
-    // then exact, weights within E_c = (3 nf + 4) 2^-24 S_c of the rebuilt
-    // ones (S_c = column c's total weight in the first build; every partial
-    // sum and difference stays below it).  A round only reads the consensus
-    // (the largest weight) and the counts, so it sees what the rebuilt MSA
-    // shows wherever the two largest weights of every column differ by more
-    // than 2 E_c; otherwise the MSA is rebuilt first.  The MSA that the
-    // decision reads is always a full build.
-    int nActive = 0, builds = 0;
-    for (uint32_t j = lane; j < nf; j += 32) nActive += !(b.forient[base + j] & kRm);
-    nActive = __reduce_add_sync(kFull, nActive);
-    bool exact = true;
-    build();
-    for (int c = lane; c < La; c += 32) {  // S_c, kept in `sup` until the properties
-        const ColInfo ci = col_info(wc, lp, c);
-        sup[c] = ci.colW;
-    }
+    int builds = 0;
+    bool exact = true, haveS = false;
+    int nActive = build();
     const float tol = __fmul_rn(2.5f * 5.9604645e-8f, (float)(3 * nf + 4));  // 2 E_c / S_c with slack
     for (int iter = 0;; iter++) {
         builds++;
@@ -1359,8 +1389,12 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
             else act += !(o & kRm);
         }
         nActive = __reduce_add_sync(kFull, act);
+        if (!haveS) {  // S_c (the first build, which wc still holds), kept in `sup` until the properties
+            for (int c = lane; c < La; c += 32) sup[c] = col_info(wc, lp, c).colW;
+            haveS = true;
+        }
         __syncwarp();
-        rowsPass(false);
+        rowsPass(std::false_type{});
         exact = false;
     }
     if (!exact) build();
@@ -1381,9 +1415,15 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
     maxc = __reduce_max_sync(kFull, maxc);
     __syncwarp();
     float avg = 0.0f;
-    if (lane == 0) {
+    if (lane == 0) {  // in column order, four columns per shared-memory load
         float sum = 0.0f;
-        for (int i = 0; i < La; i++) sum = __fadd_rn(sum, sup[i]);
+        const float4* s4 = reinterpret_cast<const float4*>(sup);
+        int i = 0;
+        for (; i + 4 <= La; i += 4) {
+            const float4 v = s4[i >> 2];
+            sum = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(sum, v.x), v.y), v.z), v.w);
+        }
+        for (; i < La; i++) sum = __fadd_rn(sum, sup[i]);
         avg = __fdiv_rn(sum, (float)La);
     }
     avg = __shfl_sync(kFull, avg, 0);
@@ -1490,7 +1530,7 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
                     const uint32_t bb = ((stage[r * pitch + (sp >> 4)] >> (30u - 2u * (uint32_t)(sp & 15))) & 3u) ^
                                         (rc ? 3u : 0u);
                     float wt = __int_as_float(md.z);
-                    if (p.useQuality)
+                    if (QUAL)
                         wt = __fmul_rn(wt, qw[row_quality(st.qual + (uint64_t)(uint32_t)md.w * st.lmax, st.lmax, rc,
                                                           pos)]);
 #pragma unroll
@@ -1633,7 +1673,7 @@ __device__ __forceinline__ void msa_warp_anchor(const StoreArg& st, const Params
         f[28] = __fmul_rn((float)La, 1.0f / 256.0f);
         f[29] = __fmul_rn((float)nd, invLa);
         f[30] = __fdiv_rn((float)nActive, ec);
-        f[31] = p.useQuality ? qw[aq[c]] : 1.0f;
+        f[31] = QUAL ? qw[aq[c]] : 1.0f;
         uint32_t wd[kLearnedFeatures / 2];
 #pragma unroll
         for (int k = 0; k < kLearnedFeatures / 2; k++) {
@@ -1672,17 +1712,24 @@ __global__ void __launch_bounds__(256, 4) msa_warp_kernel(StoreArg st, Params p,
         __syncthreads();
     }
     const uint64_t first = batch_first(b);
+    const int lane = (int)lane_id(), pitch = st.pitch;
+    const StageWalk sw{lane / pitch, lane % pitch, 32 / pitch, 32 % pitch};
+    auto anchor = [&](int i) {
+        const int a = b.order ? (int)b.order[i] : i;
+        if (p.useQuality) msa_warp_anchor<true>(st, p, b, rawOff, lp, a, first, slice, qw, sw);
+        else msa_warp_anchor<false>(st, p, b, rawOff, lp, a, first, slice, qw, sw);
+    };
     if (!b.work) {
         const int i = blockIdx.x * warps + warp;
-        if (i < b.count) msa_warp_anchor(st, p, b, rawOff, lp, b.order ? (int)b.order[i] : i, first, slice, qw);
+        if (i < b.count) anchor(i);
         return;
     }
     while (true) {
         int i = 0;
-        if (lane_id() == 0) i = (int)atomicAdd(&b.work[1], 1u);
+        if (lane == 0) i = (int)atomicAdd(&b.work[1], 1u);
         i = __shfl_sync(kFull, i, 0);
         if (i >= b.count) return;
-        msa_warp_anchor(st, p, b, rawOff, lp, b.order ? (int)b.order[i] : i, first, slice, qw);
+        anchor(i);
         __syncwarp();
     }
 }
