@@ -39,7 +39,7 @@ correction), and from the forest decision (plain driver, untimed).
           the reference's CPU path, pinned to its output) on every host core,
           over a bounded sample of anchors of the same workload (tables built
           once, not timed)
-  secondary  the same forms on the 2M-read, 10 Mbp workload with repeats
+  secondary  the same forms and e2e on the 2M-read, 10 Mbp workload with repeats
 
 `--impl reference` times the reference algorithm on the host cores: the
 reference's own build does not exist on the GPU machine, so this arm runs the
@@ -518,9 +518,11 @@ def main():
     clocks = clk.summary()
     roof = roofline_of(head["runs"]["plain"], clocks.get("sm_mhz")) if "plain" in head["runs"] else None
 
-    # e2e through the C ABI from pinned host memory (batched + learned)
-    e2e = None
-    if not args.no_e2e:
+    def e2e_of(reads, cfg_, steps):
+        """The metric end to end through the C ABI from pinned host memory
+        (batched + learned): per step a fresh context, every read appended,
+        the device build, the classifier load, the correction of this
+        replica's anchors and every result copied back."""
         n = reads.n
         lmax = int(reads.lengths.max())
         flags = np.zeros(n, np.uint8)
@@ -531,13 +533,13 @@ def main():
             # page-lock the caller's buffers (untimed set-up), as a caller streaming reads would
             if int(rt.cudaHostRegister(a.ctypes.data, a.nbytes, 0)) == 0:
                 pinned.append(a)
-        k = max(1, args.e2e_steps)
+        k = max(1, steps)
         te = 0.0
-        sf, sc = shard.shard_range(n, rank, world, bool(cfg.paired))  # this replica's anchors
+        sf, sc = shard.shard_range(n, rank, world, bool(cfg_.paired))  # this replica's anchors
         for i in range(1 + k):
             barrier()
             t0 = time.perf_counter()
-            g2 = make_ctx(reads, cfg, "batched_learned")
+            g2 = make_ctx(reads, cfg_, "batched_learned")
             g2.correct(sf, sc, flags[sf:sf + sc], rows[sf:sf + sc])
             g2.close()
             barrier()
@@ -546,15 +548,16 @@ def main():
         for a in pinned:
             rt.cudaHostUnregister(a.ctypes.data)
         te = max_over_ranks(te)
-        e2e = {"value": n * k / te, "unit": UNIT, "steps": k, "seconds_per_step": te / k,
-               "h2d_bytes_per_step": int(reads.sequences.nbytes + reads.offsets.nbytes + len(model)),
-               "d2h_bytes_per_step": int(flags[sf:sf + sc].nbytes + rows[sf:sf + sc].nbytes),
-               "pinned": len(pinned) == 4,
-               "form": "batched_learned",
-               "includes": "fresh context, append of every read from pinned host memory, device read-store and "
-                           "table build, classifier load, correction of every anchor (each replica its shard), "
-                           "every result to pinned host memory, destroy"}
-        del flags, rows
+        return {"value": n * k / te, "unit": UNIT, "steps": k, "seconds_per_step": te / k,
+                "h2d_bytes_per_step": int(reads.sequences.nbytes + reads.offsets.nbytes + len(model)),
+                "d2h_bytes_per_step": int(flags[sf:sf + sc].nbytes + rows[sf:sf + sc].nbytes),
+                "pinned": len(pinned) == 4,
+                "form": "batched_learned",
+                "includes": "fresh context, append of every read from pinned host memory, device read-store and "
+                            "table build, classifier load, correction of every anchor (each replica its shard), "
+                            "every result to pinned host memory, destroy"}
+
+    e2e = None if args.no_e2e else e2e_of(reads, cfg, args.e2e_steps)
 
     def sweep_one(reads, cfg_, form, t):
         o = form_options(cfg_, form)
@@ -606,7 +609,11 @@ def main():
     if args.secondary and args.secondary != "none" and args.secondary != args.config:
         cfg2 = sim.CONFIGS[args.secondary]
         sec = run_workload(args.secondary, cfg2, args.steps, args.warmup, None, False)
-        secondary = {"config": workload_desc(args.secondary, cfg2), "forms": sec["forms"]}
+        secondary = {"config": workload_desc(args.secondary, cfg2), "forms": sec["forms"],
+                     "plain_stage_seconds_per_step":
+                         roofline_of(sec["runs"]["plain"], clocks.get("sm_mhz"))["stage_seconds_per_step"]
+                         if "plain" in sec["runs"] else None,
+                     "e2e": None if args.no_e2e else e2e_of(sec["reads"], cfg2, max(args.e2e_steps, 5))}
         del sec
 
     cpu = None

@@ -526,7 +526,16 @@ int build_tables(cg_ctx* c) {
                       what, cudaGetErrorString(e));
         return rc == CG_OK;
     };
-    if (cuda(cudaMallocHost(&hTot, 2 * (size_t)c->nmaps * sizeof(unsigned long long)), "host totals") &&
+    // the batched driver's raw id count of every read, summed as the maps are
+    // filled (finished by ensure_batched_state); cleared before the lanes start
+    uint32_t* rawAll = nullptr;
+    c->haveRawAll = false;
+    if (c->o.driver == CG_DRIVER_BATCHED &&
+        cuda(c->rawAll.ensure(std::max<uint64_t>(n, 1) * sizeof(uint32_t)), "raw counts") &&
+        cuda(cudaMemsetAsync(c->rawAll.p, 0, n * sizeof(uint32_t), c->stream), "raw counts"))
+        rawAll = c->rawAll.as<uint32_t>();
+    if (rc == CG_OK &&
+        cuda(cudaMallocHost(&hTot, 2 * (size_t)c->nmaps * sizeof(unsigned long long)), "host totals") &&
         cuda(cudaEventCreateWithFlags(&sigDone, cudaEventDisableTiming), "event") &&
         cuda(cudaEventRecord(sigDone, c->stream), "event")) {
         for (Lane& l : lanes) {
@@ -606,7 +615,7 @@ int build_tables(cg_ctx* c) {
                                                       l.runOf.as<uint32_t>(), l.start.as<uint32_t>(),
                                                       hRuns[h], l.packed.as<unsigned long long>(),
                                                       c->maxValuesPerKey, mt.values, mt.slots,
-                                                      (uint32_t)(mt.cap - 1), l.stream);
+                                                      (uint32_t)(mt.cap - 1), l.stream, rawAll);
             if (!cuda(e, "build")) break;
             c->stats.table_keys += mt.keys;
             c->stats.table_values += mt.nvalues;
@@ -965,9 +974,9 @@ int ensure_batched_state(cg_ctx* c) {
     if (!c->evPro) CG_CUDA(c, cudaEventCreateWithFlags(&c->evPro, cudaEventDisableTiming));
     if (!c->evStart) CG_CUDA(c, cudaEventCreate(&c->evStart));
     if (!c->haveRawAll) {
-        CG_CUDA(c, c->rawAll.ensure(c->n * sizeof(uint32_t)));
-        CG_CUDA(c, launch_raw_count(store_arg(c), c->tables, c->params, c->sig.as<unsigned long long>(),
-                                    c->rawAll.as<uint32_t>(), c->stream));
+        // the table build summed the bucket sizes (batched driver only)
+        if (!c->rawAll.p) return fail(c, CG_ERR_STATE, "raw counts were not built with the tables");
+        CG_CUDA(c, launch_raw_count(store_arg(c), c->params, c->rawAll.as<uint32_t>(), c->stream));
         c->stats.kernel_launches += 1;
         c->haveRawAll = true;
     }
@@ -1403,19 +1412,24 @@ int cg_append_reads(cg_ctx* c, const char* sequences, const uint64_t* offsets, c
     if (!sequences || !offsets || num_reads == 0) return fail(c, CG_ERR_INVALID_ARGUMENT, "empty read batch");
     if (c->o.use_quality_scores && !qualities)
         return fail(c, CG_ERR_INVALID_ARGUMENT, "quality scores requested but not given");
+    // the first read whose offsets descend or span more than the longest read
+    // (in read order, as a sequential check finds it), and the longest read
+    uint64_t badOrder = ~0ull, badLength = ~0ull;
+    int lmax = 0;
+#pragma omp parallel for reduction(min : badOrder, badLength) reduction(max : lmax) if (num_reads > (1u << 16))
     for (uint64_t i = 0; i < num_reads; i++) {
-        if (offsets[i + 1] < offsets[i]) return fail(c, CG_ERR_INVALID_ARGUMENT, "offsets not ascending at %llu",
-                                                     (unsigned long long)i);
-        if (offsets[i + 1] - offsets[i] > CG_MAX_READ_LENGTH)
-            return fail(c, CG_ERR_UNSUPPORTED, "read %llu longer than %d", (unsigned long long)i, CG_MAX_READ_LENGTH);
+        if (offsets[i + 1] < offsets[i]) badOrder = std::min(badOrder, i);
+        else if (offsets[i + 1] - offsets[i] > CG_MAX_READ_LENGTH) badLength = std::min(badLength, i);
+        else lmax = std::max(lmax, (int)(offsets[i + 1] - offsets[i]));
     }
+    if (badOrder < badLength)
+        return fail(c, CG_ERR_INVALID_ARGUMENT, "offsets not ascending at %llu", (unsigned long long)badOrder);
+    if (badLength != ~0ull)
+        return fail(c, CG_ERR_UNSUPPORTED, "read %llu longer than %d", (unsigned long long)badLength,
+                    CG_MAX_READ_LENGTH);
     if (c->appended + num_reads > 0xffffffffull) return fail(c, CG_ERR_UNSUPPORTED, "more than 2^32-1 reads");
     CG_CUDA(c, cudaSetDevice(c->device));
     const uint64_t bytes = offsets[num_reads] - offsets[0];
-    std::vector<uint64_t> offs(num_reads + 1);
-    int lmax = 0;
-    for (uint64_t i = 0; i <= num_reads; i++) offs[i] = offsets[i] - offsets[0];
-    for (uint64_t i = 0; i < num_reads; i++) lmax = std::max<int>(lmax, int(offs[i + 1] - offs[i]));
     c->chunks.emplace_back();
     cg_ctx::Chunk& ch = c->chunks.back();
     ch.first = c->appended;
@@ -1424,13 +1438,15 @@ int cg_append_reads(cg_ctx* c, const char* sequences, const uint64_t* offsets, c
     CG_CUDA(c, ch.chars.ensure(std::max<uint64_t>(bytes, 1)));
     CG_CUDA(c, ch.offs.ensure((num_reads + 1) * sizeof(uint64_t)));
     CG_CUDA(c, cudaMemcpyAsync(ch.chars.p, sequences + offsets[0], bytes, cudaMemcpyHostToDevice, c->stream));
-    CG_CUDA(c, cudaMemcpyAsync(ch.offs.p, offs.data(), (num_reads + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice,
+    // the caller's offsets as they are, made relative to the chunk on the device
+    CG_CUDA(c, cudaMemcpyAsync(ch.offs.p, offsets, (num_reads + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice,
                                c->stream));
+    CG_CUDA(c, launch_rebase_offsets(ch.offs.as<uint64_t>(), num_reads + 1, offsets[0], c->stream));
     if (c->o.use_quality_scores) {
         CG_CUDA(c, ch.qual.ensure(std::max<uint64_t>(bytes, 1)));
         CG_CUDA(c, cudaMemcpyAsync(ch.qual.p, qualities + offsets[0], bytes, cudaMemcpyHostToDevice, c->stream));
     }
-    CG_CUDA(c, cudaStreamSynchronize(c->stream));  // `offs` and the caller's buffers may go away
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));  // the caller's buffers may go away
     c->appended += num_reads;
     c->appendLmax = std::max(c->appendLmax, lmax);
     return CG_OK;

@@ -129,6 +129,8 @@ cudaError_t scan_exclusive_u64(unsigned long long* data, size_t n, void* tmp, cu
 uint64_t scan_launches(uint64_t n);
 
 // read store
+// offs[i] -= base for i < count
+cudaError_t launch_rebase_offsets(uint64_t* offs, uint64_t count, uint64_t base, cudaStream_t s);
 cudaError_t launch_count_invalid(const char* chars, const uint64_t* offs, uint64_t n, uint32_t* invalid,
                                  cudaStream_t s);
 cudaError_t launch_encode(const char* chars, const uint64_t* offs, const char* quals, uint64_t n,
@@ -156,7 +158,8 @@ cudaError_t radix_sort_pairs(const unsigned long long* keysIn, uint64_t n, int b
 // runs of equal keys in sorted pairs: runOf[0..n] (scanned in place by the
 // caller into run indices, runOf[n] = number of runs R), start[0..R],
 // packed[0..R] (scanned by the caller into value offsets and totals), then
-// the kept runs' ids into values and their keys into the final table
+// the kept runs' ids into values and their keys into the final table (and,
+// with rawAll, each kept id's bucket size added to rawAll[id])
 cudaError_t launch_run_heads(const unsigned long long* keys, uint64_t n, uint32_t* runOf, cudaStream_t s);
 cudaError_t launch_run_starts(const unsigned long long* keys, uint64_t n, const uint32_t* runOf, uint32_t* start,
                               cudaStream_t s);
@@ -164,7 +167,8 @@ cudaError_t launch_run_pack(const unsigned long long* keys, const uint32_t* star
                             unsigned long long* packed, cudaStream_t s);
 cudaError_t launch_run_fill(const unsigned long long* keys, const uint32_t* ids, uint64_t n, const uint32_t* runOf,
                             const uint32_t* start, uint32_t runs, const unsigned long long* packedScan, int maxValues,
-                            uint32_t* values, Slot* fin, uint32_t finMask, cudaStream_t s);
+                            uint32_t* values, Slot* fin, uint32_t finMask, cudaStream_t s,
+                            uint32_t* rawAll = nullptr);
 
 // correction batch
 struct BatchArg {
@@ -243,9 +247,10 @@ cudaError_t launch_query_count(StoreArg st, TablesArg tb, Params p, BatchArg b, 
 cudaError_t launch_gather_unique(StoreArg st, TablesArg tb, Params p, BatchArg b, int maxRawPerAnchor,
                                  cudaStream_t s, uint32_t* bigScratch = nullptr);
 cudaError_t launch_pair_flags(BatchArg b, cudaStream_t s);
-// raw id count of every read as an anchor, out[N]
-cudaError_t launch_raw_count(StoreArg st, TablesArg tb, Params p, const unsigned long long* sig, uint32_t* out,
-                             cudaStream_t s);
+// raw id count of every read as an anchor, raw[N]: raw holds every read's
+// kept bucket sizes summed by launch_run_fill over all maps; reads that
+// cannot be anchors get zero
+cudaError_t launch_raw_count(StoreArg st, Params p, uint32_t* raw, cudaStream_t s);
 // off[num+1] = exclusive scan of raw[0..num); maxima[0] = the largest raw
 // total of a batch of `batch` anchors, maxima[1] = the largest raw count of
 // one anchor; tmp needs scan_tmp_bytes(num + 1) bytes

@@ -135,6 +135,11 @@ __device__ __forceinline__ int code_of(char c) {  // -1 for a non-ACGT character
     }
 }
 
+__global__ void rebase_kernel(uint64_t* __restrict__ offs, uint64_t count, uint64_t base) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) offs[i] -= base;
+}
+
 // one warp per read: number of characters outside ACGTacgt
 __global__ void count_invalid_kernel(const char* __restrict__ chars, const uint64_t* __restrict__ offs, uint64_t n,
                                      uint32_t* __restrict__ invalid) {
@@ -263,6 +268,12 @@ __global__ void __launch_bounds__(kSigReads * 3) signature_kernel(StoreArg st, i
 }
 
 }  // namespace
+
+cudaError_t launch_rebase_offsets(uint64_t* offs, uint64_t count, uint64_t base, cudaStream_t s) {
+    if (count == 0) return cudaSuccess;
+    rebase_kernel<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(offs, count, base);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_count_invalid(const char* chars, const uint64_t* offs, uint64_t n, uint32_t* invalid,
                                  cudaStream_t s) {

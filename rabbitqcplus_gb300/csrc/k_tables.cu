@@ -73,17 +73,22 @@ __global__ void run_pack_kernel(const unsigned long long* __restrict__ keys, con
 }
 
 // packedScan = exclusive scan of run_pack_kernel's output: the read ids of
-// every kept run, in order, at its value offset
+// every kept run, in order, at its value offset.  With rawAll set, each kept
+// id also adds its run's length -- its bucket's size, the ids a query of that
+// read finds in this map -- to rawAll[id] (atomic: the maps of a build wave
+// run concurrently).
 __global__ void run_values_kernel(const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ ids,
                                   uint64_t n, const uint32_t* __restrict__ runOf, const uint32_t* __restrict__ start,
                                   const unsigned long long* __restrict__ packedScan, int maxValues,
-                                  uint32_t* __restrict__ values) {
+                                  uint32_t* __restrict__ values, uint32_t* __restrict__ rawAll) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t r = runOf[i + 1] - 1u;
     const uint32_t s0 = start[r], len = start[r + 1] - s0;
     if (!run_kept(keys[i], len, maxValues)) return;
-    values[(uint32_t)(packedScan[r] & 0xffffffffull) + ((uint32_t)i - s0)] = ids[i];
+    const uint32_t id = ids[i];
+    values[(uint32_t)(packedScan[r] & 0xffffffffull) + ((uint32_t)i - s0)] = id;
+    if (rawAll) atomicAdd(&rawAll[id], len);
 }
 
 // every kept run's key into the final table with its value offset and length
@@ -145,23 +150,15 @@ __global__ void query_count_kernel(StoreArg st, TablesArg tb, Params p, BatchArg
     }
 }
 
-// One warp per read: the raw id count of every read as an anchor (the sum
-// of query_count_kernel), for the batched form's range offsets.
-__global__ void raw_count_kernel(StoreArg st, TablesArg tb, Params p, const unsigned long long* __restrict__ sig,
-                                 uint32_t* __restrict__ out) {
-    const uint64_t aid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (aid >= st.n) return;
-    const uint32_t lane = lane_id();
-    const bool active = st.len[aid] >= p.k && !(p.excludeAmbiguous && st.ambig[aid]);
-    uint32_t total = 0;
-    if (active) {
-        for (int m = (int)lane; m < tb.nmaps; m += 32) {
-            const uint2 r = lookup(tb.slots[m], tb.mask[m], sig[(uint64_t)m * st.n + aid]);
-            if ((int)r.y <= tb.maxValuesPerKey) total += r.y;
-        }
-    }
-    total = __reduce_add_sync(0xffffffffu, total);
-    if (lane == 0) out[aid] = total;
+// The raw id count of every read as an anchor (the sum of
+// query_count_kernel's bucket sizes), for the batched form's range offsets:
+// the table build has summed every read's kept buckets into raw; a read that
+// cannot be an anchor (shorter than k, or ambiguous and excluded) queries
+// nothing.
+__global__ void raw_count_kernel(StoreArg st, Params p, uint32_t* __restrict__ raw) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= st.n) return;
+    if (st.len[i] < p.k || (p.excludeAmbiguous && st.ambig[i])) raw[i] = 0u;
 }
 
 // Raw counts of the anchors [first, first + num) widened to u64, with a zero
@@ -534,8 +531,8 @@ cudaError_t launch_run_pack(const unsigned long long* keys, const uint32_t* star
 
 cudaError_t launch_run_fill(const unsigned long long* keys, const uint32_t* ids, uint64_t n, const uint32_t* runOf,
                             const uint32_t* start, uint32_t runs, const unsigned long long* packedScan, int maxValues,
-                            uint32_t* values, Slot* fin, uint32_t finMask, cudaStream_t s) {
-    run_values_kernel<<<grid_of(n), 256, 0, s>>>(keys, ids, n, runOf, start, packedScan, maxValues, values);
+                            uint32_t* values, Slot* fin, uint32_t finMask, cudaStream_t s, uint32_t* rawAll) {
+    run_values_kernel<<<grid_of(n), 256, 0, s>>>(keys, ids, n, runOf, start, packedScan, maxValues, values, rawAll);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     run_place_kernel<<<grid_of(runs), 256, 0, s>>>(keys, start, runs, packedScan, maxValues, fin, finMask);
@@ -596,10 +593,9 @@ cudaError_t launch_gather_unique(StoreArg st, TablesArg tb, Params p, BatchArg b
     return cudaGetLastError();
 }
 
-cudaError_t launch_raw_count(StoreArg st, TablesArg tb, Params p, const unsigned long long* sig, uint32_t* out,
-                             cudaStream_t s) {
+cudaError_t launch_raw_count(StoreArg st, Params p, uint32_t* raw, cudaStream_t s) {
     if (st.n == 0) return cudaSuccess;
-    raw_count_kernel<<<(unsigned)((st.n * 32 + 255) / 256), 256, 0, s>>>(st, tb, p, sig, out);
+    raw_count_kernel<<<(unsigned)((st.n + 255) / 256), 256, 0, s>>>(st, p, raw);
     return cudaGetLastError();
 }
 

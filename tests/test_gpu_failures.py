@@ -164,3 +164,32 @@ def test_output_directory_that_cannot_exist_is_an_io_error(tmp_path):
     with pytest.raises(capi.CareError, match="I/O"):
         capi.correct_files(o, [fq], str(blocker / "sub"), ["o.fq"])
     assert not os.path.exists(str(blocker / "sub"))
+
+
+def test_bad_offsets_are_refused_at_the_first_bad_read():
+    """cg_append_reads checks every read's offsets before any copy (the check
+    runs on several host threads for large appends): the first read, in read
+    order, whose offsets descend or that is longer than CG_MAX_READ_LENGTH is
+    named; the context takes a valid append afterwards."""
+    n = 300_000
+    offs = np.arange(n + 1, dtype=np.uint64) * 100
+    seqs = np.full(int(offs[-1]) + 10_000, ord("A"), np.uint8)
+    down = offs.copy()
+    down[200_002] = down[200_001] - 1    # read 200001 descends
+    down[250_001:] += 2000               # read 250000 is too long, after it
+    longf = offs.copy()
+    longf[100_001:] += 2000              # read 100000 is too long
+    longf[250_002] = longf[250_001] - 1  # a descent after it
+    g = capi.CareGpu(capi.CareOptions.defaults(30.0))
+    with pytest.raises(capi.CareError, match="offsets not ascending at 200001"):
+        g.append_reads(seqs, down)
+    with pytest.raises(capi.CareError, match="read 100000 longer than 1024"):
+        g.append_reads(seqs, longf)
+    r = small_reads(74)
+    g.append_reads(r.sequences, r.offsets)
+    g.build_tables()
+    n_, lmax = g.read_info()
+    assert n_ == r.n and lmax == int(r.lengths.max())
+    flags, _ = g.correct()
+    assert int((flags & capi.CG_RESULT_CORRECTED).astype(bool).sum()) > r.n // 4
+    g.close()
