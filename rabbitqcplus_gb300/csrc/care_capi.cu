@@ -248,6 +248,10 @@ struct cg_ctx {
     uint64_t n = 0;
     int lmax = 0, pitch = 0, wp = 0, k = 20, nmaps = 48, maxValuesPerKey = 75;
     DevBuf enc, len, hilo, qual, ambig, sig;
+    // strand bits of every read's minima (u16 [ceil(maps / 16)][N]) and the
+    // read ids in the tables' buckets tagged with them: fewer than 2^31 reads
+    DevBuf strand;
+    bool strandTags = false;
     std::vector<MapTable> maps;    // views into tableSlabs
     std::vector<DevBuf> tableSlabs;
     TablesArg tables{};
@@ -259,7 +263,7 @@ struct cg_ctx {
 
     // batch buffers
     DevBuf qrange, rawCount, cand, ncand, paired, aln, fid, fshift, forient, fweight, flen, nfinal, flags, out, counters;
-    DevBuf scanTmp, uoff, msaOrder, orderScratch, bigScratch, perm, lenRange;
+    DevBuf scanTmp, uoff, msaOrder, orderScratch, bigScratch, perm, lenRange, laneWork;
     uint32_t* hPinned = nullptr;  // 2 words: total raw, max raw
     bool lenVaries = false;       // reads of different lengths: candidates aligned in length order
 
@@ -488,7 +492,13 @@ int build_tables(cg_ctx* c) {
     const uint64_t n = c->n;
     CG_CUDA(c, c->sig.ensure(n * c->nmaps * sizeof(unsigned long long)));
     StoreArg st = store_arg(c);
-    CG_CUDA(c, launch_signatures(st, c->k, c->nmaps, c->sig.as<unsigned long long>(), c->stream));
+    c->strandTags = n <= 0x7fffffffull;
+    uint16_t* strand = nullptr;
+    if (c->strandTags) {
+        CG_CUDA(c, c->strand.ensure((size_t)((c->nmaps + 15) / 16) * n * sizeof(uint16_t)));
+        strand = c->strand.as<uint16_t>();
+    }
+    CG_CUDA(c, launch_signatures(st, c->k, c->nmaps, c->sig.as<unsigned long long>(), strand, c->stream));
     if (n > 0x40000000ull) return fail(c, CG_ERR_UNSUPPORTED, "too many reads for one table (%llu)",
                                        (unsigned long long)n);
     // The maps are built in waves of up to kTableStreams maps, one stream and
@@ -562,7 +572,8 @@ int build_tables(cg_ctx* c) {
             const unsigned long long* keys = c->sig.as<unsigned long long>() + (uint64_t)h * n;
             cudaError_t e = radix_sort_pairs(keys, n, bits, l.keys.as<unsigned long long>(), l.ids.as<uint32_t>(),
                                              l.keysAlt.as<unsigned long long>(), l.idsAlt.as<uint32_t>(),
-                                             l.sortTmp.p, l.stream);
+                                             l.sortTmp.p, l.stream, strand ? strand + (uint64_t)(h >> 4) * n : nullptr,
+                                             h & 15);
             if (e == cudaSuccess) e = launch_run_heads(l.keys.as<unsigned long long>(), n, l.runOf.as<uint32_t>(),
                                                        l.stream);
             if (e == cudaSuccess) e = scan_exclusive_u32(l.runOf.as<uint32_t>(), n + 1, l.scanTmp.p, l.stream);
@@ -615,7 +626,8 @@ int build_tables(cg_ctx* c) {
                                                       l.runOf.as<uint32_t>(), l.start.as<uint32_t>(),
                                                       hRuns[h], l.packed.as<unsigned long long>(),
                                                       c->maxValuesPerKey, mt.values, mt.slots,
-                                                      (uint32_t)(mt.cap - 1), l.stream, rawAll);
+                                                      (uint32_t)(mt.cap - 1), l.stream, rawAll,
+                                                      strand ? 0x7fffffffu : 0xffffffffu);
             if (!cuda(e, "build")) break;
             c->stats.table_keys += mt.keys;
             c->stats.table_values += mt.nvalues;
@@ -644,6 +656,7 @@ int build_tables(cg_ctx* c) {
     CG_CUDA(c, e);
     c->tables.nmaps = c->nmaps;
     c->tables.maxValuesPerKey = c->maxValuesPerKey;
+    c->tables.strand = strand;
     return CG_OK;
 }
 
@@ -665,7 +678,8 @@ BatchArg batch_arg(cg_ctx* c, uint64_t first, int count) {
     b.fweight = c->fweight.as<float>();
     b.flen = c->flen.as<uint16_t>();
     b.nfinal = c->nfinal.as<uint32_t>();
-    b.perm = c->lenVaries ? c->perm.as<uint32_t>() : nullptr;
+    b.perm = c->lenVaries || c->strandTags ? c->perm.as<uint32_t>() : nullptr;
+    b.lenOrder = c->lenVaries;
     b.flags = c->flags.as<uint8_t>();
     b.out = c->out.as<char>();
     b.outPitch = c->lmax;
@@ -720,7 +734,7 @@ int run_candidates(cg_ctx* c, uint64_t first, int count) {
     const uint32_t maxRaw = c->hPinned[1];
     const size_t cap = std::max<uint64_t>(total, 1);
     CG_CUDA(c, c->cand.ensure(cap * sizeof(uint32_t)));
-    if (c->lenVaries) CG_CUDA(c, c->perm.ensure(cap * sizeof(uint32_t)));
+    if (c->lenVaries || c->strandTags) CG_CUDA(c, c->perm.ensure(cap * sizeof(uint32_t)));
     CG_CUDA(c, c->paired.ensure(cap));
     CG_CUDA(c, c->aln.ensure(cap * sizeof(uint2)));
     CG_CUDA(c, c->fid.ensure(cap * sizeof(uint32_t)));
@@ -768,6 +782,11 @@ int run_batch(cg_ctx* c, uint64_t first, int count, uint8_t* hFlags, char* hOut,
                                cudaMemcpyDeviceToHost, c->stream));
     CG_CUDA(c, cudaStreamSynchronize(c->stream));
     c->stats.kernel_launches += scan_launches(count + 1) + 1;
+    // the alignment's warps take their candidates from a counter (deferred
+    // second orientations are then scanned in full warps)
+    CG_CUDA(c, c->laneWork.ensure(sizeof(unsigned int)));
+    CG_CUDA(c, cudaMemsetAsync(c->laneWork.p, 0, sizeof(unsigned int), c->stream));
+    b.laneWork = c->laneWork.as<unsigned int>();
     CG_CUDA(c, cudaEventRecord(c->st1, c->stream));
     CG_CUDA(c, launch_align_filter(st, c->params, b, c->uoff.as<uint32_t>(), c->hPinned[2], c->st1b, c->stream));
     CG_CUDA(c, cudaEventRecord(c->st2, c->stream));
@@ -836,7 +855,8 @@ BatchArg set_arg(cg_ctx* c, BatchSet& s, int count) {
     b.fweight = s.fweight.as<float>();
     b.flen = s.flen.as<uint16_t>();
     b.nfinal = s.nfinal.as<uint32_t>();
-    b.perm = c->lenVaries ? s.perm.as<uint32_t>() : nullptr;
+    b.perm = c->lenVaries || c->strandTags ? s.perm.as<uint32_t>() : nullptr;
+    b.lenOrder = c->lenVaries;
     b.flags = c->flagsRange.as<uint8_t>();
     b.out = c->outRange.as<char>();
     b.outPitch = c->lmax;
@@ -859,7 +879,7 @@ int ensure_set(cg_ctx* c, BatchSet& s, int count, uint64_t capRaw) {
     CG_CUDA(c, s.nfinal.ensure(n * sizeof(uint32_t)));
     CG_CUDA(c, s.scanTmp.ensure(scan_tmp_bytes(n + 1)));
     CG_CUDA(c, s.cand.ensure(capRaw * sizeof(uint32_t)));
-    if (c->lenVaries) CG_CUDA(c, s.perm.ensure(capRaw * sizeof(uint32_t)));
+    if (c->lenVaries || c->strandTags) CG_CUDA(c, s.perm.ensure(capRaw * sizeof(uint32_t)));
     CG_CUDA(c, s.paired.ensure(capRaw));
     CG_CUDA(c, s.aln.ensure(capRaw * sizeof(uint2)));
     CG_CUDA(c, s.fid.ensure(capRaw * sizeof(uint32_t)));
@@ -1377,10 +1397,11 @@ void cg_destroy(cg_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     release_tables(c);
-    for (DevBuf* b : {&c->enc, &c->len, &c->hilo, &c->qual, &c->ambig, &c->sig, &c->qrange, &c->rawCount, &c->cand,
+    for (DevBuf* b : {&c->enc, &c->len, &c->hilo, &c->qual, &c->ambig, &c->sig, &c->strand, &c->qrange, &c->rawCount,
+                      &c->cand,
                       &c->ncand, &c->paired, &c->aln, &c->fid, &c->fshift, &c->forient, &c->fweight, &c->flen, &c->nfinal,
                       &c->flags, &c->out, &c->counters, &c->scanTmp, &c->uoff, &c->forestNodes, &c->treeOffsets,
-                      &c->msaOrder, &c->orderScratch, &c->bigScratch, &c->perm, &c->lenRange})
+                      &c->msaOrder, &c->orderScratch, &c->bigScratch, &c->perm, &c->lenRange, &c->laneWork})
         b->release();
     for (cg_ctx::Chunk& ch : c->chunks) {
         ch.chars.release();

@@ -44,6 +44,10 @@ struct TablesArg {
     uint32_t mask[kMaxMaps];
     int nmaps;
     int maxValuesPerKey;
+    // With strand set (fewer than 2^31 reads): bit 31 of every bucket value is
+    // the value read's strand bit for that map (launch_signatures), the read id
+    // is the low 31 bits, and strand[g][anchor] holds the anchor's bits.
+    const uint16_t* strand;
 };
 
 // Read store view.
@@ -138,7 +142,11 @@ cudaError_t launch_encode(const char* chars, const uint64_t* offs, const char* q
                           uint32_t* enc, uint16_t* len, uint8_t* qual, uint8_t* ambig, int pitch, int lmax,
                           cudaStream_t s);
 cudaError_t launch_hilo(StoreArg st, uint32_t* hilo, cudaStream_t s);
-cudaError_t launch_signatures(StoreArg st, int k, int nmaps, unsigned long long* sig, cudaStream_t s);
+// sig[maps][N]; with strand set also strand[ceil(maps / 16)][N], bit q of
+// strand[g][r] = map 16 g + q's minimum of read r came from a reverse
+// complement canonical k-mer
+cudaError_t launch_signatures(StoreArg st, int k, int nmaps, unsigned long long* sig, uint16_t* strand,
+                              cudaStream_t s);
 // out[0] = shortest, out[1] = longest read of the store (out preset to {~0, 0})
 cudaError_t launch_len_range(const uint16_t* len, uint64_t n, unsigned int* out, cudaStream_t s);
 // qualityScoreBits 1 or 2: bins the stored scores of reads [0, n) in place
@@ -149,12 +157,13 @@ cudaError_t launch_quality_bins(uint8_t* qual, const uint16_t* len, uint64_t n, 
 cudaError_t launch_table_init(Slot* t, uint64_t cap, cudaStream_t s);
 // one map's (key, read id) pairs sorted by key (read ids ascending within a
 // key) into keys/vals, from the first `bits` bits of keysIn's keys (values
-// 0 .. n - 1); keysAlt/valsAlt hold n pairs of scratch, temp
+// 0 .. n - 1; with tags, n < 2^31 and bit tagBit of tags[i] rides in bit 31
+// of value i); keysAlt/valsAlt hold n pairs of scratch, temp
 // radix_sort_temp_bytes(n) bytes
 size_t radix_sort_temp_bytes(uint64_t n);
 cudaError_t radix_sort_pairs(const unsigned long long* keysIn, uint64_t n, int bits, unsigned long long* keys,
                              uint32_t* vals, unsigned long long* keysAlt, uint32_t* valsAlt, void* temp,
-                             cudaStream_t s);
+                             cudaStream_t s, const uint16_t* tags = nullptr, int tagBit = 0);
 // runs of equal keys in sorted pairs: runOf[0..n] (scanned in place by the
 // caller into run indices, runOf[n] = number of runs R), start[0..R],
 // packed[0..R] (scanned by the caller into value offsets and totals), then
@@ -168,7 +177,7 @@ cudaError_t launch_run_pack(const unsigned long long* keys, const uint32_t* star
 cudaError_t launch_run_fill(const unsigned long long* keys, const uint32_t* ids, uint64_t n, const uint32_t* runOf,
                             const uint32_t* start, uint32_t runs, const unsigned long long* packedScan, int maxValues,
                             uint32_t* values, Slot* fin, uint32_t finMask, cudaStream_t s,
-                            uint32_t* rawAll = nullptr);
+                            uint32_t* rawAll = nullptr, uint32_t idMask = 0xffffffffu);
 
 // correction batch
 struct BatchArg {
@@ -188,10 +197,13 @@ struct BatchArg {
     float* fweight;         // [totalRaw]
     uint16_t* flen;         // [totalRaw] candidate length
     uint32_t* nfinal;       // [count]
-    // [totalRaw] or null: per anchor, its candidates' positions in the order of
-    // their lengths (read lengths vary); the alignment gives lane j of an
-    // anchor its candidate perm[j], so a warp's lanes see similar lengths
+    // [totalRaw] or null: per anchor, its candidates' positions in the order
+    // the alignment takes them (lane j of an anchor gets candidate perm[j]),
+    // with each one's predicted orientation in bit 31; with lenOrder the
+    // positions are grouped by length, so that a warp's lanes see similar
+    // lengths
     uint32_t* perm;
+    int lenOrder;
     uint8_t* flags;         // [count] CG_RESULT_*
     char* out;              // [count][outPitch]
     int outPitch;
@@ -207,9 +219,12 @@ struct BatchArg {
     //     offsets from it instead of a count pass and a scan per batch
     //   work[0], work[1] = the persistent alignment and MSA kernels'
     //     work-stealing counters (zero at the start of a batch)
+    // laneWork (plain form, optional): the alignment's own work-stealing
+    // counter, zero before its launch
     const unsigned long long* cursor;
     const unsigned long long* rangeOff;
     unsigned int* work;
+    unsigned int* laneWork;
     // Learned decision (correctionType CG_CORR_LEARNED): the MSA kernel records
     // every column of a non-HQ anchor whose consensus differs from the anchor's
     // base: 32 BF16 features (colFeat) and {output row, position | consensus

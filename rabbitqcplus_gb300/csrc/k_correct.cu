@@ -12,6 +12,7 @@
 // intrinsics (the library is also built with --fmad=false): every compare the
 // decision makes sees the same float values as the reference's host code.
 
+#include <algorithm>
 #include <type_traits>
 
 #include "care_device.cuh"
@@ -603,16 +604,78 @@ __device__ __forceinline__ AlnRes align_seq_fast(const uint32_t* __restrict__ aP
 
 constexpr int kLaneThreads = 128;
 
-// One thread per (anchor, candidate): both orientations with the reference's
-// sequential scan, the orientation choice, the packed result at the
-// candidate's slot.  uoff = exclusive scan of the per-anchor candidate counts.
+// Whether some shift of one candidate orientation could still tie or beat
+// the other orientation's result in the orientation rule.  Every shift whose
+// overlap has at least minov (>= 32) bases is tested, both directions (right
+// shifts 0 .. La - minov move the anchor against the candidate's first word,
+// left shifts 1 .. Lc - minov the candidate against the anchor's): the hi
+// plane mismatches of the overlap's first 32 bases, a lower bound of the
+// shift's mismatches, against L.  Shifts are tested 32 at a time, fully
+// unrolled: each outcome's sign bit moves into a pass word, which is then
+// masked to the lane's own shifts.  aHi, cHi: the hi planes (wp words).
+template <int MAXW>
+__device__ __forceinline__ bool exists_close_shift(const uint32_t* __restrict__ aHi, const uint32_t* __restrict__ cHi,
+                                                   int wp, int La, int Lc, int minov, int L, unsigned lanes) {
+    bool found = false;
+#pragma unroll 1
+    for (int dir = 0; dir < 2; dir++) {
+        const uint32_t* sh = dir == 0 ? aHi : cHi;
+        const uint32_t o0 = dir == 0 ? cHi[0] : aHi[0];
+        const int n = dir == 0 ? (Lc >= minov ? La - minov + 1 : 0) : (La >= minov ? Lc - minov + 1 : 0);
+        uint32_t R[MAXW + 1];
+#pragma unroll
+        for (int i = 0; i <= MAXW; i++) R[i] = i < wp ? sh[i] : 0u;
+        const int wn = __reduce_max_sync(lanes, n);
+#pragma unroll 1
+        for (int base = 0; base < wn; base += 32) {
+            uint32_t pass = 0u;  // bit 31 - bb: shift base + bb has at most L
+#pragma unroll
+            for (int bb = 0; bb < 32; bb++) {
+                const uint32_t x = __funnelshift_l(R[1], R[0], bb) ^ o0;
+                pass = __funnelshift_l((uint32_t)((int)__popc(x) - L - 1), pass, 1);
+            }
+            const int lo = max(dir - base, 0), hi = min(n - base, 32);  // this lane's shifts [lo, hi)
+            const uint32_t mine = lo < hi ? (0xffffffffu >> lo) & ~(hi >= 32 ? 0u : 0xffffffffu >> hi) : 0u;
+            found |= (pass & mine) != 0u;
+            if (__all_sync(lanes, found)) return true;
+#pragma unroll
+            for (int k = 0; k < MAXW; k++) R[k] = R[k + 1];
+            R[MAXW] = 0u;
+        }
+    }
+    return found;
+}
+
+// A deferred candidate: its slot, anchor, and the result of the orientation
+// scanned first (shift | overlap << 16, nOps | valid << 16 | orientation << 17).
+__device__ __forceinline__ uint4 defer_entry(uint32_t slot, int a, const AlnRes& x, int o) {
+    return make_uint4(slot, (uint32_t)a, (uint32_t)(uint16_t)(int16_t)x.shift | ((uint32_t)x.overlap << 16),
+                      (uint32_t)(uint16_t)(int16_t)x.nOps | ((uint32_t)x.valid << 16) | ((uint32_t)o << 17));
+}
+
+// One thread per (anchor, candidate), warps taking 32-candidate chunks; the
+// packed result of the reference's orientation choice at the candidate's
+// slot.  uoff = exclusive scan of the per-anchor candidate counts.
+//
+// The reference aligns both orientations (its sequential shift scan) and
+// chooses by the mismatch ratios (choose_orientation).  Here each candidate's
+// orientation predicted by its shared minimum (bit 31 of its b.perm entry) is
+// scanned first, x1.  If x1 alone would be chosen and no shift of the other
+// orientation has at most L = floor(nOps1 * min(La, Lc) / overlap1) + 1
+// mismatches (exists_close_shift), the other orientation's best shift, at
+// overlap ov <= min(La, Lc), has a ratio of at least nOps1 / overlap1 + 1 /
+// ov: more than the float rounding of either ratio, so the rule chooses x1
+// as it would with both scans.  Otherwise the candidate is deferred: its
+// warp queues it and later scans the other orientation fully in a round of
+// 32 deferred candidates, and chooses from both results exactly as the
+// reference.  Either way the packed result is the reference's.
 template <int MAXW>
 __global__ void __launch_bounds__(kLaneThreads, 8) align_lane_kernel(StoreArg st, Params p, BatchArg b,
                                                                   const uint32_t* __restrict__ rawOff,
                                                                   const uint32_t* __restrict__ uoff, uint32_t total) {
     __shared__ int16_t maxErrTab[CG_MAX_READ_LENGTH + 2];
-    __shared__ uint32_t chunk;
     __shared__ int ovPos;  // smallest overlap whose error limit is positive
+    __shared__ uint4 deferred[kLaneThreads / 32][64];
     if (threadIdx.x == 0) ovPos = st.lmax + 1;
     for (int i = threadIdx.x; i <= st.lmax; i += blockDim.x)
         maxErrTab[i] = (int16_t)(int)__fmul_rn((float)i, p.maxErrorRate);
@@ -621,49 +684,112 @@ __global__ void __launch_bounds__(kLaneThreads, 8) align_lane_kernel(StoreArg st
         if (maxErrTab[i] > 0 && (i == 0 || maxErrTab[i - 1] <= 0)) ovPos = i;
     __syncthreads();
     const uint64_t first = batch_first(b);
-    // persistent form: blocks take 128-candidate chunks from a shared counter
-    // until the batch's candidates (uoff[count], on the device) are done
-    if (b.work) total = uoff[b.count];
-    uint32_t t0 = blockIdx.x * kLaneThreads;
+    const int lane = (int)lane_id(), warp = (int)(threadIdx.x >> 5);
+    uint4* dq = deferred[warp];
+    int queued = 0;  // the warp's deferred candidates (the same in every lane)
+    // persistent form: warps take 32-candidate chunks from a shared counter
+    // until the batch's candidates (uoff[count], on the device) are done;
+    // otherwise one chunk per warp
+    unsigned int* const work = b.work ? b.work : b.laneWork;
+    if (work) total = uoff[b.count];
+    bool chunks = true;
+    uint32_t t0 = blockIdx.x * kLaneThreads + warp * 32;
+    const int wp = st.wp;
     while (true) {
-        if (b.work) {
-            if (threadIdx.x == 0) chunk = atomicAdd(&b.work[0], (uint32_t)kLaneThreads);
-            __syncthreads();
-            t0 = chunk;
-            __syncthreads();
-        }
-        if (t0 >= total) return;
-        const uint32_t t = t0 + threadIdx.x;
-        const unsigned lanes = __ballot_sync(kFull, t < total);  // the warp's lanes with a candidate
-        if (t < total) {
-            int lo = 0, hi = b.count;  // last anchor with uoff[a] <= t
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (uoff[mid] <= t) lo = mid;
-                else hi = mid;
+        // a round: 32 deferred candidates when as many wait, else the next
+        // chunk, else what is left deferred
+        bool second = queued >= 32;
+        if (!second && chunks) {
+            if (work) {
+                uint32_t c = 0;
+                if (lane == 0) c = atomicAdd(&work[0], 32u);
+                t0 = __shfl_sync(kFull, c, 0);
             }
-            const int a = lo;
-            const uint32_t j = t - uoff[a];
-            const uint32_t slot = rawOff[a] + (b.perm ? b.perm[rawOff[a] + j] : j);
+            if (t0 >= total) chunks = false;
+        }
+        if (!second && !chunks) {
+            if (queued == 0) return;
+            second = true;
+        }
+        bool has = false, defer = false;
+        uint32_t slot = 0;
+        int a = 0, o = 0;
+        AlnRes x1{};
+        if (second) {
+            const int cnt = min(queued, 32);
+            uint4 e = make_uint4(0u, 0u, 0u, 0u);
+            if (lane < cnt) e = dq[lane];
+            __syncwarp();
+            if (lane + 32 < queued) dq[lane] = dq[lane + 32];
+            __syncwarp();
+            queued -= cnt;
+            has = lane < cnt;
+            slot = e.x;
+            a = (int)e.y;
+            x1.shift = (int)(int16_t)(e.z & 0xffffu);
+            x1.overlap = (int)(e.z >> 16);
+            x1.nOps = (int)(int16_t)(e.w & 0xffffu);
+            x1.valid = ((e.w >> 16) & 1u) != 0u;
+            o = 1 - (int)((e.w >> 17) & 1u);  // the orientation not yet scanned
+        } else {
+            const uint32_t t = t0 + (uint32_t)lane;
+            has = t < total;
+            if (has) {
+                int lo = 0, hi = b.count;  // last anchor with uoff[a] <= t
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (uoff[mid] <= t) lo = mid;
+                    else hi = mid;
+                }
+                a = lo;
+                const uint32_t j = t - uoff[a];
+                const uint32_t pe = b.perm ? b.perm[rawOff[a] + j] : j;  // position, predicted orientation
+                slot = rawOff[a] + (pe & 0x7fffffffu);
+                o = (int)(pe >> 31);
+            }
+        }
+        const unsigned lanes = __ballot_sync(kFull, has);  // the warp's lanes with a candidate
+        if (has) {
             const uint64_t aid = first + (uint64_t)a;
             const uint32_t id = b.cand[slot];
             const int La = st.len[aid], Lc = st.len[id];
-            const int wp = st.wp;
-            uint32_t A[2][MAXW + 1], C[2][MAXW + 1];
             const int minov = max(p.minOverlap, (int)__fmul_rn((float)La, p.minOverlapRatio));
-            AlnRes f, r;
-#pragma unroll 1
-            for (int o = 0; o < 2; o++) {  // forward, then reverse complement
-                const AlnRes x = align_seq_fast<MAXW>(st.hilo + aid * 4 * (uint64_t)wp,
-                                                      st.hilo + (uint64_t)id * 4 * wp + 2 * wp * o, wp, A, C, La,
-                                                      Lc, minov, maxErrTab, ovPos, lanes);
-                if (o == 0) f = x;
-                else r = x;
+            const uint32_t* aPl = st.hilo + aid * 4 * (uint64_t)wp;
+            const uint32_t* cPl = st.hilo + (uint64_t)id * 4 * wp;
+            uint32_t A[2][MAXW + 1], C[2][MAXW + 1];
+            const AlnRes x = align_seq_fast<MAXW>(aPl, cPl + 2 * wp * o, wp, A, C, La, Lc, minov, maxErrTab, ovPos,
+                                                  lanes);
+            if (second) {
+                const AlnRes& f = o == 0 ? x : x1;
+                const AlnRes& r = o == 0 ? x1 : x;
+                const int ori = choose_orientation(f, r, La, p.minOverlapRatio, p.minOverlap, p.orientMaxErrorRate);
+                b.aln[slot] = pack_aln(ori == 2 ? r : f, ori);
+            } else {
+                AlnRes none{};
+                none.valid = false;
+                const int solo = o == 0 ? choose_orientation(x, none, La, p.minOverlapRatio, p.minOverlap,
+                                                             p.orientMaxErrorRate)
+                                        : choose_orientation(none, x, La, p.minOverlapRatio, p.minOverlap,
+                                                             p.orientMaxErrorRate);
+                const bool test = solo != 3 && minov >= 32;
+                const unsigned tlanes = __ballot_sync(lanes, test);
+                bool close = true;
+                if (test) {
+                    const int L = (int)(((uint32_t)x.nOps * (uint32_t)min(La, Lc)) / (uint32_t)x.overlap) + 1;
+                    close = exists_close_shift<MAXW>(aPl, cPl + 2 * wp * (1 - o), wp, La, Lc, minov, L, tlanes);
+                }
+                if (!close) b.aln[slot] = pack_aln(x, solo);
+                defer = close;
+                x1 = x;
             }
-            const int ori = choose_orientation(f, r, La, p.minOverlapRatio, p.minOverlap, p.orientMaxErrorRate);
-            b.aln[slot] = pack_aln(ori == 2 ? r : f, ori);
         }
-        if (!b.work) return;
+        if (!second) {  // queue the deferred candidates of the chunk
+            const unsigned dm = __ballot_sync(kFull, defer);
+            if (defer) dq[queued + __popc(dm & ((1u << lane) - 1u))] = defer_entry(slot, a, x1, o);
+            queued += __popc(dm);
+            __syncwarp();
+            if (!work) chunks = false;  // one chunk per warp
+        }
     }
 }
 
@@ -1799,9 +1925,17 @@ cudaError_t launch_align_filter(StoreArg st, Params p, BatchArg b, const uint32_
     if (need <= 8 && uoff) {
         const bool persistent = shape && b.work;
         if (persistent || totalUnique > 0) {
-            // persistent: the blocks take 128-candidate chunks until uoff[count]
-            const unsigned blocks =
+            // persistent: the warps take 32-candidate chunks until uoff[count];
+            // with b.laneWork (plain form) as many blocks as fit the GPU do the same
+            unsigned blocks =
                 persistent ? (unsigned)shape->alignBlocks : (totalUnique + kLaneThreads - 1) / kLaneThreads;
+            if (!persistent && b.laneWork) {
+                int dev = 0, sms = 1, occ = 1;
+                if (cudaGetDevice(&dev) == cudaSuccess)
+                    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                occ = std::max(align_lane_occupancy(st), 1);
+                blocks = std::min(blocks, (unsigned)(std::max(sms, 1) * occ));
+            }
             if (need <= 5)
                 align_lane_kernel<5><<<blocks, kLaneThreads, 0, s>>>(st, p, b, b.rawCount, uoff, totalUnique);
             else

@@ -50,11 +50,12 @@ __global__ void __launch_bounds__(kSortThreads) radix_count_kernel(const unsigne
 }
 
 // One tile per block.  offsets = the exclusive scan of radix_count_kernel's
-// counts; vals == nullptr stands for the values 0, 1, ..., n - 1.
+// counts; vals == nullptr stands for the values 0, 1, ..., n - 1, each with
+// bit tagBit of tags[i] in bit 31 when tags is set.
 __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ vals, uint64_t n, int shift,
     const uint32_t* __restrict__ offsets, uint32_t tiles, unsigned long long* __restrict__ keysOut,
-    uint32_t* __restrict__ valsOut) {
+    uint32_t* __restrict__ valsOut, const uint16_t* __restrict__ tags, int tagBit) {
     __shared__ uint32_t wcount[kSortWarps][kDigits];  // per warp: digit counts, then the warp's start in the digit
     __shared__ uint32_t tileStart[kDigits];           // digit d's first position in the staged tile
     __shared__ uint32_t globalStart[kDigits];         // and in the output
@@ -76,7 +77,8 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
         const uint64_t i = base + (uint64_t)(32 * j + lane);
         const bool valid = i < n;
         k[j] = valid ? keys[i] : 0ull;
-        v[j] = valid ? (vals ? vals[i] : (uint32_t)i) : 0u;
+        v[j] = valid ? (vals ? vals[i] : ((uint32_t)i | (tags ? ((uint32_t)(tags[i] >> tagBit) & 1u) << 31 : 0u)))
+                     : 0u;
         rank[j] = 0;
         const unsigned act = __ballot_sync(kFull, valid);
         if (valid) {
@@ -145,9 +147,9 @@ size_t radix_sort_temp_bytes(uint64_t n) {
 
 cudaError_t radix_sort_pairs(const unsigned long long* keysIn, uint64_t n, int bits, unsigned long long* keys,
                              uint32_t* vals, unsigned long long* keysAlt, uint32_t* valsAlt, void* temp,
-                             cudaStream_t s) {
+                             cudaStream_t s, const uint16_t* tags, int tagBit) {
     if (n == 0) return cudaSuccess;
-    if (n > 0xffffffffull) return cudaErrorInvalidValue;
+    if (n > 0xffffffffull || (tags && n > 0x7fffffffull)) return cudaErrorInvalidValue;
     const uint32_t tiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
     const size_t ncounts = (size_t)kDigits * tiles;
     uint32_t* counts = static_cast<uint32_t*>(temp);
@@ -165,7 +167,7 @@ cudaError_t radix_sort_pairs(const unsigned long long* keysIn, uint64_t n, int b
         if (e != cudaSuccess) return e;
         e = scan_exclusive_u32(counts, ncounts, scanTmp, s);
         if (e != cudaSuccess) return e;
-        radix_scatter_kernel<<<tiles, kSortThreads, 0, s>>>(ki, vi, n, 8 * p, counts, tiles, ko, vo);
+        radix_scatter_kernel<<<tiles, kSortThreads, 0, s>>>(ki, vi, n, 8 * p, counts, tiles, ko, vo, tags, tagBit);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         ki = ko;

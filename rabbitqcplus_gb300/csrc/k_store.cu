@@ -225,11 +225,17 @@ __global__ void hilo_kernel(StoreArg st, uint32_t* __restrict__ hilo) {
 
 // Signatures: one thread per (read, group of 16 maps); threads of a warp take
 // consecutive reads of the same group so the map-major stores coalesce.
+// With `strand`, bit q of strand[g][read] tells whether map 16 g + q's
+// minimum came from a k-mer whose canonical form is its reverse complement:
+// two reads that share that minimum overlap in the same orientation when
+// their bits agree, which the alignment uses to choose which orientation to
+// scan first (a prediction only: the result does not depend on it).
 constexpr int kSigReads = 128;
 constexpr int kSigGroup = 16;
 
 __global__ void __launch_bounds__(kSigReads * 3) signature_kernel(StoreArg st, int k, int nmaps,
-                                                                  unsigned long long* __restrict__ sig) {
+                                                                  unsigned long long* __restrict__ sig,
+                                                                  uint16_t* __restrict__ strand) {
     const uint64_t r = (uint64_t)blockIdx.x * kSigReads + (threadIdx.x % kSigReads);
     const int g = threadIdx.x / kSigReads;
     const int m0 = g * kSigGroup;
@@ -238,6 +244,7 @@ __global__ void __launch_bounds__(kSigReads * 3) signature_kernel(StoreArg st, i
     uint64_t mins[kSigGroup];
 #pragma unroll
     for (int j = 0; j < kSigGroup; j++) mins[j] = ~0ull;
+    uint32_t sb = 0;  // strand bit of each map's minimum
     const int L = st.len[r];
     if (L >= k) {
         const uint32_t* e = st.enc + r * (uint64_t)st.pitch;
@@ -252,10 +259,14 @@ __global__ void __launch_bounds__(kSigReads * 3) signature_kernel(StoreArg st, i
                 rc = (rc >> 2) | ((3ull - bb) << rcShift);
                 if (w * 16 + j >= k - 1) {
                     const uint64_t canon = fwd < rc ? fwd : rc;
+                    const uint32_t rcBits = rc < fwd ? 0xffffu : 0u;
 #pragma unroll
                     for (int q = 0; q < kSigGroup; q++) {
                         const uint64_t hv = murmur64(canon + (uint64_t)(m0 + q));
-                        mins[q] = hv < mins[q] ? hv : mins[q];
+                        if (hv < mins[q]) {
+                            mins[q] = hv;
+                            sb = (sb & ~(1u << q)) | (rcBits & (1u << q));
+                        }
                     }
                 }
             }
@@ -265,6 +276,7 @@ __global__ void __launch_bounds__(kSigReads * 3) signature_kernel(StoreArg st, i
     for (int q = 0; q < kSigGroup; q++) {
         if (m0 + q < nmaps) sig[(uint64_t)(m0 + q) * st.n + r] = mins[q] & kmask;
     }
+    if (strand) strand[(uint64_t)g * st.n + r] = (uint16_t)sb;
 }
 
 }  // namespace
@@ -353,9 +365,10 @@ cudaError_t launch_len_range(const uint16_t* len, uint64_t n, unsigned int* out,
     return cudaGetLastError();
 }
 
-cudaError_t launch_signatures(StoreArg st, int k, int nmaps, unsigned long long* sig, cudaStream_t s) {
+cudaError_t launch_signatures(StoreArg st, int k, int nmaps, unsigned long long* sig, uint16_t* strand,
+                              cudaStream_t s) {
     const unsigned blocks = (unsigned)((st.n + kSigReads - 1) / kSigReads);
-    signature_kernel<<<blocks, kSigReads * 3, 0, s>>>(st, k, nmaps, sig);
+    signature_kernel<<<blocks, kSigReads * 3, 0, s>>>(st, k, nmaps, sig, strand);
     return cudaGetLastError();
 }
 

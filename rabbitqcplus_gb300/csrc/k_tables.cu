@@ -75,12 +75,12 @@ __global__ void run_pack_kernel(const unsigned long long* __restrict__ keys, con
 // packedScan = exclusive scan of run_pack_kernel's output: the read ids of
 // every kept run, in order, at its value offset.  With rawAll set, each kept
 // id also adds its run's length -- its bucket's size, the ids a query of that
-// read finds in this map -- to rawAll[id] (atomic: the maps of a build wave
-// run concurrently).
+// read finds in this map -- to rawAll[id & idMask] (atomic: the maps of a
+// build wave run concurrently; idMask drops a strand tag in bit 31).
 __global__ void run_values_kernel(const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ ids,
                                   uint64_t n, const uint32_t* __restrict__ runOf, const uint32_t* __restrict__ start,
                                   const unsigned long long* __restrict__ packedScan, int maxValues,
-                                  uint32_t* __restrict__ values, uint32_t* __restrict__ rawAll) {
+                                  uint32_t* __restrict__ values, uint32_t* __restrict__ rawAll, uint32_t idMask) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t r = runOf[i + 1] - 1u;
@@ -88,7 +88,7 @@ __global__ void run_values_kernel(const unsigned long long* __restrict__ keys, c
     if (!run_kept(keys[i], len, maxValues)) return;
     const uint32_t id = ids[i];
     values[(uint32_t)(packedScan[r] & 0xffffffffull) + ((uint32_t)i - s0)] = id;
-    if (rawAll) atomicAdd(&rawAll[id], len);
+    if (rawAll) atomicAdd(&rawAll[id & idMask], len);
 }
 
 // every kept run's key into the final table with its value offset and length
@@ -236,21 +236,38 @@ __device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params
     }
     for (uint32_t i = tid; i < T; i += kGatherThreads) table[i] = 0xffffffffu;
     if (tid == 0) nUnique = 0;
+    // With strand-tagged values (tb.strand set) a unique candidate's list
+    // entry is its sort key id << 1 | o, o = the orientation predicted by the
+    // map whose bucket brought its first copy: its strand bit against the
+    // anchor's for that map (0 forward, 1 reverse complement).  The ids are
+    // distinct, so sorting the keys sorts the ids.
+    const bool tagged = tb.strand != nullptr;
+    constexpr int kGroup = 16, kGroups = kGatherThreads / kGroup, kMapsPer = (kMaxMaps + kGroups - 1) / kGroups;
+    const int g = tid / kGroup, gl = tid % kGroup;
+    // this thread's maps g + k kGroups: bit k = the anchor's strand bit there
+    uint32_t aStrand = 0;
+    if (tagged) {
+#pragma unroll
+        for (int k = 0; k < kMapsPer; k++) {
+            const int m = g + k * kGroups;
+            if (m < tb.nmaps) aStrand |= (((uint32_t)tb.strand[(uint64_t)(m >> 4) * st.n + aid] >> (m & 15)) & 1u) << k;
+        }
+    }
     __syncthreads();
-    auto insert = [&](uint32_t v) {
+    auto insert = [&](uint32_t tv, int k) {  // a value of map g + k kGroups
+        const uint32_t v = tagged ? tv & 0x7fffffffu : tv;
         uint32_t h = (v * 0x9E3779B1u) & mask;
         for (uint32_t probe = 0; probe < T; probe++) {
             const uint32_t old = atomicCAS(&table[h], 0xffffffffu, v);
             if (old == 0xffffffffu) {  // the first copy of v
-                if ((uint64_t)v != aid && !(p.excludeAmbiguous && st.ambig[v])) list[atomicAdd(&nUnique, 1u)] = v;
+                if ((uint64_t)v != aid && !(p.excludeAmbiguous && st.ambig[v]))
+                    list[atomicAdd(&nUnique, 1u)] = tagged ? (v << 1) | ((tv >> 31) ^ ((aStrand >> k) & 1u)) : v;
                 return;
             }
             if (old == v) return;
             h = (h + 1) & mask;
         }
     };
-    constexpr int kGroup = 16, kGroups = kGatherThreads / kGroup, kMapsPer = (kMaxMaps + kGroups - 1) / kGroups;
-    const int g = tid / kGroup, gl = tid % kGroup;
     uint32_t vals[kMapsPer];
 #pragma unroll
     for (int k = 0; k < kMapsPer; k++) {
@@ -260,15 +277,20 @@ __device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params
     }
 #pragma unroll
     for (int k = 0; k < kMapsPer; k++)
-        if (vals[k] != 0xffffffffu) insert(vals[k]);
+        if (vals[k] != 0xffffffffu) insert(vals[k], k);
     for (int k = 0; k < kMapsPer; k++) {  // ids past a bucket's first 16
         const int m = g + k * kGroups;
         if (m >= tb.nmaps) break;
-        for (uint32_t i = kGroup + gl; i < rng[m].y; i += kGroup) insert(tb.values[m][rng[m].x + i]);
+        for (uint32_t i = kGroup + gl; i < rng[m].y; i += kGroup) insert(tb.values[m][rng[m].x + i], k);
     }
     __syncthreads();
     const uint32_t U = nUnique;
     uint32_t* out = b.cand + off;
+    const int keyShift = tagged ? 1 : 0;
+    // the sorted keys stay in shared memory for the alignment order below:
+    // in `list` after the register sort, in `table` (free once the ids are
+    // in) after the others
+    const uint32_t* sk = U <= 64 ? list : table;
     if (U <= 64) {
         // one warp: a bitonic network over 64 slots in registers, ids i and
         // i + 32 in lane i (padding sorts last; the ids are distinct)
@@ -293,8 +315,11 @@ __device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params
                     }
                 }
             }
-            if (lane < U) out[lane] = x0;
-            if (lane + 32 < U) out[lane + 32] = x1;
+            if (lane < U) out[lane] = x0 >> keyShift;
+            if (lane + 32 < U) out[lane + 32] = x1 >> keyShift;
+            __syncwarp();  // every lane has read its unsorted keys
+            if (lane < U) list[lane] = x0;  // the list holds at least U entries
+            if (lane + 32 < U) list[lane + 32] = x1;
         }
     } else if (U <= 512) {
         // rank of each id among the unique ids = its position in ascending order
@@ -302,7 +327,8 @@ __device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params
             const uint32_t v = list[i];
             uint32_t rank = 0;
             for (uint32_t k = 0; k < U; k++) rank += list[k] < v;
-            out[rank] = v;
+            out[rank] = v >> keyShift;
+            table[rank] = v;
         }
     } else {
         uint32_t S = 1;
@@ -325,21 +351,33 @@ __device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params
                 __syncthreads();
             }
         }
-        for (uint32_t i = tid; i < U; i += kGatherThreads) out[i] = table[i];
+        for (uint32_t i = tid; i < U; i += kGatherThreads) out[i] = table[i] >> keyShift;
     }
-    if (b.perm) {
+    if (b.perm && !b.lenOrder) {
+        // the alignment's order is the list's; an entry is the position with
+        // the predicted orientation in bit 31
+        __syncthreads();
+        for (uint32_t i = tid; i < U; i += kGatherThreads) b.perm[off + i] = i | (tagged ? (sk[i] & 1u) << 31 : 0u);
+    } else if (b.perm) {
         // the alignment's order: positions grouped by words per read
-        // (length / 32, up to 8), in position order within a group -- a
-        // counting sort by one warp; the list's space holds the groups
+        // (length / 32, up to 8) and within that by predicted orientation,
+        // in position order within a group -- a counting sort by one warp;
+        // the list's space holds the groups.  An entry is the position, with
+        // the predicted orientation in bit 31.
         __syncthreads();
         if (tid < 32) {
             constexpr unsigned kFull = 0xffffffffu;
-            constexpr int kGroups = 9;
+            constexpr int kGroups = 18;
             const int lane = tid;
             uint32_t cnt = 0;  // lane g < kGroups: size of group g, then its start
             for (uint32_t i0 = 0; i0 < U; i0 += 32) {
                 const uint32_t i = i0 + (uint32_t)lane;
-                const uint32_t g = i < U ? min((uint32_t)st.len[out[i]] >> 5, (uint32_t)(kGroups - 1)) : kGroups;
+                uint32_t g = kGroups;
+                if (i < U) {
+                    const uint32_t key = sk[i];
+                    g = 2 * min((uint32_t)st.len[key >> keyShift] >> 5, 8u) + (tagged ? key & 1u : 0u);
+                }
+                __syncwarp();  // sk may be `list`: every lane has its key before the groups overwrite it
                 if (i < U) list[i] = g;
 #pragma unroll
                 for (int v = 0; v < kGroups; v++) {
@@ -349,7 +387,7 @@ __device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params
             }
             uint32_t start = cnt;  // exclusive scan over the groups
 #pragma unroll
-            for (int d = 1; d < 16; d <<= 1) {
+            for (int d = 1; d < 32; d <<= 1) {
                 const uint32_t y = __shfl_up_sync(kFull, start, d);
                 if (lane >= d) start += y;
             }
@@ -365,7 +403,7 @@ __device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params
                     if (g == (uint32_t)v) r = s0 + __popc(m & ((1u << lane) - 1u));
                     if (lane == v) start += __popc(m);
                 }
-                if (i < U) b.perm[off + r] = i;
+                if (i < U) b.perm[off + r] = i | ((g & 1u) << 31);
             }
         }
     }
@@ -380,7 +418,7 @@ __device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params
 // when bigList is null); anchors with more go to bigList for gather_big_kernel,
 // whose blocks hold tables large enough for them.  The split keeps the few
 // repeat anchors' large tables from lowering every block's occupancy.
-__global__ void __launch_bounds__(kGatherThreads) gather_unique_kernel(StoreArg st, TablesArg tb, Params p,
+__global__ void __launch_bounds__(kGatherThreads, 16) gather_unique_kernel(StoreArg st, TablesArg tb, Params p,
                                                                        BatchArg b, const uint32_t* __restrict__ rawOff,
                                                                        int tableSize, uint32_t smallCap,
                                                                        uint32_t* bigList, unsigned int* bigCount) {
@@ -531,8 +569,10 @@ cudaError_t launch_run_pack(const unsigned long long* keys, const uint32_t* star
 
 cudaError_t launch_run_fill(const unsigned long long* keys, const uint32_t* ids, uint64_t n, const uint32_t* runOf,
                             const uint32_t* start, uint32_t runs, const unsigned long long* packedScan, int maxValues,
-                            uint32_t* values, Slot* fin, uint32_t finMask, cudaStream_t s, uint32_t* rawAll) {
-    run_values_kernel<<<grid_of(n), 256, 0, s>>>(keys, ids, n, runOf, start, packedScan, maxValues, values, rawAll);
+                            uint32_t* values, Slot* fin, uint32_t finMask, cudaStream_t s, uint32_t* rawAll,
+                            uint32_t idMask) {
+    run_values_kernel<<<grid_of(n), 256, 0, s>>>(keys, ids, n, runOf, start, packedScan, maxValues, values, rawAll,
+                                                 idMask);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     run_place_kernel<<<grid_of(runs), 256, 0, s>>>(keys, start, runs, packedScan, maxValues, fin, finMask);
