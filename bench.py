@@ -72,13 +72,13 @@ WINDOW = 4_194_304  # anchors per step
 # DRAM bytes (read + write) of align_lane_kernel per candidate, its warp
 # instructions per candidate and its ALU pipe activity, measured by ncu on one
 # 65536-anchor launch of the 100M-read workload's shape at 20 Mbp
-# (profiles/top3_kernels_c4_shape_20mbp.md: 624.8 MB and 9.08779e8 warp
-# instructions for the launch's 3.3555M candidates, ALU pipe 84.7% active).
+# (profiles/align_lane_kernel_c4_shape_20mbp.md: 738.1 MB and 7.67810e8 warp
+# instructions for the launch's 3.3555M candidates, ALU pipe 84.9% active).
 # On the 2M-read workload with repeats the DRAM bytes per candidate are far
 # fewer (candidates shared by the anchors of a batch hit in L2 there).
-ALIGN_DRAM_BYTES_PER_CANDIDATE = 624.8e6 / 3.3555e6
-ALIGN_WARP_INST_PER_CANDIDATE = 9.08779e8 / 3.3555e6
-ALIGN_ALU_PIPE_ACTIVE = 0.847
+ALIGN_DRAM_BYTES_PER_CANDIDATE = 738.1e6 / 3.3555e6
+ALIGN_WARP_INST_PER_CANDIDATE = 7.67810e8 / 3.3555e6
+ALIGN_ALU_PIPE_ACTIVE = 0.849
 # STEP2 speed of the oracle (the port) over the reference's own build, both on
 # 8 threads of an Intel Xeon @ 2.70 GHz, 2M-read 150 bp workload with repeats,
 # outputs byte-identical (python oracle/port_speed.py --threads 8): the port
@@ -504,7 +504,7 @@ def main():
                            "warp_instructions_per_candidate": ALIGN_WARP_INST_PER_CANDIDATE,
                            "alu_pipe_active_ncu": ALIGN_ALU_PIPE_ACTIVE,
                            "source": "smsp__inst_executed.sum per candidate from ncu "
-                                     "(profiles/top3_kernels_c4_shape_20mbp.md) x candidates of an average launch"}
+                                     "(profiles/align_lane_kernel_c4_shape_20mbp.md) x candidates of an average launch"}
         return roof
 
     clk = ClockSampler(local, paused=True)
