@@ -248,8 +248,8 @@ struct cg_ctx {
     uint64_t n = 0;
     int lmax = 0, pitch = 0, wp = 0, k = 20, nmaps = 48, maxValuesPerKey = 75;
     DevBuf enc, len, hilo, qual, ambig, sig;
-    // strand bits of every read's minima (u16 [ceil(maps / 16)][N]) and the
-    // read ids in the tables' buckets tagged with them: fewer than 2^31 reads
+    // strand bits of every read's minima in maps 0-15 (u16 [N]) and the read
+    // ids in those maps' buckets tagged with them: fewer than 2^31 reads
     DevBuf strand;
     bool strandTags = false;
     std::vector<MapTable> maps;    // views into tableSlabs
@@ -495,7 +495,7 @@ int build_tables(cg_ctx* c) {
     c->strandTags = n <= 0x7fffffffull;
     uint16_t* strand = nullptr;
     if (c->strandTags) {
-        CG_CUDA(c, c->strand.ensure((size_t)((c->nmaps + 15) / 16) * n * sizeof(uint16_t)));
+        CG_CUDA(c, c->strand.ensure((size_t)n * sizeof(uint16_t)));
         strand = c->strand.as<uint16_t>();
     }
     CG_CUDA(c, launch_signatures(st, c->k, c->nmaps, c->sig.as<unsigned long long>(), strand, c->stream));
@@ -572,8 +572,7 @@ int build_tables(cg_ctx* c) {
             const unsigned long long* keys = c->sig.as<unsigned long long>() + (uint64_t)h * n;
             cudaError_t e = radix_sort_pairs(keys, n, bits, l.keys.as<unsigned long long>(), l.ids.as<uint32_t>(),
                                              l.keysAlt.as<unsigned long long>(), l.idsAlt.as<uint32_t>(),
-                                             l.sortTmp.p, l.stream, strand ? strand + (uint64_t)(h >> 4) * n : nullptr,
-                                             h & 15);
+                                             l.sortTmp.p, l.stream, h < 16 ? strand : nullptr, h);
             if (e == cudaSuccess) e = launch_run_heads(l.keys.as<unsigned long long>(), n, l.runOf.as<uint32_t>(),
                                                        l.stream);
             if (e == cudaSuccess) e = scan_exclusive_u32(l.runOf.as<uint32_t>(), n + 1, l.scanTmp.p, l.stream);

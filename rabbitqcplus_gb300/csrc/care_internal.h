@@ -44,9 +44,10 @@ struct TablesArg {
     uint32_t mask[kMaxMaps];
     int nmaps;
     int maxValuesPerKey;
-    // With strand set (fewer than 2^31 reads): bit 31 of every bucket value is
-    // the value read's strand bit for that map (launch_signatures), the read id
-    // is the low 31 bits, and strand[g][anchor] holds the anchor's bits.
+    // With strand set (fewer than 2^31 reads): the read id is the low 31 bits
+    // of every bucket value; in maps 0-15 bit 31 is the value read's strand bit
+    // for that map (launch_signatures) and strand[anchor] holds the anchor's
+    // bits (zero elsewhere: no prediction).
     const uint16_t* strand;
 };
 
@@ -142,9 +143,9 @@ cudaError_t launch_encode(const char* chars, const uint64_t* offs, const char* q
                           uint32_t* enc, uint16_t* len, uint8_t* qual, uint8_t* ambig, int pitch, int lmax,
                           cudaStream_t s);
 cudaError_t launch_hilo(StoreArg st, uint32_t* hilo, cudaStream_t s);
-// sig[maps][N]; with strand set also strand[ceil(maps / 16)][N], bit q of
-// strand[g][r] = map 16 g + q's minimum of read r came from a reverse
-// complement canonical k-mer
+// sig[maps][N]; with strand set also strand[N], bit q of strand[r] = map
+// q's minimum of read r came from a reverse complement canonical k-mer (maps
+// 0-15)
 cudaError_t launch_signatures(StoreArg st, int k, int nmaps, unsigned long long* sig, uint16_t* strand,
                               cudaStream_t s);
 // out[0] = shortest, out[1] = longest read of the store (out preset to {~0, 0})

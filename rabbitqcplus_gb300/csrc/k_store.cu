@@ -225,11 +225,12 @@ __global__ void hilo_kernel(StoreArg st, uint32_t* __restrict__ hilo) {
 
 // Signatures: one thread per (read, group of 16 maps); threads of a warp take
 // consecutive reads of the same group so the map-major stores coalesce.
-// With `strand`, bit q of strand[g][read] tells whether map 16 g + q's
-// minimum came from a k-mer whose canonical form is its reverse complement:
-// two reads that share that minimum overlap in the same orientation when
-// their bits agree, which the alignment uses to choose which orientation to
-// scan first (a prediction only: the result does not depend on it).
+// With `strand`, bit q of strand[read] tells whether map q's minimum (maps
+// 0-15 only) came from a k-mer whose canonical form is its reverse
+// complement: two reads that share that minimum overlap in the same
+// orientation when their bits agree, which the alignment uses to choose which
+// orientation to scan first (a prediction only: the result does not depend on
+// it).  The threads of the other maps skip the bookkeeping.
 constexpr int kSigReads = 128;
 constexpr int kSigGroup = 16;
 
@@ -245,6 +246,7 @@ __global__ void __launch_bounds__(kSigReads * 3) signature_kernel(StoreArg st, i
 #pragma unroll
     for (int j = 0; j < kSigGroup; j++) mins[j] = ~0ull;
     uint32_t sb = 0;  // strand bit of each map's minimum
+    const bool track = strand && g == 0;
     const int L = st.len[r];
     if (L >= k) {
         const uint32_t* e = st.enc + r * (uint64_t)st.pitch;
@@ -259,13 +261,21 @@ __global__ void __launch_bounds__(kSigReads * 3) signature_kernel(StoreArg st, i
                 rc = (rc >> 2) | ((3ull - bb) << rcShift);
                 if (w * 16 + j >= k - 1) {
                     const uint64_t canon = fwd < rc ? fwd : rc;
-                    const uint32_t rcBits = rc < fwd ? 0xffffu : 0u;
+                    if (track) {  // the same for every thread of a warp
+                        const uint32_t rcBits = rc < fwd ? 0xffffu : 0u;
 #pragma unroll
-                    for (int q = 0; q < kSigGroup; q++) {
-                        const uint64_t hv = murmur64(canon + (uint64_t)(m0 + q));
-                        if (hv < mins[q]) {
-                            mins[q] = hv;
-                            sb = (sb & ~(1u << q)) | (rcBits & (1u << q));
+                        for (int q = 0; q < kSigGroup; q++) {
+                            const uint64_t hv = murmur64(canon + (uint64_t)(m0 + q));
+                            const bool lower = hv < mins[q];
+                            mins[q] = lower ? hv : mins[q];
+                            const uint32_t m = lower ? 1u << q : 0u;  // bit q takes this k-mer's strand
+                            sb = (sb & ~m) | (rcBits & m);
+                        }
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < kSigGroup; q++) {
+                            const uint64_t hv = murmur64(canon + (uint64_t)(m0 + q));
+                            mins[q] = hv < mins[q] ? hv : mins[q];
                         }
                     }
                 }
@@ -276,7 +286,7 @@ __global__ void __launch_bounds__(kSigReads * 3) signature_kernel(StoreArg st, i
     for (int q = 0; q < kSigGroup; q++) {
         if (m0 + q < nmaps) sig[(uint64_t)(m0 + q) * st.n + r] = mins[q] & kmask;
     }
-    if (strand) strand[(uint64_t)g * st.n + r] = (uint16_t)sb;
+    if (track) strand[r] = (uint16_t)sb;
 }
 
 }  // namespace

@@ -245,12 +245,14 @@ __device__ void gather_one(const StoreArg& st, const TablesArg& tb, const Params
     constexpr int kGroup = 16, kGroups = kGatherThreads / kGroup, kMapsPer = (kMaxMaps + kGroups - 1) / kGroups;
     const int g = tid / kGroup, gl = tid % kGroup;
     // this thread's maps g + k kGroups: bit k = the anchor's strand bit there
+    // (maps 0-15 only; the others carry no prediction)
     uint32_t aStrand = 0;
     if (tagged) {
+        const uint32_t bits = tb.strand[aid];
 #pragma unroll
         for (int k = 0; k < kMapsPer; k++) {
             const int m = g + k * kGroups;
-            if (m < tb.nmaps) aStrand |= (((uint32_t)tb.strand[(uint64_t)(m >> 4) * st.n + aid] >> (m & 15)) & 1u) << k;
+            if (m < 16) aStrand |= ((bits >> m) & 1u) << k;
         }
     }
     __syncthreads();
