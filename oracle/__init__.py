@@ -73,6 +73,7 @@ def lib() -> ctypes.CDLL:
         L.orc_candidates.argtypes = [P, ctypes.c_uint64, P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
         L.orc_correct.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, P, P, ctypes.c_size_t, ctypes.c_int, P]
         L.orc_load_forest.argtypes = [P, P, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_float]
+        L.orc_check_orientation_shortcut.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, P]
         _lib = L
     return _lib
 
@@ -115,6 +116,16 @@ class Oracle:
         cnt = ctypes.c_uint32()
         assert self._L.orc_candidates(self._h, anchor, out.ctypes.data, cap, ctypes.byref(cnt)) == 0
         return out[:cnt.value].copy()
+
+    def check_orientation_shortcut(self, first: int, count: int, threads: int | None = None) -> dict:
+        """(candidate, orientation scanned first) cases of anchors [first,
+        first + count), how many the device alignment's one-plane shortcut
+        decides, and how many of those the reference's rule decides otherwise
+        (oracle/care_oracle.cpp: orc_check_orientation_shortcut)."""
+        out = np.zeros(3, dtype=np.uint64)
+        assert self._L.orc_check_orientation_shortcut(self._h, first, count, threads or self.threads,
+                                                        out.ctypes.data) == 0
+        return {"cases": int(out[0]), "decided": int(out[1]), "wrong": int(out[2])}
 
     def correct(self, first: int = 0, count: int | None = None, threads: int | None = None):
         """Returns (flags[count], corrected[count, max_length], counters[8]).  With

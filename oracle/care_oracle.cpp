@@ -1053,6 +1053,74 @@ int orc_candidates(void* h, uint64_t anchor, uint32_t* out, uint32_t cap, uint32
     return 0;
 }
 
+// Check of the device alignment's orientation shortcut (not part of the
+// reference: the GPU kernel align_lane_kernel scans one orientation first and
+// skips the other where a one-plane test rules out a tie).  For every
+// candidate of the anchors [first, first + count) and for each orientation
+// taken as the one scanned first: the shortcut decides when that
+// orientation's result would be chosen on its own (choose it against an
+// invalid other), the minimum overlap is at least 32, and no shift of the
+// other orientation with at least that overlap has at most L = floor(nOps *
+// min(La, Lc) / overlap) + 1 hi-plane mismatches in its overlap's first 32
+// bases.  out[0] = (candidate, first orientation) cases, out[1] = cases the
+// shortcut decides, out[2] = decided cases where the reference's choice from
+// both scans differs from the first orientation (the shortcut's claim: 0).
+int orc_check_orientation_shortcut(void* h, uint64_t first, uint64_t count, int threads, uint64_t* out) {
+    const Oracle* O = static_cast<Oracle*>(h);
+    const Store& s = O->s;
+    const cg_options& o = O->o;
+    if (first + count > s.n) return CG_ERR_INVALID_ARGUMENT;
+    auto bits32 = [&](const uint32_t* p, int sh) {  // bases sh .. sh + 31 of a plane
+        const int w = sh >> 5, b = sh & 31;
+        return b ? (p[w] << b) | (p[w + 1] >> (32 - b)) : p[w];
+    };
+    uint64_t cases = 0, decided = 0, wrong = 0;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(threads) reduction(+ : cases, decided, wrong)
+    for (long long ai = 0; ai < (long long)count; ai++) {
+        const uint64_t anchor = first + (uint64_t)ai;
+        std::vector<uint32_t> ids;
+        candidates(*O, anchor, ids, nullptr);
+        const int La = s.len[anchor];
+        const uint32_t* aHi = s.planes(anchor, false);
+        const int minov = std::max(o.min_overlap, int(float(La) * o.min_overlap_ratio));
+        for (const uint32_t id : ids) {
+            const int Lc = s.len[id];
+            const uint32_t* pl[2] = {s.planes(id, false), s.planes(id, true)};
+            const Aln f = align(aHi, aHi + s.W, La, pl[0], pl[0] + s.W, Lc, o.min_overlap, o.max_error_rate,
+                                o.min_overlap_ratio);
+            const Aln r = align(aHi, aHi + s.W, La, pl[1], pl[1] + s.W, Lc, o.min_overlap, o.max_error_rate,
+                                o.min_overlap_ratio);
+            const float mer = o.estimated_errorrate * 4.0f;
+            const int ori = orientation(f, r, La, o.min_overlap_ratio, o.min_overlap, mer);
+            Aln none{};
+            none.isValid = false;
+            for (int po = 0; po < 2; po++) {
+                cases++;
+                const Aln& x1 = po == 0 ? f : r;
+                const int solo = po == 0 ? orientation(x1, none, La, o.min_overlap_ratio, o.min_overlap, mer)
+                                         : orientation(none, x1, La, o.min_overlap_ratio, o.min_overlap, mer);
+                if (solo == 3 || minov < 32) continue;
+                const int L = int((uint32_t(x1.nOps) * uint32_t(std::min(La, Lc))) / uint32_t(x1.overlap)) + 1;
+                const uint32_t* oHi = pl[1 - po];
+                bool close = false;
+                if (Lc >= minov)
+                    for (int sh = 0; sh <= La - minov && !close; sh++)
+                        close = __builtin_popcount(bits32(aHi, sh) ^ oHi[0]) <= L;
+                if (La >= minov)
+                    for (int sh = 1; sh <= Lc - minov && !close; sh++)
+                        close = __builtin_popcount(bits32(oHi, sh) ^ aHi[0]) <= L;
+                if (close) continue;
+                decided++;
+                if (ori != solo) wrong++;
+            }
+        }
+    }
+    out[0] = cases;
+    out[1] = decided;
+    out[2] = wrong;
+    return 0;
+}
+
 // Corrects anchors [first, first+count); flags and corrected sequences as in
 // cg_correct.  With candidate correction the range must be the whole read set
 // and the flags come out as cg_combine_results leaves them.  counters (8
